@@ -1,0 +1,193 @@
+"""GB300 FMM-BEM Helmholtz solver: Python front end over the C ABI of libfmmbem.so.
+
+The library is the product; this module only binds its entry points (``include/fmmbem.h``)
+with ctypes, mirroring the plan API one to one.  There is no CPU implementation behind it:
+if the CUDA library is missing or no GPU is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libfmmbem.so")
+
+FMM_FP64 = 0
+FMM_MIXED = 1
+RULE_GAUSS3 = 0
+RULE_DUNAVANT7 = 1
+MAX_LEVEL = 12
+
+_STATUS = {0: "FMM_OK", 1: "FMM_ERR_ARG", 2: "FMM_ERR_CUDA", 3: "FMM_ERR_ALLOC", 4: "FMM_ERR_IO",
+           5: "FMM_ERR_BREAKDOWN", 6: "FMM_ERR_NOT_CONVERGED", 7: "FMM_ERR_MESH"}
+
+
+class FmmError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (_STATUS.get(status, status), msg))
+        self.status = status
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("k", ctypes.c_double), ("depth", ctypes.c_int), ("s", ctypes.c_int),
+                ("p_level", ctypes.c_int * (MAX_LEVEL + 1)), ("eps", ctypes.c_double), ("rule", ctypes.c_int),
+                ("a_re", ctypes.c_double), ("a_im", ctypes.c_double), ("b_re", ctypes.c_double),
+                ("b_im", ctypes.c_double), ("c_re", ctypes.c_double), ("c_im", ctypes.c_double),
+                ("build_mixed", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("num_elem", ctypes.c_int), ("num_vert", ctypes.c_int), ("lmin", ctypes.c_int), ("lmax", ctypes.c_int),
+                ("d", ctypes.c_double), ("pt_min", ctypes.c_double * 3), ("p_level", ctypes.c_int * (MAX_LEVEL + 1)),
+                ("num_box", ctypes.c_int * (MAX_LEVEL + 1)), ("num_m2l", ctypes.c_longlong * (MAX_LEVEL + 1)),
+                ("num_near", ctypes.c_longlong), ("device_bytes", ctypes.c_size_t), ("setup_seconds", ctypes.c_double)]
+
+
+_lib = None
+c_vp = ctypes.c_void_p
+c_dp = ctypes.POINTER(ctypes.c_double)
+c_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def lib():
+    """Load libfmmbem.so; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FmmError(2, "CUDA library %s not built (run __graft_entry__.build())" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        L.fmm_default_options.argtypes = [ctypes.POINTER(Options)]
+        L.fmm_plan_create.argtypes = [c_dp, ctypes.c_int, c_ip, ctypes.c_int, ctypes.POINTER(Options), ctypes.POINTER(c_vp)]
+        L.fmm_plan_create_obj.argtypes = [ctypes.c_char_p, ctypes.POINTER(Options), ctypes.POINTER(c_vp)]
+        L.fmm_plan_destroy.argtypes = [c_vp]
+        L.fmm_plan_info.argtypes = [c_vp, ctypes.POINTER(Info)]
+        L.fmm_matvec.argtypes = [c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_int]
+        L.fmm_gmres.argtypes = [c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                c_ip, c_dp]
+        L.fmm_far_field.argtypes = [c_vp, c_vp, c_dp, ctypes.c_int, c_vp]
+        L.fmm_plane_wave_rhs.argtypes = [c_vp, c_dp, c_vp]
+        L.fmm_mesh_icosphere.argtypes = [ctypes.c_int, ctypes.c_double, c_dp, c_ip, c_ip, c_ip]
+        L.fmm_last_error.restype = ctypes.c_char_p
+        L.fmm_set_profiling.argtypes = [c_vp, ctypes.c_int]
+        L.fmm_last_timings.argtypes = [c_vp, ctypes.POINTER(ctypes.c_char_p), c_dp, c_ip]
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != 0:
+        raise FmmError(status, lib().fmm_last_error().decode(errors="replace"))
+
+
+def default_options():
+    o = Options()
+    lib().fmm_default_options(ctypes.byref(o))
+    return o
+
+
+def icosphere(subdiv, radius):
+    """Library mesh generator (``fmm_mesh_icosphere``)."""
+    nv, nf = ctypes.c_int(), ctypes.c_int()
+    _check(lib().fmm_mesh_icosphere(subdiv, radius, None, ctypes.byref(nv), None, ctypes.byref(nf)))
+    V = np.zeros((nv.value, 3))
+    F = np.zeros((nf.value, 3), dtype=np.int32)
+    _check(lib().fmm_mesh_icosphere(subdiv, radius, V.ctypes.data_as(c_dp), ctypes.byref(nv), F.ctypes.data_as(c_ip),
+                                    ctypes.byref(nf)))
+    return V, F
+
+
+def _ptr(a):
+    """Raw pointer of a numpy array or a torch tensor (host or device)."""
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Plan:
+    """A solver plan for one mesh and wavenumber (``fmm_plan_create``)."""
+
+    def __init__(self, V=None, F=None, k=1.0, depth=0, s=5, p_levels=None, eps=0.05, rule=RULE_GAUSS3,
+                 a=0.0, b=1.0, c=0.0, build_mixed=True, obj=None, device=0):
+        o = default_options()
+        o.k, o.depth, o.s, o.eps, o.rule = k, depth, s, eps, rule
+        a, b, c = complex(a), complex(b), complex(c)
+        o.a_re, o.a_im, o.b_re, o.b_im, o.c_re, o.c_im = a.real, a.imag, b.real, b.imag, c.real, c.imag
+        o.build_mixed = 1 if build_mixed else 0
+        o.device = device
+        if p_levels is not None:
+            for l, p in p_levels.items() if isinstance(p_levels, dict) else enumerate(p_levels):
+                o.p_level[l] = int(p)
+        h = c_vp()
+        if obj is not None:
+            _check(lib().fmm_plan_create_obj(obj.encode(), ctypes.byref(o), ctypes.byref(h)))
+        else:
+            V = np.ascontiguousarray(V, dtype=np.float64)
+            F = np.ascontiguousarray(F, dtype=np.int32)
+            _check(lib().fmm_plan_create(V.ctypes.data_as(c_dp), len(V), F.ctypes.data_as(c_ip), len(F),
+                                         ctypes.byref(o), ctypes.byref(h)))
+        self.h = h
+        self.info = self._info()
+        self.nf = self.info.num_elem
+
+    def _info(self):
+        i = Info()
+        _check(lib().fmm_plan_info(self.h, ctypes.byref(i)))
+        return i
+
+    def matvec(self, x, precision=FMM_FP64, out=None):
+        """y = A x.  x: complex128 numpy array (host) or torch tensor (host or CUDA)."""
+        if out is None:
+            if hasattr(x, "data_ptr"):
+                import torch
+                out = torch.empty_like(x)
+            else:
+                x = np.ascontiguousarray(x, dtype=np.complex128)
+                out = np.empty_like(x)
+        nrhs = (x.numel() if hasattr(x, "numel") else x.size) // self.nf
+        _check(lib().fmm_matvec(self.h, _ptr(x), _ptr(out), nrhs, precision))
+        return out
+
+    def gmres(self, b, x0=None, tol=1e-6, maxit=500, restart=50, precision=FMM_FP64):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.zeros_like(b) if x0 is None else np.ascontiguousarray(x0, dtype=np.complex128).copy()
+        it, rr = ctypes.c_int(), ctypes.c_double()
+        st = lib().fmm_gmres(self.h, _ptr(b), _ptr(x), tol, maxit, restart, precision, ctypes.byref(it), ctypes.byref(rr))
+        if st not in (0, 6):
+            _check(st)
+        return x, it.value, rr.value, st == 0
+
+    def far_field(self, p, pts):
+        p = np.ascontiguousarray(p, dtype=np.complex128)
+        pts = np.ascontiguousarray(pts, dtype=np.float64)
+        out = np.zeros(len(pts), dtype=np.complex128)
+        _check(lib().fmm_far_field(self.h, _ptr(p), pts.ctypes.data_as(c_dp), len(pts), _ptr(out)))
+        return out
+
+    def plane_wave(self, direction=(0.0, 0.0, 1.0)):
+        d = np.ascontiguousarray(direction, dtype=np.float64)
+        out = np.zeros(self.nf, dtype=np.complex128)
+        _check(lib().fmm_plane_wave_rhs(self.h, d.ctypes.data_as(c_dp), _ptr(out)))
+        return out
+
+    def set_profiling(self, on=True):
+        _check(lib().fmm_set_profiling(self.h, 1 if on else 0))
+
+    def timings(self):
+        n = ctypes.c_int(64)
+        names = (ctypes.c_char_p * 64)()
+        ms = (ctypes.c_double * 64)()
+        _check(lib().fmm_last_timings(self.h, names, ms, ctypes.byref(n)))
+        return [(names[i].decode(), ms[i]) for i in range(n.value)]
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().fmm_plan_destroy(self.h)
+            self.h = c_vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,315 @@
+// The FMM matvec: P2M, M2M, M2L (+ fused L2L), L2P + near field.  Templated on the
+// arithmetic type: double for the plain path, float for the mixed-precision path.
+//
+// Every translation is rotation - coaxial - rotation (RCR) as in the reference
+// (transMatsVecsMul_SR_rcr, translation.cu:1864-1961): rotate by (phi, theta, 0), apply the
+// coaxial blocks for |t|, rotate back by (0, theta, phi).  The rotation matrix is
+// e^{i m alpha} e^{-i m' gamma} H_n^{m'm}(beta) (translation.cu:1221-1235), so one real
+// table H per direction serves both rotations and the phases are applied elementwise.
+// Each destination box is owned by one CTA that accumulates all its translations in shared
+// memory and writes once: no atomics, bit-reproducible sums.
+#include "plan.h"
+
+namespace fmm {
+
+__constant__ int c_dir_dist[NDIR];
+
+template <typename T> struct Cx;
+template <> struct Cx<double> { typedef double2 t; };
+template <> struct Cx<float> { typedef float2 t; };
+
+__device__ __forceinline__ void decode_nm(int i, int &n, int &m)
+{
+    int q = (int)sqrtf((float)i);
+    while (q * q > i) q--;
+    while ((q + 1) * (q + 1) <= i) q++;
+    n = q;
+    m = i - q * q - q;
+}
+
+__device__ __forceinline__ float2 to_c(double2 v, float) { return make_float2((float)v.x, (float)v.y); }
+__device__ __forceinline__ double2 to_c(double2 v, double) { return v; }
+__device__ __forceinline__ double2 to_d(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ double2 to_d(double2 v) { return v; }
+
+// One RCR translation by a whole CTA.  x has pin^2 entries (zero padded to p); the result
+// for n < pout is accumulated into sY.  H and ph are the direction's real rotation table
+// (stride rot_size(pmax), prefix order p) and phases e^{i m phi} indexed m + pmax - 1.
+template <typename T>
+__device__ void rcr_block(int p, int pmax, const T *__restrict__ H, const typename Cx<T>::t *__restrict__ ph,
+                          const typename Cx<T>::t *__restrict__ Cc, const typename Cx<T>::t *__restrict__ xin, int pin,
+                          typename Cx<T>::t *sX, typename Cx<T>::t *sW1, typename Cx<T>::t *sW2,
+                          typename Cx<T>::t *sY, int pout)
+{
+    typedef typename Cx<T>::t C;
+    const int pp = p * p, pin2 = pin * pin, tid = threadIdx.x, nt = blockDim.x, off = pmax - 1;
+    for (int i = tid; i < pp; i += nt) {
+        int n, m;
+        decode_nm(i, n, m);
+        C v = (i < pin2) ? xin[i] : mk2((T)0, (T)0);
+        sX[i] = cmul(v, ph[m + off]);
+    }
+    __syncthreads();
+    for (int i = tid; i < pp; i += nt) {
+        int n, mp;
+        decode_nm(i, n, mp);
+        const T *col = H + rot_off(n) + (mp + n);
+        const int w = 2 * n + 1, base = n * n;
+        T ar = 0, ai = 0;
+        for (int m = 0; m < w; m++) {
+            T h = col[m * w];
+            C v = sX[base + m];
+            ar += h * v.x;
+            ai += h * v.y;
+        }
+        sW1[i] = mk2(ar, ai);
+    }
+    __syncthreads();
+    for (int i = tid; i < pp; i += nt) {
+        int np, m;
+        decode_nm(i, np, m);
+        int am = m < 0 ? -m : m, sz = p - am;
+        const C *col = Cc + coax_off(p, am) + (np - am);
+        T ar = 0, ai = 0;
+        for (int n = am; n < p; n++) {
+            C c = col[(n - am) * sz];
+            C v = sW1[n * n + n + m];
+            ar += c.x * v.x - c.y * v.y;
+            ai += c.x * v.y + c.y * v.x;
+        }
+        sW2[i] = mk2(ar, ai);
+    }
+    __syncthreads();
+    const int po2 = pout * pout;
+    for (int i = tid; i < po2; i += nt) {
+        int n, mp;
+        decode_nm(i, n, mp);
+        const T *col = H + rot_off(n) + (mp + n);
+        const int w = 2 * n + 1, base = n * n;
+        T ar = 0, ai = 0;
+        for (int m = 0; m < w; m++) {
+            T h = col[m * w];
+            C v = sW2[base + m];
+            ar += h * v.x;
+            ai += h * v.y;
+        }
+        C e = ph[mp + off];
+        // conj(e) * (ar + i ai)
+        C y = sY[i];
+        y.x += e.x * ar + e.y * ai;
+        y.y += e.x * ai - e.y * ar;
+        sY[i] = y;
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *__restrict__ leaf_elem,
+                           const typename Cx<T>::t *__restrict__ U, const double2 *__restrict__ x, double k,
+                           typename Cx<T>::t *__restrict__ Cm)
+{
+    typedef typename Cx<T>::t C;
+    int b = blockIdx.x, ppl = pl * pl;
+    int s0 = leaf_beg[b], s1 = leaf_beg[b + 1];
+    for (int i = threadIdx.x; i < ppl; i += blockDim.x) {
+        T ar = 0, ai = 0;
+        for (int s = s0; s < s1; s++) {
+            int e = leaf_elem[s];
+            double2 xe = x[e];
+            T xr = (T)(-k * xe.y), xi = (T)(k * xe.x); // i k x_e
+            C u = U[(size_t)e * ppl + i];
+            ar += xr * u.x - xi * u.y;
+            ai += xr * u.y + xi * u.x;
+        }
+        Cm[(size_t)b * ppl + i] = mk2(ar, ai);
+    }
+}
+
+template <typename T>
+__global__ void m2m_kernel(int pp, int pc, int pmax, const int *__restrict__ child_beg, const int *__restrict__ child_list,
+                           const unsigned char *__restrict__ octant, const T *__restrict__ Hss,
+                           const typename Cx<T>::t *__restrict__ PHss, const typename Cx<T>::t *__restrict__ Crr,
+                           const typename Cx<T>::t *__restrict__ Cchild, typename Cx<T>::t *__restrict__ Cpar)
+{
+    typedef typename Cx<T>::t C;
+    extern __shared__ unsigned char smraw[];
+    C *sX = (C *)smraw;
+    int P2 = pp * pp;
+    C *sW1 = sX + P2, *sW2 = sW1 + P2, *sY = sW2 + P2;
+    int q = blockIdx.x, rs = rot_size(pmax), w = 2 * pmax - 1;
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) sY[i] = mk2((T)0, (T)0);
+    __syncthreads();
+    for (int s = child_beg[q]; s < child_beg[q + 1]; s++) {
+        int ch = child_list[s], o = octant[ch];
+        rcr_block<T>(pp, pmax, Hss + (size_t)o * rs, PHss + (size_t)o * w, Crr, Cchild + (size_t)ch * pc * pc, pc,
+                     sX, sW1, sW2, sY, pp);
+    }
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) Cpar[(size_t)q * P2 + i] = sY[i];
+}
+
+template <typename T>
+__global__ void m2l_kernel(int p, int pmax, int pp, const int *__restrict__ sr_beg, const int *__restrict__ sr_src,
+                           const short *__restrict__ sr_dir, const T *__restrict__ Hsr,
+                           const typename Cx<T>::t *__restrict__ PHsr, const typename Cx<T>::t *__restrict__ Csr,
+                           const typename Cx<T>::t *__restrict__ Cm, const int *__restrict__ parent,
+                           const unsigned char *__restrict__ octant, const T *__restrict__ Hrr,
+                           const typename Cx<T>::t *__restrict__ PHrr, const typename Cx<T>::t *__restrict__ Crr,
+                           const typename Cx<T>::t *__restrict__ Dpar, typename Cx<T>::t *__restrict__ Dl)
+{
+    typedef typename Cx<T>::t C;
+    extern __shared__ unsigned char smraw[];
+    int pe = pp > p ? pp : p, E2 = pe * pe, P2 = p * p;
+    C *sX = (C *)smraw;
+    C *sW1 = sX + E2, *sW2 = sW1 + E2, *sY = sW2 + E2;
+    int b = blockIdx.x, rs = rot_size(pmax), w = 2 * pmax - 1, cs = coax_size(p);
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) sY[i] = mk2((T)0, (T)0);
+    __syncthreads();
+    if (pp > 0) {
+        // L2L: parent local (order pp) translated to this box, truncated to p
+        int o = octant[b];
+        rcr_block<T>(pp, pmax, Hrr + (size_t)o * rs, PHrr + (size_t)o * w, Crr, Dpar + (size_t)parent[b] * pp * pp, pp,
+                     sX, sW1, sW2, sY, p);
+    }
+    for (int s = sr_beg[b]; s < sr_beg[b + 1]; s++) {
+        int src = sr_src[s], dir = sr_dir[s];
+        rcr_block<T>(p, pmax, Hsr + (size_t)dir * rs, PHsr + (size_t)dir * w, Csr + (size_t)c_dir_dist[dir] * cs,
+                     Cm + (size_t)src * P2, p, sX, sW1, sW2, sY, p);
+    }
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) Dl[(size_t)b * P2 + i] = sY[i];
+}
+
+template <typename T>
+__global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_leaf, const typename Cx<T>::t *__restrict__ Dl,
+                                const typename Cx<T>::t *__restrict__ Rv, const int *__restrict__ near_beg,
+                                const int *__restrict__ near_col, const typename Cx<T>::t *__restrict__ nearv,
+                                const double2 *__restrict__ x, double2 a, double2 *__restrict__ y)
+{
+    typedef typename Cx<T>::t C;
+    int lane = threadIdx.x & 31;
+    int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (e >= nf) return;
+    int ppl = pl * pl;
+    T ar = 0, ai = 0;
+    for (int s = near_beg[e] + lane; s < near_beg[e + 1]; s += 32) {
+        C v = nearv[s];
+        double2 xd = x[near_col[s]];
+        T xr = (T)xd.x, xi = (T)xd.y;
+        ar += v.x * xr - v.y * xi;
+        ai += v.x * xi + v.y * xr;
+    }
+    const C *D = Dl + (size_t)elem_leaf[e] * ppl;
+    const C *R = Rv + (size_t)e * ppl;
+    for (int i = lane; i < ppl; i += 32) {
+        C d = D[i], r = R[i];
+        ar += d.x * r.x - d.y * r.y;
+        ai += d.x * r.y + d.y * r.x;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ar += __shfl_xor_sync(0xffffffffu, ar, o);
+        ai += __shfl_xor_sync(0xffffffffu, ai, o);
+    }
+    if (lane == 0) {
+        double2 xe = x[e];
+        y[e] = make_double2(a.x * xe.x - a.y * xe.y + (double)ar, a.x * xe.y + a.y * xe.x + (double)ai);
+    }
+}
+
+static inline int block_for(int p) { return p >= 16 ? 256 : 128; }
+
+static void timer_begin(Plan *P, const char *name)
+{
+    if (!P->profiling || P->ntimers >= MAX_TIMERS) return;
+    Timer &t = P->timers[P->ntimers];
+    t.name = name;
+    cudaEventRecord(t.beg, P->stream);
+}
+static void timer_end(Plan *P)
+{
+    if (!P->profiling || P->ntimers >= MAX_TIMERS) return;
+    cudaEventRecord(P->timers[P->ntimers].end, P->stream);
+    P->ntimers++;
+}
+
+template <typename T>
+static int run_matvec_t(Plan *P, const double2 *x, double2 *y)
+{
+    typedef typename Cx<T>::t C;
+    const bool f64 = sizeof(T) == 8;
+    int lmin = P->lmin, lmax = P->lmax, pmax = P->pmax;
+    cudaStream_t st = P->stream;
+    size_t smax = 4 * (size_t)pmax * pmax * sizeof(C);
+    static bool attr_done[2] = {false, false};
+    static size_t attr_bytes[2] = {0, 0};
+    int slot = f64 ? 0 : 1;
+    if (!attr_done[slot] || attr_bytes[slot] < smax) {
+        FMM_CUDA_TRY(cudaFuncSetAttribute(m2m_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+        FMM_CUDA_TRY(cudaFuncSetAttribute(m2l_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+        attr_done[slot] = true;
+        attr_bytes[slot] = smax;
+    }
+    P->ntimers = 0;
+    const T *Hsr = f64 ? (const T *)P->Hsr64 : (const T *)P->Hsr32;
+    const T *Hss = f64 ? (const T *)P->Hss64 : (const T *)P->Hss32;
+    const T *Hrr = f64 ? (const T *)P->Hrr64 : (const T *)P->Hrr32;
+    const C *PHsr = f64 ? (const C *)P->PHsr64 : (const C *)P->PHsr32;
+    const C *PHss = f64 ? (const C *)P->PHss64 : (const C *)P->PHss32;
+    const C *PHrr = f64 ? (const C *)P->PHrr64 : (const C *)P->PHrr32;
+    auto Cm = [&](int l) { return f64 ? (C *)P->lev[l].Cm64 : (C *)P->lev[l].Cm32; };
+    auto Dl = [&](int l) { return f64 ? (C *)P->lev[l].Dl64 : (C *)P->lev[l].Dl32; };
+    auto Csr = [&](int l) { return f64 ? (const C *)P->lev[l].Csr64 : (const C *)P->lev[l].Csr32; };
+    auto Crr = [&](int l) { return f64 ? (const C *)P->lev[l].Crr64 : (const C *)P->lev[l].Crr32; };
+    const C *U = f64 ? (const C *)P->U64 : (const C *)P->U32;
+    const C *Rv = f64 ? (const C *)P->Rv64 : (const C *)P->Rv32;
+    const C *nearv = f64 ? (const C *)P->near64 : (const C *)P->near32;
+    LevelDev &LL = P->lev[lmax];
+
+    timer_begin(P, "p2m");
+    p2m_kernel<T><<<LL.nb, 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, U, x, P->opt.k, Cm(lmax));
+    timer_end(P);
+    for (int l = lmax; l > lmin; l--) {
+        LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
+        size_t sm = 4 * (size_t)PL.p * PL.p * sizeof(C);
+        timer_begin(P, "m2m");
+        m2m_kernel<T><<<PL.nb, block_for(PL.p), sm, st>>>(PL.p, L.p, pmax, PL.child_beg, PL.child_list, L.octant, Hss,
+                                                           PHss, Crr(l), Cm(l), Cm(l - 1));
+        timer_end(P);
+    }
+    for (int l = lmin; l <= lmax; l++) {
+        LevelDev &L = P->lev[l];
+        int pp = l > lmin ? P->lev[l - 1].p : 0;
+        int pe = pp > L.p ? pp : L.p;
+        size_t sm = 4 * (size_t)pe * pe * sizeof(C);
+        timer_begin(P, "m2l+l2l");
+        m2l_kernel<T><<<L.nb, block_for(pe), sm, st>>>(L.p, pmax, pp, L.sr_beg, L.sr_src, L.sr_dir, Hsr, PHsr, Csr(l),
+                                                         Cm(l), L.parent, L.octant, Hrr, PHrr, l > lmin ? Crr(l) : nullptr,
+                                                         l > lmin ? Dl(l - 1) : nullptr, Dl(l));
+        timer_end(P);
+    }
+    timer_begin(P, "l2p+near");
+    double2 a = make_double2(P->opt.a_re, P->opt.a_im);
+    l2p_near_kernel<T><<<(P->nf * 32 + 255) / 256, 256, 0, st>>>(P->nf, LL.p, P->elem_leaf, Dl(lmax), Rv, P->near_beg,
+                                                                  P->near_col, nearv, x, a, y);
+    timer_end(P);
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
+int set_dir_dist(const int *dd)
+{
+    FMM_CUDA_TRY(cudaMemcpyToSymbol(c_dir_dist, dd, sizeof(int) * NDIR));
+    return FMM_OK;
+}
+
+int run_matvec(Plan *P, const double2 *x, double2 *y, int precision)
+{
+    if (precision == FMM_MIXED) {
+        if (!P->U32) {
+            fmm_set_error("plan was created without build_mixed");
+            return FMM_ERR_ARG;
+        }
+        return run_matvec_t<float>(P, x, y);
+    }
+    return run_matvec_t<double>(P, x, y);
+}
+
+} // namespace fmm

@@ -1,0 +1,95 @@
+// Internal plan layout shared by the translation units of libfmmbem.
+#pragma once
+#include "fmm_common.cuh"
+#include "octree_host.h"
+#include "../../include/fmmbem.h"
+#include <vector>
+
+namespace fmm {
+
+constexpr int NDIR = 316;      // M2L offsets (dx,dy,dz) in [-3,3]^3 with max |d| >= 2
+constexpr int NDIST = 15;      // distinct squared lengths of those offsets
+constexpr int MAX_TIMERS = 64;
+
+struct LevelDev {
+    int nb = 0, p = 0;
+    int *parent = nullptr;        // [nb], index in level l-1 (l > lmin)
+    unsigned char *octant = nullptr; // [nb], Morton digit of the box inside its parent
+    int *child_beg = nullptr;     // [nb+1] CSR over level l+1
+    int *child_list = nullptr;
+    int *sr_beg = nullptr;        // [nb+1] CSR of M2L sources by destination
+    int *sr_src = nullptr;        // source index in this level
+    short *sr_dir = nullptr;      // direction index 0..315
+    long long num_sr = 0;
+    double2 *Cm64 = nullptr, *Dl64 = nullptr;
+    float2 *Cm32 = nullptr, *Dl32 = nullptr;
+    double2 *Csr64 = nullptr;     // NDIST coaxial (S|R) blocks at order p
+    float2 *Csr32 = nullptr;
+    double2 *Crr64 = nullptr;     // coaxial (R|R) at order p_{l-1} for M2M into / L2L out of level l-1
+    float2 *Crr32 = nullptr;
+};
+
+struct Timer {
+    const char *name;
+    cudaEvent_t beg, end;
+};
+
+struct Plan {
+    fmm_options opt;
+    int nf = 0, nv = 0, lmin = 2, lmax = 0, pmax = 0, pleaf = 0;
+    HostTree tree;
+    std::vector<double> V;
+    std::vector<int> F;
+    LevelDev lev[FMM_MAX_LEVEL + 2];
+    // direction tables
+    int dir_slot[343];            // (dx+3)*49+(dy+3)*7+(dz+3) -> 0..315 or -1
+    int dir_dist[NDIR];           // direction -> distance slot
+    double *Hsr64 = nullptr, *Hss64 = nullptr, *Hrr64 = nullptr; // real rotation coefficients at pmax
+    float *Hsr32 = nullptr, *Hss32 = nullptr, *Hrr32 = nullptr;
+    double2 *PHsr64 = nullptr, *PHss64 = nullptr, *PHrr64 = nullptr; // e^{i m phi}, m = -(pmax-1)..pmax-1
+    float2 *PHsr32 = nullptr, *PHss32 = nullptr, *PHrr32 = nullptr;
+    // mesh and elements
+    double *V_dev = nullptr;
+    int *F_dev = nullptr;
+    int *elem_leaf = nullptr;     // leaf index per element
+    int *leaf_beg = nullptr, *leaf_elem = nullptr;
+    double2 *U64 = nullptr, *Rv64 = nullptr;   // P2M / L2P element tables [nf * pleaf^2]
+    float2 *U32 = nullptr, *Rv32 = nullptr;
+    int *near_beg = nullptr, *near_col = nullptr;
+    double2 *near64 = nullptr;
+    float2 *near32 = nullptr;
+    long long num_near = 0;
+    // work vectors
+    double2 *xbuf = nullptr, *ybuf = nullptr;
+    int nrhs_cap = 0;
+    cudaStream_t stream = nullptr;
+    size_t device_bytes = 0;
+    double setup_seconds = 0.0;
+    // profiling
+    int profiling = 0;
+    Timer timers[MAX_TIMERS];
+    int ntimers = 0, timers_created = 0;
+    // GMRES workspace
+    double2 *gm_V = nullptr, *gm_w = nullptr, *gm_r = nullptr, *gm_x = nullptr, *gm_b = nullptr, *gm_d = nullptr;
+    double2 *gm_dev_h = nullptr;
+    int gm_restart = 0;
+};
+
+// allocation tracking
+cudaError_t dev_alloc(Plan *P, void **ptr, size_t bytes);
+
+// tables.cu
+int gen_rotation_tables(Plan *P);
+int gen_coax_tables(Plan *P);
+int gen_element_tables(Plan *P);
+int gen_near_field(Plan *P);
+int launch_far_field(Plan *P, const double2 *p, const double *pts, int npts, double2 *out);
+int launch_plane_wave(Plan *P, const double *dir, double2 *rhs);
+
+// octree_gpu.cu
+int build_lists(Plan *P);
+
+// passes.cu
+int run_matvec(Plan *P, const double2 *x, double2 *y, int precision);
+
+} // namespace fmm

@@ -1,0 +1,667 @@
+// Setup kernels: rotation and coaxial translation tables, element moment tables for
+// P2M/L2P, the near-field matrix by quadrature, far-field evaluation.  All in FP64; the
+// mixed-precision path receives FP32 copies.
+#include "plan.h"
+#include <math.h>
+#include <vector>
+#include <algorithm>
+
+namespace fmm {
+
+// ----------------------------------------------------------------------------- quadrature
+// Regular rules: barycentric points and weights with  int_T f dS = J * sum_q w_q f(x_q),
+// J = |(n0-n2) x (n1-n2)|.  Rule 0 is the collapsed 3x3 Gauss rule of integral.cu:80-109
+// (weights 0.25 w_n w_m rho, points in the reference's loop order); rule 1 is Dunavant's
+// 7-point degree-5 rule (area = J/2).  CRULE holds the collapsed rule that also serves the
+// singular centroid split (integral.cu:202-249).
+__constant__ double c_rule_bary[2][16 * 3];
+__constant__ double c_rule_w[2][16];
+__constant__ int c_rule_n[2];
+
+static void gauss_legendre(int n, double *x, double *w)
+{
+    for (int i = 0; i < n; i++) {
+        double z = cos(FMM_PI * (i + 0.75) / (n + 0.5)), pp = 0.0;
+        for (int it = 0; it < 100; it++) {
+            double p1 = 1.0, p2 = 0.0;
+            for (int j = 1; j <= n; j++) {
+                double p3 = p2;
+                p2 = p1;
+                p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+            }
+            pp = n * (z * p1 - p2) / (z * z - 1.0);
+            double z1 = z;
+            z = z1 - p1 / pp;
+            if (fabs(z - z1) < 1e-16) break;
+        }
+        x[n - 1 - i] = z;
+        w[n - 1 - i] = 2.0 / ((1.0 - z * z) * pp * pp);
+    }
+}
+
+static int upload_rules()
+{
+    double bary[2][48] = {{0}}, w[2][16] = {{0}};
+    int n[2];
+    double x[3], wt[3];
+    gauss_legendre(3, x, wt);
+    int q = 0;
+    for (int i = 0; i < 3; i++) {
+        double theta = 0.5 + 0.5 * x[i];
+        for (int j = 0; j < 3; j++) {
+            double rho = 0.5 + 0.5 * x[j];
+            double xi1 = rho * (1 - theta), xi2 = rho - xi1, xi3 = 1 - xi1 - xi2;
+            bary[0][3 * q] = xi1; bary[0][3 * q + 1] = xi2; bary[0][3 * q + 2] = xi3;
+            w[0][q] = 0.25 * wt[i] * wt[j] * rho;
+            q++;
+        }
+    }
+    n[0] = q;
+    double s15 = sqrt(15.0);
+    double b1 = (6.0 - s15) / 21.0, a1 = 1.0 - 2.0 * b1, w1 = (155.0 - s15) / 1200.0;
+    double b2 = (6.0 + s15) / 21.0, a2 = 1.0 - 2.0 * b2, w2 = (155.0 + s15) / 1200.0;
+    double pts[7][3] = {{1.0 / 3, 1.0 / 3, 1.0 / 3}, {a1, b1, b1}, {b1, a1, b1}, {b1, b1, a1},
+                        {a2, b2, b2}, {b2, a2, b2}, {b2, b2, a2}};
+    double ww[7] = {9.0 / 40, w1, w1, w1, w2, w2, w2};
+    for (int t = 0; t < 7; t++) {
+        for (int a = 0; a < 3; a++) bary[1][3 * t + a] = pts[t][a];
+        w[1][t] = 0.5 * ww[t];
+    }
+    n[1] = 7;
+    FMM_CUDA_TRY(cudaMemcpyToSymbol(c_rule_bary, bary, sizeof(bary)));
+    FMM_CUDA_TRY(cudaMemcpyToSymbol(c_rule_w, w, sizeof(w)));
+    FMM_CUDA_TRY(cudaMemcpyToSymbol(c_rule_n, n, sizeof(n)));
+    return FMM_OK;
+}
+
+// ----------------------------------------------------------------------------- rotations
+// H_n^{m'm}(beta) of the reference (rotMatsInit + sparseRotMatGen, translation.cu:1064-1237)
+// evaluated from Wigner's d^n_{m'm}(beta) with the stable three-term recurrence in degree:
+//   j sqrt(((j+1)^2-m^2)((j+1)^2-m'^2)) d^{j+1} = (2j+1)(j(j+1)cos b - m m') d^j
+//                                               - (j+1) sqrt((j^2-m^2)(j^2-m'^2)) d^{j-1},
+// started at j0 = max(|m|,|m'|) from the one-term Wigner sum, and
+//   H = (-1)^{max(m',0)} (-1)^{max(-m,0)} d.
+// The reference's recurrence over m loses orthogonality in FP64 beyond p ~ 15.
+__device__ double wigner_start(int j, int mp, int m, double c, double s)
+{
+    int mu, sgn = 1;
+    if (m == j) mu = mp;
+    else if (mp == j) { mu = m; if ((m - j) & 1) sgn = -1; }
+    else if (m == -j) { mu = -mp; if ((-mp - j) & 1) sgn = -1; }
+    else mu = -m;
+    double binom = 1.0;
+    for (int i = 1; i <= j - mu; i++) binom = binom * (double)(j + mu + i) / (double)i;
+    double v = sqrt(binom);
+    for (int i = 0; i < j + mu; i++) v *= c;
+    for (int i = 0; i < j - mu; i++) v *= s;
+    return sgn * v;
+}
+
+__global__ void wigner_H_kernel(const double *betas, int p, double *H)
+{
+    int dir = blockIdx.y;
+    double beta = betas[dir];
+    double c = cos(0.5 * beta), s = sin(0.5 * beta), cb = cos(beta);
+    int w = 2 * p - 1, npair = w * w, rs = rot_size(p);
+    double *Hd = H + (size_t)dir * rs;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npair; t += gridDim.x * blockDim.x) {
+        int mp = t / w - (p - 1), m = t % w - (p - 1);
+        int amp = mp < 0 ? -mp : mp, am = m < 0 ? -m : m;
+        int j0 = amp > am ? amp : am;
+        double sign = ((((mp > 0) ? mp : 0) + ((m < 0) ? -m : 0)) & 1) ? -1.0 : 1.0;
+        double dprev = 0.0, dcur = wigner_start(j0, mp, m, c, s);
+        Hd[rot_off(j0) + (mp + j0) + (m + j0) * (2 * j0 + 1)] = sign * dcur;
+        for (int j = j0; j + 1 < p; j++) {
+            double dn;
+            if (j == 0) {
+                dn = cb * dcur;
+            } else {
+                double a = j * sqrt(((j + 1.0) * (j + 1.0) - (double)m * m) * ((j + 1.0) * (j + 1.0) - (double)mp * mp));
+                double b = (2.0 * j + 1.0) * (j * (j + 1.0) * cb - (double)m * mp);
+                double cc = (j + 1.0) * sqrt(((double)j * j - (double)m * m) * ((double)j * j - (double)mp * mp));
+                dn = (b * dcur - cc * dprev) / a;
+            }
+            dprev = dcur;
+            dcur = dn;
+            Hd[rot_off(j + 1) + (mp + j + 1) + (m + j + 1) * (2 * j + 3)] = sign * dcur;
+        }
+    }
+}
+
+__global__ void phase_kernel(const double *phis, int ndir, int p, double2 *PH)
+{
+    int w = 2 * p - 1;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ndir * w; t += gridDim.x * blockDim.x) {
+        int dir = t / w, m = t % w - (p - 1);
+        double s, c;
+        sincos(m * phis[dir], &s, &c);
+        PH[t] = make_double2(c, s);
+    }
+}
+
+__global__ void to_float_kernel(const double *in, float *out, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+static void to_float(const double *in, float *out, size_t n, cudaStream_t s)
+{
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    if (blocks < 1) blocks = 1;
+    to_float_kernel<<<blocks, 256, 0, s>>>(in, out, n);
+}
+
+int gen_rotation_tables(Plan *P)
+{
+    int p = P->pmax, rs = rot_size(p), w = 2 * p - 1;
+    std::vector<double> beta_sr(NDIR), phi_sr(NDIR), beta_ss(8), phi_ss(8), beta_rr(8), phi_rr(8);
+    int idx = 0;
+    for (int s = 0; s < 343; s++) {
+        int dx = s / 49 - 3, dy = (s / 7) % 7 - 3, dz = s % 7 - 3;
+        if (std::abs(dx) <= 1 && std::abs(dy) <= 1 && std::abs(dz) <= 1) { P->dir_slot[s] = -1; continue; }
+        double r = sqrt((double)(dx * dx + dy * dy + dz * dz));
+        beta_sr[idx] = acos(dz / r);
+        phi_sr[idx] = atan2((double)dy, (double)dx);
+        int s2 = dx * dx + dy * dy + dz * dz;
+        static const int s2list[NDIST] = {4, 5, 6, 8, 9, 10, 11, 12, 13, 14, 17, 18, 19, 22, 27};
+        int slot = -1;
+        for (int q = 0; q < NDIST; q++) if (s2list[q] == s2) slot = q;
+        P->dir_dist[idx] = slot;
+        P->dir_slot[s] = idx++;
+    }
+    for (int o = 0; o < 8; o++) {
+        double t[3] = {0.5 - ((o >> 2) & 1), 0.5 - ((o >> 1) & 1), 0.5 - (o & 1)};
+        double r = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+        beta_ss[o] = acos(t[2] / r);  // M2M: parent - child
+        phi_ss[o] = atan2(t[1], t[0]);
+        beta_rr[o] = acos(-t[2] / r); // L2L: child - parent
+        phi_rr[o] = atan2(-t[1], -t[0]);
+    }
+    double *dtmp = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&dtmp, sizeof(double) * (NDIR + 16) * 2));
+    std::vector<double> ball(NDIR + 16), pall(NDIR + 16);
+    for (int i = 0; i < NDIR; i++) { ball[i] = beta_sr[i]; pall[i] = phi_sr[i]; }
+    for (int o = 0; o < 8; o++) {
+        ball[NDIR + o] = beta_ss[o]; pall[NDIR + o] = phi_ss[o];
+        ball[NDIR + 8 + o] = beta_rr[o]; pall[NDIR + 8 + o] = phi_rr[o];
+    }
+    FMM_CUDA_TRY(cudaMemcpy(dtmp, ball.data(), sizeof(double) * (NDIR + 16), cudaMemcpyHostToDevice));
+    FMM_CUDA_TRY(cudaMemcpy(dtmp + NDIR + 16, pall.data(), sizeof(double) * (NDIR + 16), cudaMemcpyHostToDevice));
+    double *Hall = nullptr;
+    double2 *PHall = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&Hall, sizeof(double) * (size_t)(NDIR + 16) * rs));
+    FMM_CUDA_TRY(cudaMalloc(&PHall, sizeof(double2) * (size_t)(NDIR + 16) * w));
+    dim3 grid((w * w + 255) / 256, NDIR + 16);
+    wigner_H_kernel<<<grid, 256, 0, P->stream>>>(dtmp, p, Hall);
+    phase_kernel<<<((NDIR + 16) * w + 255) / 256, 256, 0, P->stream>>>(dtmp + NDIR + 16, NDIR + 16, p, PHall);
+    FMM_CUDA_TRY(cudaGetLastError());
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    // split into the three families (views into one allocation)
+    P->Hsr64 = Hall;
+    P->Hss64 = Hall + (size_t)NDIR * rs;
+    P->Hrr64 = Hall + (size_t)(NDIR + 8) * rs;
+    P->PHsr64 = PHall;
+    P->PHss64 = PHall + (size_t)NDIR * w;
+    P->PHrr64 = PHall + (size_t)(NDIR + 8) * w;
+    P->device_bytes += sizeof(double) * (size_t)(NDIR + 16) * rs + sizeof(double2) * (size_t)(NDIR + 16) * w;
+    if (P->opt.build_mixed) {
+        float *H32 = nullptr;
+        float2 *PH32 = nullptr;
+        FMM_CUDA_TRY(cudaMalloc(&H32, sizeof(float) * (size_t)(NDIR + 16) * rs));
+        FMM_CUDA_TRY(cudaMalloc(&PH32, sizeof(float2) * (size_t)(NDIR + 16) * w));
+        to_float(Hall, H32, (size_t)(NDIR + 16) * rs, P->stream);
+        to_float((const double *)PHall, (float *)PH32, (size_t)(NDIR + 16) * w * 2, P->stream);
+        P->Hsr32 = H32;
+        P->Hss32 = H32 + (size_t)NDIR * rs;
+        P->Hrr32 = H32 + (size_t)(NDIR + 8) * rs;
+        P->PHsr32 = PH32;
+        P->PHss32 = PH32 + (size_t)NDIR * w;
+        P->PHrr32 = PH32 + (size_t)(NDIR + 8) * w;
+        P->device_bytes += sizeof(float) * (size_t)(NDIR + 16) * rs + sizeof(float2) * (size_t)(NDIR + 16) * w;
+    }
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    cudaFree(dtmp);
+    return FMM_OK;
+}
+
+// ----------------------------------------------------------------------------- coaxial
+// (S|R) or (R|R) coaxial blocks for translation length t along z, following
+// sparseCoaxTransMatGen (translation.cu:678-771) with the initial column of
+// srCoaxTransMatsInit / rrCoaxTransMatsInit (translation.cu:555-584, 919-949) in FP64.
+// One CTA per matrix; E[m][n'][n] lives in a global scratch slice.  The diagonal
+// recurrence over m is sequential across the block; the n recurrence for each m is
+// independent and runs one warp per m.
+__global__ void coax_kernel(double k, const double *tvals, int p, int sr, double2 *scratch, double2 *out)
+{
+    int mat = blockIdx.x;
+    double t = tvals[mat];
+    int R = 2 * p - 1;
+    double2 *E = scratch + (size_t)mat * p * R * p;
+    double2 *C = out + (size_t)mat * coax_size(p);
+#define EE(m, np, n) E[((size_t)(m) * R + (np)) * p + (n)]
+    extern __shared__ double sh[];
+    double *jn = sh, *yn = sh + R;
+    if (threadIdx.x == 0) {
+        sph_jn_array(R, k * t, jn);
+        if (sr) sph_yn_array(R, k * t, yn);
+    }
+    __syncthreads();
+    for (int np = threadIdx.x; np < R; np += blockDim.x) {
+        double sg = (np & 1) ? -1.0 : 1.0, f = sg * sqrt(2.0 * np + 1.0);
+        EE(0, np, 0) = make_double2(f * jn[np], sr ? f * yn[np] : 0.0);
+    }
+    __syncthreads();
+    for (int m = 0; m + 1 <= p - 1; m++) {
+        double den = coefB(m + 1, -m - 1);
+        for (int np = m + 1 + threadIdx.x; np <= 2 * p - 2 - (m + 1); np += blockDim.x) {
+            double t0 = coefB(np, -m - 1) / den, t1 = coefB(np + 1, m) / den;
+            double2 a = EE(m, np - 1, m), b = EE(m, np + 1, m);
+            EE(m + 1, np, m + 1) = make_double2(t0 * a.x - t1 * b.x, t0 * a.y - t1 * b.y);
+        }
+        __syncthreads();
+    }
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int m = warp; m <= p - 2; m += nw) {
+        for (int n = m; n + 1 <= p - 1; n++) {
+            double den = coefA(n, m);
+            for (int np = m + lane; np <= 2 * p - 2 - (n + 1); np += 32) {
+                double t0 = coefA(np - 1, m) / den, t1 = coefA(np, m) / den, t2 = coefA(n - 1, m) / den;
+                double2 e0 = (np - 1 >= m) ? EE(m, np - 1, n) : make_double2(0.0, 0.0);
+                double2 e1 = EE(m, np + 1, n);
+                double2 e2 = (n - 1 >= m) ? EE(m, np, n - 1) : make_double2(0.0, 0.0);
+                EE(m, np, n + 1) = make_double2(t0 * e0.x - t1 * e1.x + t2 * e2.x, t0 * e0.y - t1 * e1.y + t2 * e2.y);
+            }
+            __threadfence_block();
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    for (int m = 0; m < p; m++) {
+        int sz = p - m, off = coax_off(p, m);
+        for (int i = threadIdx.x; i < sz * sz; i += blockDim.x) {
+            int a = i % sz, b = i / sz; // a = n'-m, b = n-m
+            C[off + i] = EE(m, m + a, m + b);
+        }
+    }
+#undef EE
+}
+
+int gen_coax_tables(Plan *P)
+{
+    double k = P->opt.k;
+    static const int s2list[NDIST] = {4, 5, 6, 8, 9, 10, 11, 12, 13, 14, 17, 18, 19, 22, 27};
+    size_t maxScratch = 0;
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        int p = P->lev[l].p;
+        maxScratch = std::max(maxScratch, (size_t)NDIST * p * (2 * p - 1) * p);
+        if (l > P->lmin) {
+            int pp = P->lev[l - 1].p;
+            maxScratch = std::max(maxScratch, (size_t)pp * (2 * pp - 1) * pp);
+        }
+    }
+    double2 *scratch = nullptr;
+    double *tdev = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&scratch, sizeof(double2) * maxScratch));
+    FMM_CUDA_TRY(cudaMalloc(&tdev, sizeof(double) * NDIST));
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        LevelDev &L = P->lev[l];
+        int p = L.p;
+        double size = P->tree.d * ldexp(1.0, -l);
+        double tv[NDIST];
+        for (int q = 0; q < NDIST; q++) tv[q] = sqrt((double)s2list[q]) * size;
+        FMM_CUDA_TRY(cudaMemcpy(tdev, tv, sizeof(tv), cudaMemcpyHostToDevice));
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Csr64, sizeof(double2) * NDIST * coax_size(p)));
+        coax_kernel<<<NDIST, 256, sizeof(double) * 2 * (2 * p - 1), P->stream>>>(k, tdev, p, 1, scratch, L.Csr64);
+        FMM_CUDA_TRY(cudaGetLastError());
+        FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+        if (P->opt.build_mixed) {
+            FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Csr32, sizeof(float2) * NDIST * coax_size(p)));
+            to_float((const double *)L.Csr64, (float *)L.Csr32, (size_t)2 * NDIST * coax_size(p), P->stream);
+        }
+        if (l > P->lmin) {
+            int pp = P->lev[l - 1].p;
+            double trr = 0.5 * sqrt(3.0) * size;
+            FMM_CUDA_TRY(cudaMemcpy(tdev, &trr, sizeof(double), cudaMemcpyHostToDevice));
+            FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Crr64, sizeof(double2) * coax_size(pp)));
+            coax_kernel<<<1, 256, sizeof(double) * 2 * (2 * pp - 1), P->stream>>>(k, tdev, pp, 0, scratch, L.Crr64);
+            FMM_CUDA_TRY(cudaGetLastError());
+            FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+            if (P->opt.build_mixed) {
+                FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Crr32, sizeof(float2) * coax_size(pp)));
+                to_float((const double *)L.Crr64, (float *)L.Crr32, (size_t)2 * coax_size(pp), P->stream);
+            }
+        }
+    }
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    cudaFree(scratch);
+    cudaFree(tdev);
+    return FMM_OK;
+}
+
+// ----------------------------------------------------------------------------- geometry
+__device__ __forceinline__ void load_tri(const double *V, const int *F, int e, double *nod)
+{
+    for (int t = 0; t < 3; t++) {
+        int v = F[3 * e + t];
+        nod[3 * t] = V[3 * v]; nod[3 * t + 1] = V[3 * v + 1]; nod[3 * t + 2] = V[3 * v + 2];
+    }
+}
+__device__ __forceinline__ void tri_centroid(const double *nod, double *y)
+{
+    for (int a = 0; a < 3; a++) {
+        double c23 = 0.5 * (nod[3 + a] + nod[6 + a]);
+        y[a] = nod[a] + (2.0 / 3.0) * (c23 - nod[a]);
+    }
+}
+__device__ __forceinline__ double tri_normal(const double *nod, double *nh)
+{
+    double u0 = nod[0] - nod[6], u1 = nod[1] - nod[7], u2 = nod[2] - nod[8];
+    double v0 = nod[3] - nod[6], v1 = nod[4] - nod[7], v2 = nod[5] - nod[8];
+    double n0 = u1 * v2 - u2 * v1, n1 = u2 * v0 - u0 * v2, n2 = u0 * v1 - u1 * v0;
+    double J = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+    nh[0] = n0 / J; nh[1] = n1 / J; nh[2] = n2 / J;
+    return J;
+}
+
+// G = exp(ikr)/(4 pi r) (integral.cu:72-78) and dG/dn_x (integral.cu:391-402)
+__device__ __forceinline__ double2 green_k(double k, const double *x, const double *y, const double *nh, int kern)
+{
+    double d0 = x[0] - y[0], d1 = x[1] - y[1], d2 = x[2] - y[2];
+    double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    double s, c;
+    sincos(k * r, &s, &c);
+    double inv = 1.0 / (4.0 * FMM_PI * r);
+    double gr = c * inv, gi = s * inv;
+    if (!kern) return make_double2(gr, gi);
+    double dn = (d0 * nh[0] + d1 * nh[1] + d2 * nh[2]) / r;
+    // g * (-1/r + i k) * dn
+    double ar = -1.0 / r, ai = k;
+    return make_double2((gr * ar - gi * ai) * dn, (gr * ai + gi * ar) * dn);
+}
+
+__device__ double2 elem_integral(double k, const double *nod, const double *y, int rule, int kern)
+{
+    double nh[3];
+    double J = tri_normal(nod, nh);
+    double2 acc = make_double2(0.0, 0.0);
+    int nq = c_rule_n[rule];
+    for (int q = 0; q < nq; q++) {
+        const double *b = &c_rule_bary[rule][3 * q];
+        double x[3];
+        for (int a = 0; a < 3; a++) x[a] = nod[a] * b[0] + nod[3 + a] * b[1] + nod[6 + a] * b[2];
+        double2 g = green_k(k, x, y, nh, kern);
+        double wq = c_rule_w[rule][q] * J;
+        acc.x += wq * g.x; acc.y += wq * g.y;
+    }
+    return acc;
+}
+
+__device__ double2 elem_integral_sgl(double k, const double *nod, int kern)
+{
+    double y[3];
+    tri_centroid(nod, y);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int s = 0; s < 3; s++) {
+        double sub[9];
+        int a0 = 3 * s, b0 = 3 * ((s + 1) % 3);
+        for (int t = 0; t < 3; t++) { sub[t] = nod[a0 + t]; sub[3 + t] = nod[b0 + t]; sub[6 + t] = y[t]; }
+        double2 part = elem_integral(k, sub, y, 0, kern);
+        acc.x += part.x; acc.y += part.y;
+    }
+    return acc;
+}
+
+// ----------------------------------------------------------------------------- element tables
+// U_e[n,m] = b int R_n^{-m}(x - c) dS + c int dR_n^{-m}/dn dS   (integral.cu:251-365, the P2M
+// moments of bottomLevelCoeff_L with its loop corrected), Rv_e[n,m] = R_n^m(y_e - c) (L2P).
+// One warp per element; the basis at each quadrature point is staged in shared memory.
+struct BasisSh {
+    double *jn, *Q;
+    double2 *ph;
+};
+
+__device__ __forceinline__ double2 basis_R(const BasisSh &B, int pb, int n, int m)
+{
+    // R_n^m = j_n Q_n^{|m|} e^{i m phi}; zero outside the valid range
+    if (n < 0 || n >= pb) return make_double2(0.0, 0.0);
+    int am = m < 0 ? -m : m;
+    if (am > n) return make_double2(0.0, 0.0);
+    double v = B.jn[n] * B.Q[n * (n + 1) / 2 + am];
+    double2 e = B.ph[m + pb];
+    return make_double2(v * e.x, v * e.y);
+}
+
+__device__ __forceinline__ void basis_prepare(const BasisSh &B, int pb, double k, const double *v, int lane)
+{
+    if (lane == 0) {
+        double r = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        double ct = 1.0, phi = 0.0;
+        if (r > 0.0) { ct = v[2] / r; phi = atan2(v[1], v[0]); }
+        sph_jn_array(pb, k * r, B.jn);
+        legendre_Q(pb, ct, B.Q);
+        for (int m = -pb; m <= pb; m++) {
+            double s, c;
+            sincos(m * phi, &s, &c);
+            B.ph[m + pb] = make_double2(c, s);
+        }
+    }
+    __syncwarp();
+}
+
+// per-warp shared memory (in doubles) of the element-table kernel: j_n and Q, padded to an
+// even count so the double2 phases that follow stay 16-byte aligned, then 2pb+1 phases
+__host__ __device__ __forceinline__ int basis_ph_offset(int pb) { return (pb + pb * (pb + 1) / 2 + 1) & ~1; }
+__host__ __device__ __forceinline__ int basis_per_warp(int pb) { return basis_ph_offset(pb) + 2 * (2 * pb + 1); }
+
+__global__ void element_tables_kernel(const double *V, const int *F, const int *elem_leaf, const double *box_ctr,
+                                      int nf, int pl, double k, double2 bco, double2 cco, int rule,
+                                      double2 *U, double2 *Rv)
+{
+    extern __shared__ double2 smem2[];
+    double *smem = (double *)smem2;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int pb = pl + 1;
+    double *base = smem + (size_t)warp * basis_per_warp(pb);
+    BasisSh B;
+    B.jn = base;
+    B.Q = base + pb;
+    B.ph = (double2 *)(base + basis_ph_offset(pb));
+    int ppl = pl * pl;
+    for (int e = blockIdx.x * nw + warp; e < nf; e += gridDim.x * nw) {
+        double nod[9], nh[3], c[3], y[3];
+        load_tri(V, F, e, nod);
+        double J = tri_normal(nod, nh);
+        int b = elem_leaf[e];
+        c[0] = box_ctr[3 * b]; c[1] = box_ctr[3 * b + 1]; c[2] = box_ctr[3 * b + 2];
+        double2 *Ue = U + (size_t)e * ppl;
+        for (int i = lane; i < ppl; i += 32) Ue[i] = make_double2(0.0, 0.0);
+        int nq = c_rule_n[rule];
+        for (int q = 0; q < nq; q++) {
+            const double *bb = &c_rule_bary[rule][3 * q];
+            double v[3];
+            for (int a = 0; a < 3; a++) v[a] = nod[a] * bb[0] + nod[3 + a] * bb[1] + nod[6 + a] * bb[2] - c[a];
+            double wq = c_rule_w[rule][q] * J;
+            __syncwarp();
+            basis_prepare(B, pb, k, v, lane);
+            for (int i = lane; i < ppl; i += 32) {
+                int n = (int)sqrt((double)i);
+                while (n * n > i) n--;
+                while ((n + 1) * (n + 1) <= i) n++;
+                int m = i - n * n - n;
+                int mm = -m; // moments use R_n^{-m}
+                double2 acc = make_double2(0.0, 0.0);
+                if (bco.x != 0.0 || bco.y != 0.0) {
+                    double2 r = basis_R(B, pb, n, mm);
+                    acc = cadd(acc, cmul(bco, r));
+                }
+                if (cco.x != 0.0 || cco.y != 0.0) {
+                    // directional derivative along nh (integral.cu:284-331)
+                    double2 t0 = csub(cscale(basis_R(B, pb, n + 1, mm + 1), coefB(n + 1, -(mm + 1))),
+                                      cscale(basis_R(B, pb, n - 1, mm + 1), coefB(n, mm)));
+                    double2 t1 = csub(cscale(basis_R(B, pb, n + 1, mm - 1), coefB(n + 1, mm - 1)),
+                                      cscale(basis_R(B, pb, n - 1, mm - 1), coefB(n, -mm)));
+                    double2 t2 = csub(cscale(basis_R(B, pb, n - 1, mm), coefA(n - 1, mm)),
+                                      cscale(basis_R(B, pb, n + 1, mm), coefA(n, mm)));
+                    double2 f0 = make_double2(0.5 * k * nh[0], -0.5 * k * nh[1]);
+                    double2 f1 = make_double2(0.5 * k * nh[0], 0.5 * k * nh[1]);
+                    double2 d = cadd(cadd(cmul(f0, t0), cmul(f1, t1)), cscale(t2, k * nh[2]));
+                    acc = cadd(acc, cmul(cco, d));
+                }
+                Ue[i] = cadd(Ue[i], cscale(acc, wq));
+            }
+            __syncwarp();
+        }
+        tri_centroid(nod, y);
+        double v[3] = {y[0] - c[0], y[1] - c[1], y[2] - c[2]};
+        basis_prepare(B, pb, k, v, lane);
+        double2 *Re = Rv + (size_t)e * ppl;
+        for (int i = lane; i < ppl; i += 32) {
+            int n = (int)sqrt((double)i);
+            while (n * n > i) n--;
+            while ((n + 1) * (n + 1) <= i) n++;
+            int m = i - n * n - n;
+            Re[i] = basis_R(B, pb, n, m);
+        }
+        __syncwarp();
+    }
+}
+
+int gen_element_tables(Plan *P)
+{
+    int st = upload_rules();
+    if (st != FMM_OK) return st;
+    int pl = P->pleaf;
+    LevelDev &L = P->lev[P->lmax];
+    // leaf box centres: descale(boxCenter) = d (2^-l x + 2^-(l+1)) + pt_min
+    std::vector<double> ctr(3 * L.nb);
+    double h = ldexp(1.0, -P->lmax), h2 = ldexp(1.0, -P->lmax - 1);
+    for (int i = 0; i < L.nb; i++) {
+        int x, y, z;
+        box_xyz(P->tree.sets[P->lmax][i], P->lmax, &x, &y, &z);
+        ctr[3 * i] = P->tree.d * (h * x + h2) + P->tree.pt_min[0];
+        ctr[3 * i + 1] = P->tree.d * (h * y + h2) + P->tree.pt_min[1];
+        ctr[3 * i + 2] = P->tree.d * (h * z + h2) + P->tree.pt_min[2];
+    }
+    double *ctr_dev = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&ctr_dev, sizeof(double) * ctr.size()));
+    FMM_CUDA_TRY(cudaMemcpy(ctr_dev, ctr.data(), sizeof(double) * ctr.size(), cudaMemcpyHostToDevice));
+    size_t tbl = (size_t)P->nf * pl * pl;
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->U64, sizeof(double2) * tbl));
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->Rv64, sizeof(double2) * tbl));
+    int pb = pl + 1;
+    int warps = 4;
+    size_t shm = (size_t)basis_per_warp(pb) * warps * sizeof(double);
+    if (shm > 48 * 1024) FMM_CUDA_TRY(cudaFuncSetAttribute(element_tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    int blocks = std::min((P->nf + warps - 1) / warps, 152 * 32);
+    double2 bco = make_double2(P->opt.b_re, P->opt.b_im), cco = make_double2(P->opt.c_re, P->opt.c_im);
+    element_tables_kernel<<<blocks, 32 * warps, shm, P->stream>>>(P->V_dev, P->F_dev, P->elem_leaf, ctr_dev, P->nf, pl,
+                                                                   P->opt.k, bco, cco, P->opt.rule, P->U64, P->Rv64);
+    FMM_CUDA_TRY(cudaGetLastError());
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    if (P->opt.build_mixed) {
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&P->U32, sizeof(float2) * tbl));
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&P->Rv32, sizeof(float2) * tbl));
+        to_float((const double *)P->U64, (float *)P->U32, 2 * tbl, P->stream);
+        to_float((const double *)P->Rv64, (float *)P->Rv32, 2 * tbl, P->stream);
+        FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    }
+    cudaFree(ctr_dev);
+    return FMM_OK;
+}
+
+// ----------------------------------------------------------------------------- near field
+// A_ij = b int_{T_j} G(x, y_i) dS + c int_{T_j} dG/dn_x(x, y_i) dS for source elements j in
+// the leaf boxes adjacent to (or equal to) the leaf box of target i; the self term uses the
+// centroid split.  One warp per target element, one lane per source element.
+__global__ void near_field_kernel(const double *V, const int *F, int nf, const int *near_beg, const int *near_col,
+                                  double k, double2 bco, double2 cco, int rule, double2 *out)
+{
+    int lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int nwt = (gridDim.x * blockDim.x) >> 5;
+    for (int i = warp; i < nf; i += nwt) {
+        double nodi[9], y[3];
+        load_tri(V, F, i, nodi);
+        tri_centroid(nodi, y);
+        for (int s = near_beg[i] + lane; s < near_beg[i + 1]; s += 32) {
+            int j = near_col[s];
+            double nod[9];
+            load_tri(V, F, j, nod);
+            double2 v = make_double2(0.0, 0.0);
+            bool sgl = (i == j);
+            if (bco.x != 0.0 || bco.y != 0.0) v = cadd(v, cmul(bco, sgl ? elem_integral_sgl(k, nod, 0) : elem_integral(k, nod, y, rule, 0)));
+            if (cco.x != 0.0 || cco.y != 0.0) v = cadd(v, cmul(cco, sgl ? elem_integral_sgl(k, nod, 1) : elem_integral(k, nod, y, rule, 1)));
+            out[s] = v;
+        }
+    }
+}
+
+int gen_near_field(Plan *P)
+{
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->near64, sizeof(double2) * (P->num_near + 1)));
+    double2 bco = make_double2(P->opt.b_re, P->opt.b_im), cco = make_double2(P->opt.c_re, P->opt.c_im);
+    int blocks = std::min((P->nf + 7) / 8, 152 * 16);
+    near_field_kernel<<<blocks, 256, 0, P->stream>>>(P->V_dev, P->F_dev, P->nf, P->near_beg, P->near_col, P->opt.k,
+                                                      bco, cco, P->opt.rule, P->near64);
+    FMM_CUDA_TRY(cudaGetLastError());
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    if (P->opt.build_mixed) {
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&P->near32, sizeof(float2) * (P->num_near + 1)));
+        to_float((const double *)P->near64, (float *)P->near32, 2 * (size_t)P->num_near, P->stream);
+        FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    }
+    return FMM_OK;
+}
+
+// ----------------------------------------------------------------------------- far field
+__global__ void far_field_kernel(const double *V, const int *F, int nf, double k, int rule, const double2 *p,
+                                 const double *pts, double2 *out)
+{
+    int t = blockIdx.x;
+    double y[3] = {pts[3 * t], pts[3 * t + 1], pts[3 * t + 2]};
+    double2 acc = make_double2(0.0, 0.0);
+    for (int j = threadIdx.x; j < nf; j += blockDim.x) {
+        double nod[9];
+        load_tri(V, F, j, nod);
+        acc = cadd(acc, cmul(p[j], elem_integral(k, nod, y, rule, 1)));
+    }
+    __shared__ double2 red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[t] = red[0];
+}
+
+int launch_far_field(Plan *P, const double2 *p, const double *pts, int npts, double2 *out)
+{
+    if (npts <= 0) return FMM_OK;
+    far_field_kernel<<<npts, 256, 0, P->stream>>>(P->V_dev, P->F_dev, P->nf, P->opt.k, P->opt.rule, p, pts, out);
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
+__global__ void plane_wave_kernel(const double *V, const int *F, int nf, double k, double dx, double dy, double dz,
+                                  double2 *rhs)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nf; e += gridDim.x * blockDim.x) {
+        double nod[9], y[3];
+        load_tri(V, F, e, nod);
+        tri_centroid(nod, y);
+        double s, c;
+        sincos(k * (dx * y[0] + dy * y[1] + dz * y[2]), &s, &c);
+        rhs[e] = make_double2(c, s);
+    }
+}
+
+int launch_plane_wave(Plan *P, const double *dir, double2 *rhs)
+{
+    plane_wave_kernel<<<(P->nf + 255) / 256, 256, 0, P->stream>>>(P->V_dev, P->F_dev, P->nf, P->opt.k, dir[0], dir[1],
+                                                                   dir[2], rhs);
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
+} // namespace fmm

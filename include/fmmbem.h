@@ -1,0 +1,119 @@
+/* fmmbem.h -- C ABI of the GB300 FMM-BEM Helmholtz solver (libfmmbem.so).
+ *
+ * One plan holds everything for one mesh and one wavenumber on one GPU: the octree
+ * (bit-exact with the reference's octree.c), the rotation and coaxial translation tables,
+ * the element moment tables for P2M/L2P, the near-field matrix, and device buffers for
+ * the FP64 and mixed-precision matvecs.  The operator is
+ *
+ *     y = a x + b L x + c M x,   (L x)_i = sum_j int_{T_j} G(x, y_i) x_j dS,
+ *                                (M x)_i = sum_j int_{T_j} dG/dn_x(x, y_i) x_j dS,
+ *
+ * with collocation at triangle centroids and one unknown per triangle (constant elements),
+ * G = exp(ik r)/(4 pi r).  The reference's OprL (translation.cu:3412) computes the far part
+ * of L only; fmm_matvec replaces it with the complete operator.  For a rigid (sound-hard)
+ * body the exterior Neumann problem is a = 1/2, b = 0, c = -1 with right-hand side p_inc.
+ *
+ * Complex arrays are cuDoubleComplex (re, im interleaved doubles).  Every entry point
+ * returns an fmm_status; FMM_OK is 0 (EXIT_SUCCESS).  Plans are not thread-safe: callers
+ * serialise calls on one plan.  Pointers may be host or device memory (checked with
+ * cudaPointerGetAttributes); host buffers are staged through the plan's pinned buffers.
+ */
+#ifndef FMMBEM_H
+#define FMMBEM_H
+#include <cuComplex.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    FMM_OK = 0,
+    FMM_ERR_ARG = 1,          /* invalid argument or size out of range */
+    FMM_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    FMM_ERR_ALLOC = 3,        /* host or device allocation failed */
+    FMM_ERR_IO = 4,           /* mesh file could not be read */
+    FMM_ERR_BREAKDOWN = 5,    /* GMRES breakdown (zero Krylov vector, NaN) */
+    FMM_ERR_NOT_CONVERGED = 6,/* GMRES hit maxit before tol */
+    FMM_ERR_MESH = 7          /* degenerate mesh (zero-area element, bad index) */
+} fmm_status;
+
+typedef enum { FMM_FP64 = 0, FMM_MIXED = 1 } fmm_precision;
+typedef enum { FMM_RULE_GAUSS3 = 0, FMM_RULE_DUNAVANT7 = 1 } fmm_rule;
+
+#define FMM_MAX_LEVEL 12
+
+typedef struct {
+    double k;                 /* wavenumber */
+    int depth;                /* leaf level; 0 = choose from s like deterLmax */
+    int s;                    /* leaf occupancy for the depth rule (reference: 5) */
+    int p_level[FMM_MAX_LEVEL + 1]; /* truncation order per level l (index l); 0 = truncNum */
+    double eps;               /* truncNum accuracy parameter (reference: 0.05) */
+    int rule;                 /* regular quadrature rule (fmm_rule) */
+    double a_re, a_im, b_re, b_im, c_re, c_im; /* operator a I + b L + c M */
+    int build_mixed;          /* also build the FP32 tables for FMM_MIXED */
+    int device;               /* CUDA device ordinal */
+} fmm_options;
+
+typedef struct {
+    int num_elem, num_vert, lmin, lmax;
+    double d, pt_min[3];
+    int p_level[FMM_MAX_LEVEL + 1];
+    int num_box[FMM_MAX_LEVEL + 1];
+    long long num_m2l[FMM_MAX_LEVEL + 1];
+    long long num_near;
+    size_t device_bytes;
+    double setup_seconds;
+} fmm_info;
+
+typedef struct fmm_plan fmm_plan;
+
+/* Fill opt with the reference's defaults: s = 5, eps = 0.05, 3x3 collapsed Gauss rule,
+ * single-layer operator (a = 0, b = 1, c = 0) as in OprL, device 0. */
+void fmm_default_options(fmm_options *opt);
+
+/* Create a plan from vertices V[3*nv] (double) and triangles F[3*nf] (0-based).  The octree
+ * follows srcBoxes/FMMLevelSet (octree.c:749-906); tables are generated on the GPU. */
+int fmm_plan_create(const double *V, int nv, const int *F, int nf, const fmm_options *opt, fmm_plan **plan);
+
+/* Same from an OBJ file parsed like readOBJ (octree.c:586-619). */
+int fmm_plan_create_obj(const char *path, const fmm_options *opt, fmm_plan **plan);
+
+int fmm_plan_destroy(fmm_plan *plan);
+int fmm_plan_info(const fmm_plan *plan, fmm_info *info);
+
+/* y = A x for nrhs right-hand sides stored one after another (nf each).  precision is
+ * FMM_FP64 (plain path) or FMM_MIXED (FP32 translations and near field).  x and y may be
+ * host or device pointers. */
+int fmm_matvec(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComplex *y, int nrhs, int precision);
+
+/* Solve A x = b with restarted GMRES (FP64 Arnoldi).  FMM_FP64 runs plain GMRES on the FP64
+ * matvec; FMM_MIXED runs iterative refinement: FP64 outer residual, inner GMRES on the
+ * mixed-precision matvec.  x holds the initial guess on entry.  iters/relres may be NULL. */
+int fmm_gmres(fmm_plan *plan, const cuDoubleComplex *b, cuDoubleComplex *x, double tol, int maxit,
+              int restart, int precision, int *iters, double *relres);
+
+/* Scattered pressure of a rigid body at npts exterior points from the surface pressure p:
+ * sum_j p_j int_{T_j} dG/dn_x(x, y) dS(x), regular rule of the plan. */
+int fmm_far_field(fmm_plan *plan, const cuDoubleComplex *p, const double *pts, int npts, cuDoubleComplex *out);
+
+/* Right-hand side for a unit plane wave exp(i k d.x) at the element centroids. */
+int fmm_plane_wave_rhs(fmm_plan *plan, const double *dir, cuDoubleComplex *rhs);
+
+/* Mesh generators (front end for the synthetic configurations).  Return counts through
+ * nv/nf; with V or F NULL only the counts are returned.  Vertex coordinates are rounded to
+ * 9 significant digits, the precision an OBJ writer of this library emits. */
+int fmm_mesh_icosphere(int subdiv, double radius, double *V, int *nv, int *F, int *nf);
+
+/* Last error message of the calling thread (static storage). */
+const char *fmm_last_error(void);
+
+/* Per-kernel timing of the last matvec on the plan's stream (milliseconds), filled when
+ * profiling is enabled with fmm_set_profiling(plan, 1).  names[i] are static strings. */
+int fmm_set_profiling(fmm_plan *plan, int on);
+int fmm_last_timings(const fmm_plan *plan, const char **names, double *ms, int *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -16,7 +16,8 @@ def icosphere(subdiv, radius):
     F = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
          (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
          (8, 6, 7), (9, 8, 1)]
-    V = [np.array(v, dtype=np.float64) / np.sqrt(np.dot(v, v)) for v in V]
+    V = [np.array(v, dtype=np.float64) for v in V]
+    V = [v / np.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) for v in V]
     for _ in range(subdiv):
         cache = {}
         newF = []

@@ -1,0 +1,234 @@
+"""Pin the oracle against the reference's own outputs (tests/golden) and against analytic
+identities.  CPU only."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import meshes
+from oracle import octree_oracle as oo
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+META = json.load(open(os.path.join(GOLDEN, "octree_meta.json")))
+
+
+def digest(a):
+    a = np.ascontiguousarray(a)
+    return hashlib.sha256(a.astype(a.dtype.newbyteorder("<")).tobytes()).hexdigest()
+
+
+def _oracle_tree(case):
+    m = META[case]
+    V, F = meshes.roundtrip(*meshes.icosphere(m["subdiv"], m["radius"]))
+    T = oo.build(V, F, s=m["s"], depth=m["depth"] or None)
+    return V, F, T
+
+
+@pytest.mark.parametrize("case", sorted(META))
+def test_octree_matches_reference(case):
+    """Level sets, interaction lists and element-to-box indices equal the reference's."""
+    g = dict(np.load(os.path.join(GOLDEN, "octree_%s.npz" % case)))
+    m = META[case]
+    V, F, T = _oracle_tree(case)
+    lmax = T["lmax"]
+    assert lmax == int(g["lmax"])
+    assert T["d"] == float(g["d"])
+    assert np.array_equal(T["pt_min"], g["pt_min"])
+    out = {"btm_idx": oo.btm_lvl_elem_idx(V, F, T["pt_min"], T["d"], T["level_sets"][-1], lmax).astype(np.int32)}
+    for l in range(2, lmax + 1):
+        assert np.array_equal(T["level_sets"][l - 2], g["set_%d" % l]), "level %d set" % l
+    sr = oo.sr_lists(T["level_sets"], lmax)
+    ss = oo.ss_rr_lists(T["level_sets"], lmax)
+    for l in range(2, lmax + 1):
+        num, org, dst = sr[l - 2]
+        out["srnum_%d" % l] = num.astype(np.int32)
+        out["sr_origin_%d" % l] = org.astype(np.int32)
+        out["sr_dest_%d" % l] = dst.astype(np.int32)
+        if l > 2:
+            out["ss_dest_%d" % l] = ss[l].astype(np.int32)
+            out["rr_origin_%d" % l] = ss[l].astype(np.int32)
+    for key, val in out.items():
+        if key in g:
+            assert np.array_equal(val, g[key]), key
+        else:
+            assert digest(val) == m["sha256"][key], key
+
+
+def test_quadrature_and_green_vs_reference(oracle):
+    """Element integrals of G and dG/dn (regular and singular) against the reference's FP32."""
+    q = np.load(os.path.join(GOLDEN, "quadrature.npz"))
+    tris, ys, ks = q["tris"].astype(np.float64), q["ys"].astype(np.float64), q["ks"]
+    for a, k in enumerate(ks):
+        kf = float(np.float32(k))
+        for b in range(len(tris)):
+            for sgl in (0, 1):
+                for kind, ref in (("G", q["G"]), ("dG", q["dG"])):
+                    mine = oracle.elem_integral(kind, kf, tris[b], ys[b], rule=0, sgl=bool(sgl))
+                    r = complex(*ref[a, b, sgl])
+                    scale = max(abs(r), abs(oracle.elem_integral("G", kf, tris[b], ys[b], rule=0, sgl=bool(sgl))))
+                    # the reference's FP32 phase k*r carries ~ulp(k r) absolute error
+                    kr = kf * (np.linalg.norm(tris[b].reshape(3, 3) - ys[b], axis=1).max())
+                    tol = 3e-7 * max(30.0, kr)
+                    if kind == "dG" and sgl:
+                        # flat element: (x - y).n = 0, the self term vanishes; the
+                        # reference returns FP32 rounding noise
+                        assert abs(mine) < 1e-13 and abs(r) < 1e-5
+                        continue
+                    assert abs(mine - r) <= tol * scale + 1e-9, (kind, a, b, sgl, mine, r)
+
+
+def test_p2m_moments_vs_reference(oracle):
+    """P2M moments int R_n^{-m} and int dR_n^{-m}/dn (triElemIntegral_R / pRpn)."""
+    q = np.load(os.path.join(GOLDEN, "quadrature.npz"))
+    tris, mom = q["tris"].astype(np.float64), q["moments"]
+    ctr = q["moment_ctr"].astype(np.float64)
+    k = float(np.float32(q["moment_k"]))
+    for b in range(1, len(tris)):
+        for deriv in (0, 1):
+            mine = oracle.elem_moments(k, tris[b], ctr, 6, rule=0, deriv=bool(deriv))
+            ref = mom[b, deriv, :, 0] + 1j * mom[b, deriv, :, 1]
+            assert np.linalg.norm(mine - ref) <= 1e-5 * np.linalg.norm(ref), (b, deriv)
+
+
+def test_truncnum_vs_reference(oracle):
+    q = np.load(os.path.join(GOLDEN, "quadrature.npz"))
+    for k, eps, sig, a, p in q["truncnum"]:
+        assert oracle.truncnum(k, eps, sig, a) == int(p)
+
+
+def test_rotation_matrices_vs_reference(oracle):
+    """Sparse rotation matrices (rotMatsInit + sparseRotMatGen, FP32) against the oracle's
+    Wigner-based FP64 coefficients."""
+    g = np.load(os.path.join(GOLDEN, "tables_rot.npz"))
+    for key in g.files:
+        a, b, c, p = key.split("_")
+        a, b, c, p = float(np.float32(a)), float(np.float32(b)), float(np.float32(c)), int(p)
+        ref = g[key][0::2] + 1j * g[key][1::2]
+        mine = oracle.rot_matrix(a, b, c, p)
+        if p <= 8:
+            assert np.max(np.abs(mine - ref)) < 5e-5, key
+        else:
+            # the reference's FP32 recurrence has drifted by p = 12 (entries off by ~1e-3)
+            assert np.max(np.abs(mine - ref)) > 1e-4, key
+
+
+def _rot_blocks(H, p):
+    off = 0
+    for n in range(p):
+        w = 2 * n + 1
+        yield H[off:off + w * w].reshape(w, w, order="F")
+        off += w * w
+
+
+def test_reference_rotation_recurrence_is_unstable(oracle):
+    """The reference's H recurrence (translation.cu:1179-1204) loses orthogonality as p grows
+    even in FP64, while the Wigner-d evaluation stays orthogonal to rounding at p = 40."""
+    beta = 0.9553166181245093
+    worst = lambda H, p: max(np.max(np.abs(B @ B.T - np.eye(len(B)))) for B in _rot_blocks(H, p))
+    assert worst(oracle.rot_H(beta, 40), 40) < 1e-12
+    assert worst(oracle.rot_H(beta, 20, recur=True), 20) > 1e-8
+    assert worst(oracle.rot_H(beta, 10, recur=True), 10) < 1e-11
+
+
+def test_coaxial_matrices_vs_reference(oracle):
+    """Sparse coaxial matrices (S|R), (R|R) against the reference's FP32 generator."""
+    g = np.load(os.path.join(GOLDEN, "tables_coax.npz"))
+    for key in g.files:
+        k, t, p, sr = key.split("_")
+        k, t, p, sr = float(np.float32(k)), float(np.float32(t)), int(p), int(sr)
+        ref = g[key][0::2] + 1j * g[key][1::2]
+        mine = oracle.coax(k, t, p, bool(sr))
+        assert np.linalg.norm(mine - ref) <= 1e-4 * np.linalg.norm(ref), key
+
+
+def test_wigner_rotation_equals_reference_recurrence(oracle):
+    """Where the reference's H recurrence is accurate (p <= 10) the stable Wigner form agrees."""
+    for beta in (0.1, 0.9553166181245093, 2.2, 3.0):
+        a = oracle.rot_H(beta, 10)
+        b = oracle.rot_H(beta, 10, recur=True)
+        assert np.max(np.abs(a - b)) < 1e-11
+
+
+@pytest.mark.parametrize("p,off,k,box", [(12, (2, 1, 0), 18.32, 0.05), (40, (3, 2, 1), 146.55, 0.15),
+                                          (30, (2, 0, 2), 146.55, 0.075)])
+def test_rcr_translation_addition_theorem(oracle, p, off, k, box):
+    """Multipole of a point source, RCR-translated to a local expansion, equals G directly."""
+    rng = np.random.default_rng(3)
+    cs = np.zeros(3)
+    cd = np.array(off, float) * box
+    y0 = rng.uniform(-0.4, 0.4, 3) * box
+    x = cd + rng.uniform(-0.4, 0.4, 3) * box
+    R = oracle.basis(p, k, y0 - cs)
+    C = np.zeros(p * p, complex)
+    for n in range(p):
+        for m in range(-n, n + 1):
+            C[n * n + n + m] = 1j * k * R[n * n + n - m]
+    D = oracle.rcr(k, cd - cs, p, True, C)
+    loc = np.sum(D * oracle.basis(p, k, x - cd))
+    r = np.linalg.norm(x - y0)
+    direct = np.exp(1j * k * r) / (4 * np.pi * r)
+    assert abs(loc - direct) < 1e-9 * abs(direct) + (1e-6 if p == 12 else 0)
+
+
+def test_fmm_oracle_converges_to_dense(oracle):
+    """FMM oracle vs the dense direct-quadrature operator on the 1280-triangle sphere."""
+    V, F = meshes.roundtrip(*meshes.icosphere(3, 0.1))
+    k = 2 * np.pi * 1000 / 343.0
+    T = oracle.tree_for_fmm(V, F, depth=3)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(len(F)) + 1j * rng.standard_normal(len(F))
+    yd = oracle.dense_apply(V, F, k, x, a=0.5, c=-1.0, rule=1, b=0.0)
+    errs = []
+    for p in (6, 10, 14):
+        y = oracle.FMM(V, F, k, T, [p, p], a=0.5, b=0.0, c=-1.0, rule=1).apply(x)
+        errs.append(np.linalg.norm(y - yd) / np.linalg.norm(yd))
+    assert errs[0] > errs[1] > errs[2]
+    assert errs[2] < 2e-6
+
+
+def test_bem_dense_solution_matches_mie(oracle):
+    """Rigid sphere (ka = 0.9): dense BEM solve of (1/2 - M) p = p_inc, far field vs Mie."""
+    V, F = meshes.roundtrip(*meshes.icosphere(3, 0.1))
+    k = 9.0
+    n = len(F)
+    A = np.zeros((n, n), complex)
+    for j in range(n):
+        e = np.zeros(n, complex)
+        e[j] = 1.0
+        A[:, j] = oracle.dense_apply(V, F, k, e, a=0.5, b=0.0, c=-1.0, rule=1)
+    C = oo.tri_centroids(V, F)
+    rhs = np.exp(1j * k * C[:, 2])
+    p = np.linalg.solve(A, rhs)
+    pts = meshes.fibonacci_sphere(50, 1.0)
+    ff = oracle.far_field(V, F, k, p, pts, rule=1)
+    mie = oracle.mie_rigid(k, 0.1, pts)
+    assert np.linalg.norm(ff - mie) / np.linalg.norm(mie) < 0.03
+
+
+def test_gsl_shim_against_scipy():
+    """The project-written GSL stand-in used to build the reference oracle (only where built)."""
+    import ctypes
+    from scipy.special import lpmv, spherical_jn, spherical_yn
+    from oracle import build as ob
+
+    if not os.path.exists(ob.REF_LIB):
+        pytest.skip("reference oracle not built on this machine")
+    L = ctypes.CDLL(ob.REF_LIB)
+    for name in ("gsl_sf_bessel_jl", "gsl_sf_bessel_yl"):
+        getattr(L, name).restype = ctypes.c_double
+        getattr(L, name).argtypes = [ctypes.c_int, ctypes.c_double]
+    L.gsl_sf_legendre_Plm.restype = ctypes.c_double
+    L.gsl_sf_legendre_Plm.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double]
+    for n in range(0, 60, 3):
+        for x in (0.05, 0.7, 2.75, 19.0, 44.0, 114.0):
+            a, b = L.gsl_sf_bessel_jl(n, x), spherical_jn(n, x)
+            assert abs(a - b) <= 1e-11 * abs(b) + 1e-300
+            a, b = L.gsl_sf_bessel_yl(n, x), spherical_yn(n, x)
+            assert abs(a - b) <= 1e-11 * abs(b)
+    for n in range(0, 30, 2):
+        for m in range(0, n + 1, 3):
+            for x in (-0.7, 0.1, 0.95):
+                a, b = L.gsl_sf_legendre_Plm(n, m, x), lpmv(m, n, x)
+                assert abs(a - b) <= 1e-11 * abs(b) + 1e-300
