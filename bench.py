@@ -1,0 +1,379 @@
+"""Benchmark: mixed-precision FMM-BEM matvec on the 81,920-triangle sphere (8 kHz).
+
+Workload (the mixed-precision-vs-FP64 configuration): rigid sphere r = 0.3 m meshed as an
+icosphere with 6 subdivisions (81,920 flat triangles), k = 2 pi 8000/343 (ka = 44), octree
+depth 6, truncation p = 40/30/20/14/10 at levels 2..6, the reference's 3x3 collapsed Gauss
+rule, operator (1/2) I - M of the exterior Neumann problem, input densities with real and
+imaginary parts i.i.d. N(0,1) from seed 0 (synthetic data; the reference publishes no
+dataset or numbers).
+
+A step is one matvec.  ``value`` is matvec/s of the mixed-precision path with inputs
+resident in HBM, timed with CUDA events on the plan's stream around each step, with L2
+flushed between steps (a 512 MiB write).  ``e2e`` is the same metric through the public
+C ABI with host buffers (H2D of x and D2H of y inside the timed region).  Also reported:
+FP64-plain matvec/s, the mixed-vs-FP64 relative error, and an IR-GMRES solve of the
+plane-wave problem to 1e-6 in both precisions.
+
+``--impl reference`` times the CPU restatement of the reference algorithm (the oracle port,
+FP64, all host cores) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+SUBDIV, RADIUS, FREQ, DEPTH = 6, 0.3, 8000.0, 6
+P_LEVELS = {2: 40, 3: 30, 4: 20, 5: 14, 6: 10}
+METRIC = "solve s & matvec/s, mixed-prec batched vs FP64 plain at 1e-5 rel err, 1 GB300"
+UNIT = "matvec/s"
+
+
+def f_rcr(p):
+    """Algorithmic flops of one RCR translation at order p (8 flops per complex MAC)."""
+    return 8.0 * (10.0 * p ** 3 - p) / 3.0
+
+
+def workload_config(extra=None):
+    cfg = {"workload": "rigid sphere r=0.3 m, icosphere-6 (81920 tri), 8 kHz (ka=44), depth 6, "
+                       "p=40/30/20/14/10, 3x3 collapsed Gauss, operator I/2 - M, N(0,1) densities seed 0",
+           "num_elements": 81920, "depth": DEPTH, "p_levels": [P_LEVELS[l] for l in range(2, 7)],
+           "l2_flush_between_steps": True}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        try:
+            import torch
+            if not torch.cuda.is_available():
+                backend = "gloo"
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % gpu)
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("bf16_tflops", 1900.0), d.get("hbm_gbs", 6800.0), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "m2l_kernel_cfg2.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_matvec:"):
+            try:
+                return float(line.split(":")[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def make_mesh(fm):
+    return fm.icosphere(SUBDIV, RADIUS)
+
+
+def cpu_reference_arm(args, world, rank):
+    """Time the FP64 CPU restatement of the reference algorithm on all host cores."""
+    if rank != 0:
+        return
+    from oracle import oracle_py as O
+    import fmbem_gpu_c_gb300 as fm
+    V, F = make_mesh(fm)
+    k = 2 * np.pi * FREQ / 343.0
+    T = O.tree_for_fmm(V, F, depth=DEPTH)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    f = O.FMM(V, F, k, T, [P_LEVELS[l] for l in range(2, 7)], a=0.5, b=0.0, c=-1.0, rule=0, nthreads=cores)
+    setup = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(len(F)) + 1j * rng.standard_normal(len(F))
+    for _ in range(args.warmup):
+        f.apply(x)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        f.apply(x)
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic", "config": workload_config({"setup_s": setup}),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "full workload, %d matvecs of the FP64 CPU restatement (oracle)" % args.steps},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample():
+    """Oracle port on all host cores, bounded to ~10 s of CPU work."""
+    from oracle import oracle_py as O
+    import fmbem_gpu_c_gb300 as fm
+    V, F = make_mesh(fm)
+    k = 2 * np.pi * FREQ / 343.0
+    T = O.tree_for_fmm(V, F, depth=DEPTH)
+    cores = os.cpu_count() or 1
+    f = O.FMM(V, F, k, T, [P_LEVELS[l] for l in range(2, 7)], a=0.5, b=0.0, c=-1.0, rule=0, nthreads=cores)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(len(F)) + 1j * rng.standard_normal(len(F))
+    y = f.apply(x)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < 10.0 and n < 50:
+        f.apply(x)
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "full workload, %d FP64 matvecs of the CPU restatement (oracle) in %.1f s" % (n, dt)}, x, y
+
+
+def gpu_arm(args, world, rank, local):
+    import torch
+    import fmbem_gpu_c_gb300 as fm
+
+    torch.cuda.set_device(local)
+    V, F = make_mesh(fm)
+    k = 2 * np.pi * FREQ / 343.0
+    t0 = time.perf_counter()
+    plan = fm.Plan(V, F, k=k, depth=DEPTH, p_levels=P_LEVELS, rule=fm.RULE_GAUSS3, a=0.5, b=0.0, c=-1.0,
+                   device=local)
+    setup_s = time.perf_counter() - t0
+    info = plan.info
+    nf = plan.nf
+    rng = np.random.default_rng(rank)
+    xh = rng.standard_normal(nf) + 1j * rng.standard_normal(nf)
+    x = torch.from_numpy(xh).to("cuda")
+    y = torch.empty_like(x)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    # warm-up
+    for _ in range(args.warmup):
+        plan.matvec(x, fm.FMM_MIXED, out=y)
+    torch.cuda.synchronize()
+
+    # timed mixed-precision steps (per-step kernel timing from the plan's events)
+    plan.set_profiling(True)
+    step_ms, kernel_ms = [], {}
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            plan.matvec(x, fm.FMM_MIXED, out=y)
+            tm = plan.timings()
+            step_ms.append(sum(ms for _, ms in tm))
+            for name, ms in tm:
+                kernel_ms.setdefault(name, []).append(ms)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    barrier(world)
+    plan.set_profiling(False)
+    t_step = max_over_ranks(world, float(np.mean(step_ms)) / 1e3)
+    value = world / t_step
+    launches_per_step = len(tm)
+
+    # dominant kernel: M2L (+ fused L2L) at all levels, algorithmic RCR flops
+    m2l_flops = sum(info.num_m2l[l] * f_rcr(info.p_level[l]) for l in range(info.lmin, info.lmax + 1))
+    l2l_flops = sum(info.num_box[l] * f_rcr(info.p_level[l - 1]) for l in range(info.lmin + 1, info.lmax + 1))
+    m2l_ms = float(np.sum([np.mean(v) for n, v in kernel_ms.items() if n.startswith("m2l")]))
+    bf16_peak, hbm_peak, peak_kind = peaks()
+    achieved_tflops = (m2l_flops + l2l_flops) / (m2l_ms / 1e3) / 1e12
+
+    # FP64 plain path and accuracy
+    plan.matvec(x, fm.FMM_FP64, out=y)
+    torch.cuda.synchronize()
+    t64 = []
+    y64 = torch.empty_like(x)
+    for _ in range(3):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        plan.matvec(x, fm.FMM_FP64, out=y64)
+        torch.cuda.synchronize()
+        t64.append(time.perf_counter() - a)
+    plan.matvec(x, fm.FMM_MIXED, out=y)
+    torch.cuda.synchronize()
+    rel_err = float((torch.linalg.norm(y - y64) / torch.linalg.norm(y64)).item())
+    fp64_rate = 1.0 / float(np.median(t64))
+
+    # end to end through the C ABI with host buffers
+    yh = np.empty_like(xh)
+    plan.matvec(xh, fm.FMM_MIXED, out=yh)
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        plan.matvec(xh, fm.FMM_MIXED, out=yh)
+        e2e_t.append(time.perf_counter() - a)
+    e2e_value = world / max_over_ranks(world, float(np.mean(e2e_t)))
+
+    solve = None
+    if args.solve:
+        # Plane wave exp(ikz).  Both paths solve to a residual of 1e-7 (at ka = 44 the operator
+        # is ill-conditioned enough that 1e-6 leaves ~2e-5 in the far field); the far fields
+        # are compared with an FP64 reference solved to 1e-10 (FP64 residual, refinement).
+        b = plan.plane_wave((0.0, 0.0, 1.0))
+        tol = 1e-7
+        a = time.perf_counter()
+        x64, it64, rr64, ok64 = plan.gmres(b, tol=tol, restart=60, maxit=600, precision=fm.FMM_FP64)
+        t_plain = time.perf_counter() - a
+        a = time.perf_counter()
+        xmx, itmx, rrmx, okmx = plan.gmres(b, tol=tol, restart=60, maxit=600, precision=fm.FMM_MIXED)
+        t_mixed = time.perf_counter() - a
+        xref, itr, rrr, okr = plan.gmres(b, x0=xmx, tol=1e-10, restart=60, maxit=600, precision=fm.FMM_MIXED)
+        pts = fm.fibonacci_sphere(64, 2.0)
+        ffr = plan.far_field(xref, pts)
+        ff64 = plan.far_field(x64, pts)
+        ffmx = plan.far_field(xmx, pts)
+        nr = np.linalg.norm(ffr)
+        solve = {"tol": tol, "plain_fp64_s": t_plain, "plain_iters": it64, "plain_relres": rr64,
+                 "mixed_ir_s": t_mixed, "mixed_inner_iters": itmx, "mixed_relres": rrmx, "speedup": t_plain / t_mixed,
+                 "far_field_rel_err_mixed": float(np.linalg.norm(ffmx - ffr) / nr),
+                 "far_field_rel_err_plain": float(np.linalg.norm(ff64 - ffr) / nr),
+                 "reference": "FP64-residual refinement to 1e-10 (%d inner iterations)" % itr}
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu, xc, yc_ref = cpu_baseline_sample()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 (FP32 translations and near field, FP64 input/output)", "data": "synthetic",
+        "config": workload_config({"setup_s": setup_s, "parallelism": "replicas" if world > 1 else "single",
+                                   "wall_s_timed_region": wall}),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nf * 16, "d2h_bytes_per_step": nf * 16},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"bound": "tensor", "kernel": "m2l_kernel<float> (M2L + fused L2L, all levels)",
+                     "achieved": achieved_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
+                     "frac": achieved_tflops / bf16_peak, "peak_source": peak_kind + " bf16 burst",
+                     "traffic": ncu_traffic(), "algorithmic_flops_per_matvec": m2l_flops + l2l_flops,
+                     "ms_per_matvec": m2l_ms},
+        "kernels_ms": {n: float(np.mean(v)) for n, v in kernel_ms.items()},
+        "fp64_plain": {"value": fp64_rate, "unit": UNIT, "mixed_speedup": value / world / fp64_rate,
+                       "mixed_vs_fp64_rel_err": rel_err},
+        "solve": solve,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    plan.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-solve", dest="solve", action="store_false")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        cpu_reference_arm(args, world, rank)
+    else:
+        gpu_arm(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -42,7 +42,8 @@ class Info(ctypes.Structure):
     _fields_ = [("num_elem", ctypes.c_int), ("num_vert", ctypes.c_int), ("lmin", ctypes.c_int), ("lmax", ctypes.c_int),
                 ("d", ctypes.c_double), ("pt_min", ctypes.c_double * 3), ("p_level", ctypes.c_int * (MAX_LEVEL + 1)),
                 ("num_box", ctypes.c_int * (MAX_LEVEL + 1)), ("num_m2l", ctypes.c_longlong * (MAX_LEVEL + 1)),
-                ("num_near", ctypes.c_longlong), ("device_bytes", ctypes.c_size_t), ("setup_seconds", ctypes.c_double)]
+                ("num_near", ctypes.c_longlong), ("device_bytes", ctypes.c_size_t), ("setup_seconds", ctypes.c_double),
+                ("m2l_schedule", ctypes.c_int * (MAX_LEVEL + 1)), ("m2l_split", ctypes.c_int * (MAX_LEVEL + 1))]
 
 
 _lib = None
@@ -191,3 +192,11 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def fibonacci_sphere(n, radius):
+    """n points on a sphere of the given radius (Fibonacci lattice), for far-field checks."""
+    i = np.arange(n) + 0.5
+    phi = np.arccos(1 - 2 * i / n)
+    theta = np.pi * (1 + 5 ** 0.5) * i
+    return radius * np.stack([np.cos(theta) * np.sin(phi), np.sin(theta) * np.sin(phi), np.cos(phi)], axis=1)

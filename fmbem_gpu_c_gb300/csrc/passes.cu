@@ -6,9 +6,14 @@
 // coaxial blocks for |t|, rotate back by (0, theta, phi).  The rotation matrix is
 // e^{i m alpha} e^{-i m' gamma} H_n^{m'm}(beta) (translation.cu:1221-1235), so one real
 // table H per direction serves both rotations and the phases are applied elementwise.
-// Each destination box is owned by one CTA that accumulates all its translations in shared
-// memory and writes once: no atomics, bit-reproducible sums.
+// The FP64 path is owner-computes: each destination box is owned by one CTA that accumulates
+// all its translations in shared memory and writes once (no atomics, bit-reproducible).
+// The mixed path picks per level, by timing at plan creation, between that, a source-split
+// variant and a direction-grouped variant; the latter two add into the locals with FP32
+// atomics, so mixed results vary in the last bits from run to run.
 #include "plan.h"
+#include <algorithm>
+#include <vector>
 
 namespace fmm {
 
@@ -147,8 +152,17 @@ __global__ void m2m_kernel(int pp, int pc, int pmax, const int *__restrict__ chi
     for (int i = threadIdx.x; i < P2; i += blockDim.x) Cpar[(size_t)q * P2 + i] = sY[i];
 }
 
+enum { M2L_OWNER = 0, M2L_L2L_ONLY = 1, M2L_SPLIT = 2 };
+
+__device__ __forceinline__ void atomic_add_c(float2 *a, float2 v) { atomicAdd(a, v); }
+__device__ __forceinline__ void atomic_add_c(double2 *a, double2 v)
+{
+    atomicAdd(&a->x, v.x);
+    atomicAdd(&a->y, v.y);
+}
+
 template <typename T>
-__global__ void m2l_kernel(int p, int pmax, int pp, const int *__restrict__ sr_beg, const int *__restrict__ sr_src,
+__global__ void m2l_kernel(int mode, int p, int pmax, int pp, const int *__restrict__ sr_beg, const int *__restrict__ sr_src,
                            const short *__restrict__ sr_dir, const T *__restrict__ Hsr,
                            const typename Cx<T>::t *__restrict__ PHsr, const typename Cx<T>::t *__restrict__ Csr,
                            const typename Cx<T>::t *__restrict__ Cm, const int *__restrict__ parent,
@@ -162,20 +176,140 @@ __global__ void m2l_kernel(int p, int pmax, int pp, const int *__restrict__ sr_b
     C *sX = (C *)smraw;
     C *sW1 = sX + E2, *sW2 = sW1 + E2, *sY = sW2 + E2;
     int b = blockIdx.x, rs = rot_size(pmax), w = 2 * pmax - 1, cs = coax_size(p);
+    // mode M2L_OWNER: L2L + every M2L source, written once.  M2L_L2L_ONLY: the L2L part
+    // (zeros at the top level), written once.  M2L_SPLIT: sources of chunk blockIdx.y,
+    // added with atomics onto what M2L_L2L_ONLY wrote.
     for (int i = threadIdx.x; i < P2; i += blockDim.x) sY[i] = mk2((T)0, (T)0);
     __syncthreads();
-    if (pp > 0) {
+    if (pp > 0 && mode != M2L_SPLIT) {
         // L2L: parent local (order pp) translated to this box, truncated to p
         int o = octant[b];
         rcr_block<T>(pp, pmax, Hrr + (size_t)o * rs, PHrr + (size_t)o * w, Crr, Dpar + (size_t)parent[b] * pp * pp, pp,
                      sX, sW1, sW2, sY, p);
     }
-    for (int s = sr_beg[b]; s < sr_beg[b + 1]; s++) {
-        int src = sr_src[s], dir = sr_dir[s];
-        rcr_block<T>(p, pmax, Hsr + (size_t)dir * rs, PHsr + (size_t)dir * w, Csr + (size_t)c_dir_dist[dir] * cs,
-                     Cm + (size_t)src * P2, p, sX, sW1, sW2, sY, p);
+    if (mode != M2L_L2L_ONLY) {
+        int s0 = sr_beg[b], s1 = sr_beg[b + 1];
+        if (mode == M2L_SPLIT) {
+            int chunk = (s1 - s0 + gridDim.y - 1) / gridDim.y;
+            s0 = s0 + blockIdx.y * chunk;
+            s1 = min(s1, s0 + chunk);
+        }
+        for (int s = s0; s < s1; s++) {
+            int src = sr_src[s], dir = sr_dir[s];
+            rcr_block<T>(p, pmax, Hsr + (size_t)dir * rs, PHsr + (size_t)dir * w, Csr + (size_t)c_dir_dist[dir] * cs,
+                         Cm + (size_t)src * P2, p, sX, sW1, sW2, sY, p);
+        }
     }
-    for (int i = threadIdx.x; i < P2; i += blockDim.x) Dl[(size_t)b * P2 + i] = sY[i];
+    if (mode == M2L_SPLIT) {
+        for (int i = threadIdx.x; i < P2; i += blockDim.x) atomic_add_c(&Dl[(size_t)b * P2 + i], sY[i]);
+    } else {
+        for (int i = threadIdx.x; i < P2; i += blockDim.x) Dl[(size_t)b * P2 + i] = sY[i];
+    }
+}
+
+// Direction-grouped M2L: every CTA takes one work item (direction, range of translations
+// with that offset), stages the direction's rotation coefficients, coaxial blocks and
+// phases in shared memory once, and streams the translations through its warps -- one warp
+// per translation, warp-synchronous stages, results added to the destination locals with
+// vector atomics.  The tables are read from HBM/L2 once per item instead of once per
+// translation.
+template <typename T>
+__device__ __forceinline__ void rcr_warp(int p, const T *__restrict__ sH, const typename Cx<T>::t *__restrict__ sPh,
+                                         const typename Cx<T>::t *__restrict__ sC, const typename Cx<T>::t *__restrict__ xin,
+                                         typename Cx<T>::t *sX, typename Cx<T>::t *sW1, typename Cx<T>::t *sW2,
+                                         typename Cx<T>::t *__restrict__ yout, int lane)
+{
+    typedef typename Cx<T>::t C;
+    const int pp = p * p, off = p - 1;
+    for (int i = lane; i < pp; i += 32) {
+        int n, m;
+        decode_nm(i, n, m);
+        sX[i] = cmul(xin[i], sPh[m + off]);
+    }
+    __syncwarp();
+    for (int i = lane; i < pp; i += 32) {
+        int n, mp;
+        decode_nm(i, n, mp);
+        const T *col = sH + rot_off(n) + (mp + n);
+        const int w = 2 * n + 1, base = n * n;
+        T ar = 0, ai = 0;
+        for (int m = 0; m < w; m++) {
+            T h = col[m * w];
+            C v = sX[base + m];
+            ar += h * v.x;
+            ai += h * v.y;
+        }
+        sW1[i] = mk2(ar, ai);
+    }
+    __syncwarp();
+    for (int i = lane; i < pp; i += 32) {
+        int np, m;
+        decode_nm(i, np, m);
+        int am = m < 0 ? -m : m, sz = p - am;
+        const C *col = sC + coax_off(p, am) + (np - am);
+        T ar = 0, ai = 0;
+        for (int n = am; n < p; n++) {
+            C c = col[(n - am) * sz];
+            C v = sW1[n * n + n + m];
+            ar += c.x * v.x - c.y * v.y;
+            ai += c.x * v.y + c.y * v.x;
+        }
+        sW2[i] = mk2(ar, ai);
+    }
+    __syncwarp();
+    for (int i = lane; i < pp; i += 32) {
+        int n, mp;
+        decode_nm(i, n, mp);
+        const T *col = sH + rot_off(n) + (mp + n);
+        const int w = 2 * n + 1, base = n * n;
+        T ar = 0, ai = 0;
+        for (int m = 0; m < w; m++) {
+            T h = col[m * w];
+            C v = sW2[base + m];
+            ar += h * v.x;
+            ai += h * v.y;
+        }
+        C e = sPh[mp + off];
+        atomic_add_c(&yout[i], mk2(e.x * ar + e.y * ai, e.x * ai - e.y * ar));
+    }
+    __syncwarp();
+}
+
+template <typename T>
+__global__ void m2l_dir_kernel(int p, int pmax, const int4 *__restrict__ items, const int *__restrict__ g_src,
+                               const int *__restrict__ g_dst, const T *__restrict__ Hsr,
+                               const typename Cx<T>::t *__restrict__ PHsr, const typename Cx<T>::t *__restrict__ Csr,
+                               const typename Cx<T>::t *__restrict__ Cm, typename Cx<T>::t *__restrict__ Dl)
+{
+    typedef typename Cx<T>::t C;
+    extern __shared__ unsigned char smraw[];
+    const int4 it = items[blockIdx.x];
+    const int dir = it.x, rs = rot_size(p), cs = coax_size(p), w = 2 * p - 1, P2 = p * p;
+    // layout: coax (C), phases (C), per-warp X/W1/W2 (C), then H (T)
+    C *sC = (C *)smraw;
+    C *sPh = sC + cs;
+    C *sWarp = sPh + w;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    T *sH = (T *)(sWarp + (size_t)nw * 3 * P2);
+    const T *Hg = Hsr + (size_t)dir * rot_size(pmax);
+    const C *Cg = Csr + (size_t)c_dir_dist[dir] * cs;
+    const C *Pg = PHsr + (size_t)dir * (2 * pmax - 1) + (pmax - p);
+    for (int i = threadIdx.x; i < rs; i += blockDim.x) sH[i] = Hg[i];
+    for (int i = threadIdx.x; i < cs; i += blockDim.x) sC[i] = Cg[i];
+    for (int i = threadIdx.x; i < w; i += blockDim.x) sPh[i] = Pg[i];
+    __syncthreads();
+    C *sX = sWarp + (size_t)warp * 3 * P2, *sW1 = sX + P2, *sW2 = sW1 + P2;
+    for (int t = it.y + warp; t < it.y + it.z; t += nw) {
+        int src = g_src[t], dst = g_dst[t];
+        rcr_warp<T>(p, sH, sPh, sC, Cm + (size_t)src * P2, sX, sW1, sW2, Dl + (size_t)dst * P2, lane);
+    }
+}
+
+template <typename T>
+size_t m2l_dir_smem(int p, int nwarps)
+{
+    typedef typename Cx<T>::t C;
+    return sizeof(C) * ((size_t)coax_size(p) + (2 * p - 1) + (size_t)nwarps * 3 * p * p) + sizeof(T) * (size_t)rot_size(p);
 }
 
 template <typename T>
@@ -231,6 +365,45 @@ static void timer_end(Plan *P)
 }
 
 template <typename T>
+static int launch_m2l_level(Plan *P, int l, int sched, int split, const char *tname)
+{
+    typedef typename Cx<T>::t C;
+    const bool f64 = sizeof(T) == 8;
+    int lmin = P->lmin, pmax = P->pmax;
+    cudaStream_t st = P->stream;
+    LevelDev &L = P->lev[l];
+    const T *Hsr = f64 ? (const T *)P->Hsr64 : (const T *)P->Hsr32;
+    const T *Hrr = f64 ? (const T *)P->Hrr64 : (const T *)P->Hrr32;
+    const C *PHsr = f64 ? (const C *)P->PHsr64 : (const C *)P->PHsr32;
+    const C *PHrr = f64 ? (const C *)P->PHrr64 : (const C *)P->PHrr32;
+    const C *Csr = f64 ? (const C *)L.Csr64 : (const C *)L.Csr32;
+    const C *Crr = l > lmin ? (f64 ? (const C *)L.Crr64 : (const C *)L.Crr32) : nullptr;
+    const C *Cm = f64 ? (const C *)L.Cm64 : (const C *)L.Cm32;
+    C *Dl = f64 ? (C *)L.Dl64 : (C *)L.Dl32;
+    const C *Dpar = l > lmin ? (f64 ? (const C *)P->lev[l - 1].Dl64 : (const C *)P->lev[l - 1].Dl32) : nullptr;
+    int pp = l > lmin ? P->lev[l - 1].p : 0;
+    int pe = pp > L.p ? pp : L.p;
+    size_t sm = 4 * (size_t)pe * pe * sizeof(C);
+    timer_begin(P, tname);
+    int first_mode = (sched == M2L_SCHED_OWNER) ? M2L_OWNER : M2L_L2L_ONLY;
+    m2l_kernel<T><<<L.nb, block_for(pe), sm, st>>>(first_mode, L.p, pmax, pp, L.sr_beg, L.sr_src, L.sr_dir, Hsr, PHsr,
+                                                     Csr, Cm, L.parent, L.octant, Hrr, PHrr, Crr, Dpar, Dl);
+    if (sched == M2L_SCHED_SPLIT) {
+        size_t sm2 = 4 * (size_t)L.p * L.p * sizeof(C);
+        m2l_kernel<T><<<dim3(L.nb, split), block_for(L.p), sm2, st>>>(M2L_SPLIT, L.p, pmax, 0, L.sr_beg, L.sr_src,
+                                                                      L.sr_dir, Hsr, PHsr, Csr, Cm, L.parent, L.octant,
+                                                                      Hrr, PHrr, Crr, Dpar, Dl);
+    } else if (sched == M2L_SCHED_DIR) {
+        size_t sm3 = m2l_dir_smem<T>(L.p, L.dir_warps);
+        m2l_dir_kernel<T><<<L.n_items, 32 * L.dir_warps, sm3, st>>>(L.p, pmax, L.dir_items, L.g_src, L.g_dst, Hsr,
+                                                                    PHsr, Csr, Cm, Dl);
+    }
+    timer_end(P);
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
+template <typename T>
 static int run_matvec_t(Plan *P, const double2 *x, double2 *y)
 {
     typedef typename Cx<T>::t C;
@@ -244,6 +417,7 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y)
     if (!attr_done[slot] || attr_bytes[slot] < smax) {
         FMM_CUDA_TRY(cudaFuncSetAttribute(m2m_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
         FMM_CUDA_TRY(cudaFuncSetAttribute(m2l_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+        FMM_CUDA_TRY(cudaFuncSetAttribute(m2l_dir_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
         attr_done[slot] = true;
         attr_bytes[slot] = smax;
     }
@@ -263,29 +437,27 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y)
     const C *nearv = f64 ? (const C *)P->near64 : (const C *)P->near32;
     LevelDev &LL = P->lev[lmax];
 
+    static const char *m2m_names[] = {"m2m_l0", "m2m_l1", "m2m_l2", "m2m_l3", "m2m_l4", "m2m_l5", "m2m_l6",
+                                      "m2m_l7", "m2m_l8", "m2m_l9", "m2m_l10", "m2m_l11", "m2m_l12", "m2m_l13"};
+    static const char *m2l_names[] = {"m2l_l0", "m2l_l1", "m2l_l2", "m2l_l3", "m2l_l4", "m2l_l5", "m2l_l6",
+                                      "m2l_l7", "m2l_l8", "m2l_l9", "m2l_l10", "m2l_l11", "m2l_l12", "m2l_l13"};
     timer_begin(P, "p2m");
     p2m_kernel<T><<<LL.nb, 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, U, x, P->opt.k, Cm(lmax));
     timer_end(P);
     for (int l = lmax; l > lmin; l--) {
         LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
         size_t sm = 4 * (size_t)PL.p * PL.p * sizeof(C);
-        timer_begin(P, "m2m");
+        timer_begin(P, m2m_names[l]);
         m2m_kernel<T><<<PL.nb, block_for(PL.p), sm, st>>>(PL.p, L.p, pmax, PL.child_beg, PL.child_list, L.octant, Hss,
                                                            PHss, Crr(l), Cm(l), Cm(l - 1));
         timer_end(P);
     }
     for (int l = lmin; l <= lmax; l++) {
-        LevelDev &L = P->lev[l];
-        int pp = l > lmin ? P->lev[l - 1].p : 0;
-        int pe = pp > L.p ? pp : L.p;
-        size_t sm = 4 * (size_t)pe * pe * sizeof(C);
-        timer_begin(P, "m2l+l2l");
-        m2l_kernel<T><<<L.nb, block_for(pe), sm, st>>>(L.p, pmax, pp, L.sr_beg, L.sr_src, L.sr_dir, Hsr, PHsr, Csr(l),
-                                                         Cm(l), L.parent, L.octant, Hrr, PHrr, l > lmin ? Crr(l) : nullptr,
-                                                         l > lmin ? Dl(l - 1) : nullptr, Dl(l));
-        timer_end(P);
+        int st = launch_m2l_level<T>(P, l, f64 ? M2L_SCHED_OWNER : P->lev[l].sched32, f64 ? 1 : P->lev[l].split32,
+                                     m2l_names[l]);
+        if (st) return st;
     }
-    timer_begin(P, "l2p+near");
+    timer_begin(P, "l2p_near");
     double2 a = make_double2(P->opt.a_re, P->opt.a_im);
     l2p_near_kernel<T><<<(P->nf * 32 + 255) / 256, 256, 0, st>>>(P->nf, LL.p, P->elem_leaf, Dl(lmax), Rv, P->near_beg,
                                                                   P->near_col, nearv, x, a, y);
@@ -310,6 +482,97 @@ int run_matvec(Plan *P, const double2 *x, double2 *y, int precision)
         return run_matvec_t<float>(P, x, y);
     }
     return run_matvec_t<double>(P, x, y);
+}
+
+
+// Translations of each level sorted by direction, cut into work items of at most `chunk`
+// translations (one CTA each).
+int build_dir_groups(Plan *P)
+{
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        LevelDev &L = P->lev[l];
+        long long T = L.num_sr;
+        if (T == 0) continue;
+        std::vector<int> beg(L.nb + 1), src(T);
+        std::vector<short> dir(T);
+        FMM_CUDA_TRY(cudaMemcpy(beg.data(), L.sr_beg, sizeof(int) * (L.nb + 1), cudaMemcpyDeviceToHost));
+        FMM_CUDA_TRY(cudaMemcpy(src.data(), L.sr_src, sizeof(int) * T, cudaMemcpyDeviceToHost));
+        FMM_CUDA_TRY(cudaMemcpy(dir.data(), L.sr_dir, sizeof(short) * T, cudaMemcpyDeviceToHost));
+        std::vector<int> cnt(NDIR + 1, 0);
+        for (long long t = 0; t < T; t++) cnt[dir[t] + 1]++;
+        for (int d = 0; d < NDIR; d++) cnt[d + 1] += cnt[d];
+        std::vector<int> gs(T), gd(T), fill(NDIR, 0);
+        for (int b = 0; b < L.nb; b++)
+            for (int t = beg[b]; t < beg[b + 1]; t++) {
+                int d = dir[t], pos = cnt[d] + fill[d]++;
+                gs[pos] = src[t];
+                gd[pos] = b;
+            }
+        const int chunk = 128;
+        std::vector<int4> items;
+        for (int d = 0; d < NDIR; d++)
+            for (int a = cnt[d]; a < cnt[d + 1]; a += chunk) items.push_back(make_int4(d, a, std::min(chunk, cnt[d + 1] - a), 0));
+        L.n_items = (int)items.size();
+        L.dir_warps = L.p <= 14 ? 8 : 4;
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.dir_items, sizeof(int4) * items.size()));
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.g_src, sizeof(int) * T));
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.g_dst, sizeof(int) * T));
+        FMM_CUDA_TRY(cudaMemcpy(L.dir_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+        FMM_CUDA_TRY(cudaMemcpy(L.g_src, gs.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
+        FMM_CUDA_TRY(cudaMemcpy(L.g_dst, gd.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
+    }
+    return FMM_OK;
+}
+
+// Per-level schedule of the mixed-precision M2L picked by timing the candidates on this
+// plan's own tables: owner-computes, source-split with atomics (2..16 chunks), and the
+// direction-grouped kernel where its shared-memory footprint fits (p <= 20).
+int tune_m2l(Plan *P)
+{
+    if (!P->U32) return FMM_OK;
+    cudaEvent_t a, b;
+    FMM_CUDA_TRY(cudaEventCreate(&a));
+    FMM_CUDA_TRY(cudaEventCreate(&b));
+    int saved = P->profiling;
+    P->profiling = 0;
+    // representative inputs: unit coefficients (the timing does not depend on the values)
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        LevelDev &L = P->lev[l];
+        std::vector<float2> ones((size_t)L.nb * L.p * L.p, make_float2(1e-3f, 0.f));
+        FMM_CUDA_TRY(cudaMemcpy(L.Cm32, ones.data(), sizeof(float2) * ones.size(), cudaMemcpyHostToDevice));
+        FMM_CUDA_TRY(cudaMemcpy(L.Dl32, ones.data(), sizeof(float2) * ones.size(), cudaMemcpyHostToDevice));
+    }
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        LevelDev &L = P->lev[l];
+        struct Cand { int sched, split; };
+        std::vector<Cand> cands = {{M2L_SCHED_OWNER, 1}};
+        for (int s = 2; s <= 16; s *= 2)
+            if ((long long)L.nb * s <= 152LL * 64 && L.num_sr / std::max(1, L.nb) >= 2 * s) cands.push_back({M2L_SCHED_SPLIT, s});
+        if (L.p <= 20 && L.n_items > 0 && m2l_dir_smem<float>(L.p, L.dir_warps) <= 220 * 1024) cands.push_back({M2L_SCHED_DIR, 1});
+        float best = 1e30f;
+        for (auto &c : cands) {
+            float tsum = 0.f;
+            for (int rep = 0; rep < 3; rep++) {
+                FMM_CUDA_TRY(cudaEventRecord(a, P->stream));
+                int st = launch_m2l_level<float>(P, l, c.sched, c.split, "tune");
+                if (st) return st;
+                FMM_CUDA_TRY(cudaEventRecord(b, P->stream));
+                FMM_CUDA_TRY(cudaEventSynchronize(b));
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, a, b);
+                if (rep > 0) tsum += ms;
+            }
+            if (tsum < best) {
+                best = tsum;
+                L.sched32 = c.sched;
+                L.split32 = c.split;
+            }
+        }
+    }
+    P->profiling = saved;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return FMM_OK;
 }
 
 } // namespace fmm

@@ -67,6 +67,7 @@ static void free_plan(Plan *P)
         LevelDev &L = P->lev[l];
         F(L.parent); F(L.octant); F(L.child_beg); F(L.child_list); F(L.sr_beg); F(L.sr_src); F(L.sr_dir);
         F(L.Cm64); F(L.Dl64); F(L.Cm32); F(L.Dl32); F(L.Csr64); F(L.Csr32); F(L.Crr64); F(L.Crr32);
+        F(L.dir_items); F(L.g_src); F(L.g_dst);
     }
     F(P->Hsr64); F(P->PHsr64); F(P->Hsr32); F(P->PHsr32);
     F(P->V_dev); F(P->F_dev); F(P->elem_leaf); F(P->leaf_beg); F(P->leaf_elem);
@@ -149,6 +150,10 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
     }
     TRY(gen_element_tables(P));
     TRY(gen_near_field(P));
+    if (opt->build_mixed) {
+        TRY(build_dir_groups(P));
+        TRY(tune_m2l(P));
+    }
     CTRY(dev_alloc(P, (void **)&P->xbuf, sizeof(double2) * nf));
     CTRY(dev_alloc(P, (void **)&P->ybuf, sizeof(double2) * nf));
     P->nrhs_cap = 1;
@@ -202,6 +207,8 @@ extern "C" int fmm_plan_info(const fmm_plan *plan, fmm_info *info)
         info->p_level[l] = P->lev[l].p;
         info->num_box[l] = P->lev[l].nb;
         info->num_m2l[l] = P->lev[l].num_sr;
+        info->m2l_schedule[l] = P->lev[l].sched32;
+        info->m2l_split[l] = P->lev[l].split32;
     }
     info->num_near = P->num_near;
     info->device_bytes = P->device_bytes;

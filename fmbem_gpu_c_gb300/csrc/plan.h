@@ -27,7 +27,16 @@ struct LevelDev {
     float2 *Csr32 = nullptr;
     double2 *Crr64 = nullptr;     // coaxial (R|R) at order p_{l-1} for M2M into / L2L out of level l-1
     float2 *Crr32 = nullptr;
+    // mixed-precision M2L schedule chosen by the autotuner (tune_m2l)
+    int sched32 = 0;              // M2L_SCHED_OWNER, _SPLIT or _DIR
+    int split32 = 1;              // source chunks per destination for _SPLIT
+    int dir_warps = 8;            // warps per CTA for _DIR
+    int n_items = 0;              // direction-grouped work items
+    int4 *dir_items = nullptr;    // (direction, first, count, 0)
+    int *g_src = nullptr, *g_dst = nullptr; // translations sorted by direction
 };
+
+enum { M2L_SCHED_OWNER = 0, M2L_SCHED_SPLIT = 1, M2L_SCHED_DIR = 2 };
 
 struct Timer {
     const char *name;
@@ -85,11 +94,15 @@ int gen_element_tables(Plan *P);
 int gen_near_field(Plan *P);
 int launch_far_field(Plan *P, const double2 *p, const double *pts, int npts, double2 *out);
 int launch_plane_wave(Plan *P, const double *dir, double2 *rhs);
+int gen_rotation_matrices_f32(const double *alpha, const double *beta, const double *gamma, int n, int p, float2 *host_out);
+int gen_coax_matrices_f32(double k, const double *t, int n, int p, int sr, float2 *host_out);
 
 // octree_gpu.cu
 int build_lists(Plan *P);
 
 // passes.cu
 int run_matvec(Plan *P, const double2 *x, double2 *y, int precision);
+int build_dir_groups(Plan *P);
+int tune_m2l(Plan *P);
 
 } // namespace fmm

@@ -225,6 +225,43 @@ int gen_rotation_tables(Plan *P)
     return FMM_OK;
 }
 
+// Complex rotation matrices e^{i m alpha} e^{-i m' gamma} H_n^{m'm}(beta) in FP32, the
+// sparse layout of sparseRotMatGen (translation.cu:1221-1235).
+__global__ void assemble_rot_kernel(const double *H, const double *alpha, const double *gamma, int p, float2 *out)
+{
+    int a = blockIdx.y, rs = rot_size(p);
+    const double *Ha = H + (size_t)a * rs;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rs; i += gridDim.x * blockDim.x) {
+        int n = 0;
+        while (rot_off(n + 1) <= i) n++;
+        int loc = i - rot_off(n), w = 2 * n + 1;
+        int mp = loc % w - n, m = loc / w - n;
+        double s, c;
+        sincos(m * alpha[a] - mp * gamma[a], &s, &c);
+        out[(size_t)a * rs + i] = make_float2((float)(c * Ha[i]), (float)(s * Ha[i]));
+    }
+}
+
+int gen_rotation_matrices_f32(const double *alpha, const double *beta, const double *gamma, int n, int p, float2 *host_out)
+{
+    if (n <= 0) return FMM_OK;
+    int rs = rot_size(p), w = 2 * p - 1;
+    double *d = nullptr, *H = nullptr;
+    float2 *o = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&d, sizeof(double) * 3 * n));
+    FMM_CUDA_TRY(cudaMalloc(&H, sizeof(double) * (size_t)n * rs));
+    FMM_CUDA_TRY(cudaMalloc(&o, sizeof(float2) * (size_t)n * rs));
+    FMM_CUDA_TRY(cudaMemcpy(d, alpha, sizeof(double) * n, cudaMemcpyHostToDevice));
+    FMM_CUDA_TRY(cudaMemcpy(d + n, beta, sizeof(double) * n, cudaMemcpyHostToDevice));
+    FMM_CUDA_TRY(cudaMemcpy(d + 2 * n, gamma, sizeof(double) * n, cudaMemcpyHostToDevice));
+    wigner_H_kernel<<<dim3((w * w + 255) / 256, n), 256>>>(d + n, p, H);
+    assemble_rot_kernel<<<dim3((rs + 255) / 256, n), 256>>>(H, d, d + 2 * n, p, o);
+    FMM_CUDA_TRY(cudaGetLastError());
+    FMM_CUDA_TRY(cudaMemcpy(host_out, o, sizeof(float2) * (size_t)n * rs, cudaMemcpyDeviceToHost));
+    cudaFree(d); cudaFree(H); cudaFree(o);
+    return FMM_OK;
+}
+
 // ----------------------------------------------------------------------------- coaxial
 // (S|R) or (R|R) coaxial blocks for translation length t along z, following
 // sparseCoaxTransMatGen (translation.cu:678-771) with the initial column of
@@ -336,6 +373,27 @@ int gen_coax_tables(Plan *P)
     FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
     cudaFree(scratch);
     cudaFree(tdev);
+    return FMM_OK;
+}
+
+// FP32 sparse coaxial matrices for n translation lengths (the output of
+// genRR/SRSparseCoaxTransMat, translation.cu:822-1062), generated in FP64.
+int gen_coax_matrices_f32(double k, const double *t, int n, int p, int sr, float2 *host_out)
+{
+    if (n <= 0) return FMM_OK;
+    int cs = coax_size(p);
+    double2 *scratch = nullptr, *o = nullptr;
+    double *td = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&scratch, sizeof(double2) * (size_t)n * p * (2 * p - 1) * p));
+    FMM_CUDA_TRY(cudaMalloc(&o, sizeof(double2) * (size_t)n * cs));
+    FMM_CUDA_TRY(cudaMalloc(&td, sizeof(double) * n));
+    FMM_CUDA_TRY(cudaMemcpy(td, t, sizeof(double) * n, cudaMemcpyHostToDevice));
+    coax_kernel<<<n, 256, sizeof(double) * 2 * (2 * p - 1)>>>(k, td, p, sr, scratch, o);
+    FMM_CUDA_TRY(cudaGetLastError());
+    std::vector<double2> h((size_t)n * cs);
+    FMM_CUDA_TRY(cudaMemcpy(h.data(), o, sizeof(double2) * h.size(), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < h.size(); i++) host_out[i] = make_float2((float)h[i].x, (float)h[i].y);
+    cudaFree(scratch); cudaFree(o); cudaFree(td);
     return FMM_OK;
 }
 
