@@ -108,21 +108,30 @@ __device__ void rcr_block(int p, int pmax, const T *__restrict__ H, const typena
     __syncthreads();
 }
 
+// flip = 0: C_b[n,m] = ik sum_e x_e U_e[n,m] (element moments of R_n^{-m}).
+// flip = 1 (transposed operator): the same with the table read at (n,-m); with U = Rv this
+// is the multipole expansion ik sum_i y_i R_n^{-m}(y_i - c) of point sources at centroids.
 template <typename T>
 __global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *__restrict__ leaf_elem,
                            const typename Cx<T>::t *__restrict__ U, const double2 *__restrict__ x, double k,
-                           typename Cx<T>::t *__restrict__ Cm)
+                           typename Cx<T>::t *__restrict__ Cm, int flip)
 {
     typedef typename Cx<T>::t C;
     int b = blockIdx.x, ppl = pl * pl;
     int s0 = leaf_beg[b], s1 = leaf_beg[b + 1];
     for (int i = threadIdx.x; i < ppl; i += blockDim.x) {
+        int q = i;
+        if (flip) {
+            int n, m;
+            decode_nm(i, n, m);
+            q = n * n + n - m;
+        }
         T ar = 0, ai = 0;
         for (int s = s0; s < s1; s++) {
             int e = leaf_elem[s];
             double2 xe = x[e];
             T xr = (T)(-k * xe.y), xi = (T)(k * xe.x); // i k x_e
-            C u = U[(size_t)e * ppl + i];
+            C u = U[(size_t)e * ppl + q];
             ar += xr * u.x - xi * u.y;
             ai += xr * u.y + xi * u.x;
         }
@@ -150,6 +159,12 @@ __global__ void m2m_kernel(int pp, int pc, int pmax, const int *__restrict__ chi
                      sX, sW1, sW2, sY, pp);
     }
     for (int i = threadIdx.x; i < P2; i += blockDim.x) Cpar[(size_t)q * P2 + i] = sY[i];
+}
+
+__global__ void to_float_kernel2(const double *in, float *out, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
 }
 
 enum { M2L_OWNER = 0, M2L_L2L_ONLY = 1, M2L_SPLIT = 2 };
@@ -316,7 +331,7 @@ template <typename T>
 __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_leaf, const typename Cx<T>::t *__restrict__ Dl,
                                 const typename Cx<T>::t *__restrict__ Rv, const int *__restrict__ near_beg,
                                 const int *__restrict__ near_col, const typename Cx<T>::t *__restrict__ nearv,
-                                const double2 *__restrict__ x, double2 a, double2 *__restrict__ y)
+                                const double2 *__restrict__ x, double2 a, double2 *__restrict__ y, int flip)
 {
     typedef typename Cx<T>::t C;
     int lane = threadIdx.x & 31;
@@ -334,7 +349,13 @@ __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_lea
     const C *D = Dl + (size_t)elem_leaf[e] * ppl;
     const C *R = Rv + (size_t)e * ppl;
     for (int i = lane; i < ppl; i += 32) {
-        C d = D[i], r = R[i];
+        int q = i;
+        if (flip) {
+            int n, m;
+            decode_nm(i, n, m);
+            q = n * n + n - m;
+        }
+        C d = D[i], r = R[q];
         ar += d.x * r.x - d.y * r.y;
         ai += d.x * r.y + d.y * r.x;
     }
@@ -362,6 +383,23 @@ static void timer_end(Plan *P)
     if (!P->profiling || P->ntimers >= MAX_TIMERS) return;
     cudaEventRecord(P->timers[P->ntimers].end, P->stream);
     P->ntimers++;
+}
+
+// Raise the dynamic shared-memory limit of the translation kernels to what order pmax needs
+// (4 p^2 complex for the CTA-level RCR, up to 220 KiB for the direction-grouped kernel).
+template <typename T>
+static int set_smem_attrs(int pmax)
+{
+    typedef typename Cx<T>::t C;
+    static size_t done[2] = {0, 0};
+    int slot = sizeof(T) == 8 ? 0 : 1;
+    size_t smax = 4 * (size_t)pmax * pmax * sizeof(C);
+    if (done[slot] >= smax) return FMM_OK;
+    FMM_CUDA_TRY(cudaFuncSetAttribute(m2m_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+    FMM_CUDA_TRY(cudaFuncSetAttribute(m2l_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+    FMM_CUDA_TRY(cudaFuncSetAttribute(m2l_dir_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    done[slot] = smax;
+    return FMM_OK;
 }
 
 template <typename T>
@@ -404,22 +442,15 @@ static int launch_m2l_level(Plan *P, int l, int sched, int split, const char *tn
 }
 
 template <typename T>
-static int run_matvec_t(Plan *P, const double2 *x, double2 *y)
+static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
 {
     typedef typename Cx<T>::t C;
     const bool f64 = sizeof(T) == 8;
     int lmin = P->lmin, lmax = P->lmax, pmax = P->pmax;
     cudaStream_t st = P->stream;
-    size_t smax = 4 * (size_t)pmax * pmax * sizeof(C);
-    static bool attr_done[2] = {false, false};
-    static size_t attr_bytes[2] = {0, 0};
-    int slot = f64 ? 0 : 1;
-    if (!attr_done[slot] || attr_bytes[slot] < smax) {
-        FMM_CUDA_TRY(cudaFuncSetAttribute(m2m_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
-        FMM_CUDA_TRY(cudaFuncSetAttribute(m2l_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
-        FMM_CUDA_TRY(cudaFuncSetAttribute(m2l_dir_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        attr_done[slot] = true;
-        attr_bytes[slot] = smax;
+    {
+        int st = set_smem_attrs<T>(pmax);
+        if (st) return st;
     }
     P->ntimers = 0;
     const T *Hsr = f64 ? (const T *)P->Hsr64 : (const T *)P->Hsr32;
@@ -442,7 +473,10 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y)
     static const char *m2l_names[] = {"m2l_l0", "m2l_l1", "m2l_l2", "m2l_l3", "m2l_l4", "m2l_l5", "m2l_l6",
                                       "m2l_l7", "m2l_l8", "m2l_l9", "m2l_l10", "m2l_l11", "m2l_l12", "m2l_l13"};
     timer_begin(P, "p2m");
-    p2m_kernel<T><<<LL.nb, 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, U, x, P->opt.k, Cm(lmax));
+    // the transposed operator swaps the roles of the element moments and the centroid basis
+    // (index-flipped), keeps every translation, and uses the transposed near-field matrix
+    p2m_kernel<T><<<LL.nb, 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, transpose ? Rv : U, x, P->opt.k, Cm(lmax),
+                                         transpose);
     timer_end(P);
     for (int l = lmax; l > lmin; l--) {
         LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
@@ -459,8 +493,10 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y)
     }
     timer_begin(P, "l2p_near");
     double2 a = make_double2(P->opt.a_re, P->opt.a_im);
-    l2p_near_kernel<T><<<(P->nf * 32 + 255) / 256, 256, 0, st>>>(P->nf, LL.p, P->elem_leaf, Dl(lmax), Rv, P->near_beg,
-                                                                  P->near_col, nearv, x, a, y);
+    const C *nearT = f64 ? (const C *)P->nearT64 : (const C *)P->nearT32;
+    l2p_near_kernel<T><<<(P->nf * 32 + 255) / 256, 256, 0, st>>>(
+        P->nf, LL.p, P->elem_leaf, Dl(lmax), transpose ? U : Rv, transpose ? P->nearT_beg : P->near_beg,
+        transpose ? P->nearT_col : P->near_col, transpose ? nearT : nearv, x, a, y, transpose);
     timer_end(P);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
@@ -472,16 +508,77 @@ int set_dir_dist(const int *dd)
     return FMM_OK;
 }
 
-int run_matvec(Plan *P, const double2 *x, double2 *y, int precision)
+int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpose)
 {
+    if (transpose && !P->nearT_beg) {
+        fmm_set_error("transposed near field not built");
+        return FMM_ERR_ARG;
+    }
     if (precision == FMM_MIXED) {
         if (!P->U32) {
             fmm_set_error("plan was created without build_mixed");
             return FMM_ERR_ARG;
         }
-        return run_matvec_t<float>(P, x, y);
+        return run_matvec_t<float>(P, x, y, transpose);
     }
-    return run_matvec_t<double>(P, x, y);
+    return run_matvec_t<double>(P, x, y, transpose);
+}
+
+__global__ void gather_kernel(const double2 *src, const long long *perm, long long n, double2 *dst)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = src[perm[i]];
+}
+
+__global__ void conj_kernel(const double2 *x, double2 *y, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = make_double2(x[i].x, -x[i].y);
+}
+
+void launch_conj(Plan *P, const double2 *x, double2 *y)
+{
+    conj_kernel<<<(P->nf + 255) / 256, 256, 0, P->stream>>>(x, y, P->nf);
+}
+
+// Near-field matrix transposed (CSR by source element), built on first use of the
+// transposed operator: (A^T y)_j collects A_ij y_i over the targets i near j.
+int build_transpose(Plan *P)
+{
+    if (P->nearT_beg) return FMM_OK;
+    long long nnz = P->num_near;
+    std::vector<int> beg(P->nf + 1), col(nnz);
+    FMM_CUDA_TRY(cudaMemcpy(beg.data(), P->near_beg, sizeof(int) * (P->nf + 1), cudaMemcpyDeviceToHost));
+    FMM_CUDA_TRY(cudaMemcpy(col.data(), P->near_col, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+    std::vector<int> tb(P->nf + 1, 0), tc(nnz), fill(P->nf, 0);
+    std::vector<long long> perm(nnz);
+    for (long long s = 0; s < nnz; s++) tb[col[s] + 1]++;
+    for (int j = 0; j < P->nf; j++) tb[j + 1] += tb[j];
+    for (int i = 0; i < P->nf; i++)
+        for (int s = beg[i]; s < beg[i + 1]; s++) {
+            int j = col[s];
+            long long pos = tb[j] + fill[j]++;
+            tc[pos] = i;
+            perm[pos] = s;
+        }
+    long long *perm_dev = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&perm_dev, sizeof(long long) * std::max<long long>(1, nnz)));
+    FMM_CUDA_TRY(cudaMemcpy(perm_dev, perm.data(), sizeof(long long) * nnz, cudaMemcpyHostToDevice));
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->nearT_beg, sizeof(int) * (P->nf + 1)));
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->nearT_col, sizeof(int) * std::max<long long>(1, nnz)));
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->nearT64, sizeof(double2) * std::max<long long>(1, nnz)));
+    FMM_CUDA_TRY(cudaMemcpy(P->nearT_beg, tb.data(), sizeof(int) * (P->nf + 1), cudaMemcpyHostToDevice));
+    FMM_CUDA_TRY(cudaMemcpy(P->nearT_col, tc.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
+    gather_kernel<<<152 * 8, 256, 0, P->stream>>>(P->near64, perm_dev, nnz, P->nearT64);
+    FMM_CUDA_TRY(cudaGetLastError());
+    if (P->U32) {
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&P->nearT32, sizeof(float2) * std::max<long long>(1, nnz)));
+        int blocks = 152 * 8;
+        to_float_kernel2<<<blocks, 256, 0, P->stream>>>((const double *)P->nearT64, (float *)P->nearT32, 2 * (size_t)nnz);
+        FMM_CUDA_TRY(cudaGetLastError());
+    }
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    cudaFree(perm_dev);
+    return FMM_OK;
 }
 
 
@@ -530,6 +627,10 @@ int build_dir_groups(Plan *P)
 int tune_m2l(Plan *P)
 {
     if (!P->U32) return FMM_OK;
+    {
+        int st = set_smem_attrs<float>(P->pmax);
+        if (st) return st;
+    }
     cudaEvent_t a, b;
     FMM_CUDA_TRY(cudaEventCreate(&a));
     FMM_CUDA_TRY(cudaEventCreate(&b));

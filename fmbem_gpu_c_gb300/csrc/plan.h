@@ -68,6 +68,9 @@ struct Plan {
     double2 *near64 = nullptr;
     float2 *near32 = nullptr;
     long long num_near = 0;
+    int *nearT_beg = nullptr, *nearT_col = nullptr; // transposed near field, built on first use
+    double2 *nearT64 = nullptr;
+    float2 *nearT32 = nullptr;
     // work vectors
     double2 *xbuf = nullptr, *ybuf = nullptr;
     int nrhs_cap = 0;
@@ -101,7 +104,9 @@ int gen_coax_matrices_f32(double k, const double *t, int n, int p, int sr, float
 int build_lists(Plan *P);
 
 // passes.cu
-int run_matvec(Plan *P, const double2 *x, double2 *y, int precision);
+int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpose = 0);
+int build_transpose(Plan *P);
+void launch_conj(Plan *P, const double2 *x, double2 *y);
 int build_dir_groups(Plan *P);
 int tune_m2l(Plan *P);
 

@@ -324,6 +324,23 @@ __global__ void coax_kernel(double k, const double *tvals, int p, int sr, double
 #undef EE
 }
 
+// The mixed-precision path stores the coaxial blocks in FP32.  At high order and small
+// k t the (S|R) entries grow like h_{2p-2}(k t) and can leave the float range; refuse to
+// build such a plan rather than carry inf through the matvec.
+static int check_fp32_range(const double2 *dev, size_t n, int l)
+{
+    std::vector<double2> h(n);
+    FMM_CUDA_TRY(cudaMemcpy(h.data(), dev, sizeof(double2) * n, cudaMemcpyDeviceToHost));
+    double mx = 0.0;
+    for (size_t i = 0; i < n; i++) mx = std::max(mx, std::max(fabs(h[i].x), fabs(h[i].y)));
+    if (!(mx < 1e37)) {
+        fmm_set_error("level %d coaxial entries reach %.3g, beyond FP32 range: lower p at this level or build "
+                      "without the mixed-precision tables", l, mx);
+        return FMM_ERR_ARG;
+    }
+    return FMM_OK;
+}
+
 int gen_coax_tables(Plan *P)
 {
     double k = P->opt.k;
@@ -353,6 +370,8 @@ int gen_coax_tables(Plan *P)
         FMM_CUDA_TRY(cudaGetLastError());
         FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
         if (P->opt.build_mixed) {
+            int st = check_fp32_range(L.Csr64, (size_t)NDIST * coax_size(p), l);
+            if (st != FMM_OK) return st;
             FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Csr32, sizeof(float2) * NDIST * coax_size(p)));
             to_float((const double *)L.Csr64, (float *)L.Csr32, (size_t)2 * NDIST * coax_size(p), P->stream);
         }
