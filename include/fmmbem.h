@@ -21,6 +21,7 @@
 #ifndef FMMBEM_H
 #define FMMBEM_H
 #include <cuComplex.h>
+#include <cuda_runtime_api.h>
 #include <stddef.h>
 
 #ifdef __cplusplus
@@ -106,6 +107,28 @@ int fmm_plane_wave_rhs(fmm_plan *plan, const double *dir, cuDoubleComplex *rhs);
  * nv/nf; with V or F NULL only the counts are returned.  Vertex coordinates are rounded to
  * 9 significant digits, the precision an OBJ writer of this library emits. */
 int fmm_mesh_icosphere(int subdiv, double radius, double *V, int *nv, int *F, int *nf);
+
+/* Coaxial translation matrices in FP64, without any device allocation.  This entry point has
+ * no counterpart in the reference.  It is meant for callers that must not let a library
+ * allocate device memory: an application that owns all device memory through its own pool,
+ * a loop with timing limits where cudaMalloc/cudaFree would synchronise the device, or code
+ * that only holds buffers it was handed.
+ *   Input: t[n] translation lengths (device memory of the current device), wavenumber k,
+ *   order p (1..64), sr = 1 for (S|R) and 0 for (R|R).
+ *   Output: out[n * sparseCoaxTransSize(p)] on the current device, with matrix i at
+ *   i * sparseCoaxTransSize(p), in the sparse layout of genSRSparseCoaxTransMat.
+ * The kernel runs on `stream` and nothing is synchronised.  Its scratch is a fixed 8 MiB
+ * array that the library holds on every device it is used on; a call needs
+ * n * p * (2p-1) * p <= 2^19 complex entries and is rejected with FMM_ERR_ARG above that
+ * (e.g. p = 30: n <= 9).  Nothing has to be zeroed first.  A matrix whose k*t is not in
+ * (0, 1e5] comes out as NaN.
+ * The first call on each device looks up the scratch address (cudaGetSymbolAddress), which
+ * loads the library's device code on that device if it is not loaded yet.  Make that first
+ * call before any stream capture.  Calls share one scratch per device: two calls whose
+ * kernels overlap (different streams or host threads without ordering) race and corrupt
+ * each other's results, so order them on one stream or with events. */
+int fmm_coax_matrices_noalloc(double k, const double *t, int n, int p, int sr, cuDoubleComplex *out,
+                              cudaStream_t stream);
 
 /* Last error message of the calling thread (static storage). */
 const char *fmm_last_error(void);
