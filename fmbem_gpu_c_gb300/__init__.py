@@ -65,6 +65,7 @@ def lib():
         L.fmm_plan_destroy.argtypes = [c_vp]
         L.fmm_plan_info.argtypes = [c_vp, ctypes.POINTER(Info)]
         L.fmm_matvec.argtypes = [c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_int]
+        L.fmm_matvec_adjoint.argtypes = [c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.fmm_gmres.argtypes = [c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                 c_ip, c_dp]
         L.fmm_far_field.argtypes = [c_vp, c_vp, c_dp, ctypes.c_int, c_vp]
@@ -148,6 +149,19 @@ class Plan:
                 out = np.empty_like(x)
         nrhs = (x.numel() if hasattr(x, "numel") else x.size) // self.nf
         _check(lib().fmm_matvec(self.h, _ptr(x), _ptr(out), nrhs, precision))
+        return out
+
+    def matvec_adjoint(self, x, precision=FMM_FP64, conjugate=False, out=None):
+        """y = A^T x, or A^H x with conjugate=True (vector-Jacobian products, adjoint solves)."""
+        if out is None:
+            if hasattr(x, "data_ptr"):
+                import torch
+                out = torch.empty_like(x)
+            else:
+                x = np.ascontiguousarray(x, dtype=np.complex128)
+                out = np.empty_like(x)
+        nrhs = (x.numel() if hasattr(x, "numel") else x.size) // self.nf
+        _check(lib().fmm_matvec_adjoint(self.h, _ptr(x), _ptr(out), nrhs, precision, 1 if conjugate else 0))
         return out
 
     def gmres(self, b, x0=None, tol=1e-6, maxit=500, restart=50, precision=FMM_FP64):

@@ -247,6 +247,44 @@ extern "C" int fmm_matvec(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComp
     return FMM_OK;
 }
 
+// Transposed operator: the sources become point sources at the centroids (multipole
+// R_n^{-m}(y_i - c)) and the targets element integrals (local expansion integrated against
+// b R + c dR/dn), with the same translation tables; the near field is the transposed CSR.
+// A^H x = conj(A^T conj(x)).
+extern "C" int fmm_matvec_adjoint(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComplex *y, int nrhs, int precision,
+                                  int conjugate)
+{
+    Plan *P = (Plan *)plan;
+    if (!P || !x || !y || nrhs < 1) { fmm_set_error("invalid argument"); return FMM_ERR_ARG; }
+    if (precision != FMM_FP64 && precision != FMM_MIXED) { fmm_set_error("unknown precision %d", precision); return FMM_ERR_ARG; }
+    {
+        int st = build_transpose(P);
+        if (st) return st;
+    }
+    bool xd = is_device_ptr(x), yd = is_device_ptr(y);
+    for (int r = 0; r < nrhs; r++) {
+        const double2 *xs = (const double2 *)x + (size_t)r * P->nf;
+        double2 *ys = (double2 *)y + (size_t)r * P->nf;
+        const double2 *xin = xs;
+        double2 *yout = yd ? ys : P->ybuf;
+        if (!xd) {
+            FMM_CUDA_TRY(cudaMemcpyAsync(P->xbuf, xs, sizeof(double2) * P->nf, cudaMemcpyHostToDevice, P->stream));
+            xin = P->xbuf;
+        }
+        if (conjugate) {
+            launch_conj(P, xin, P->xbuf);
+            xin = P->xbuf;
+        }
+        int st = run_matvec(P, xin, yout, precision, 1);
+        if (st) return st;
+        if (conjugate) launch_conj(P, yout, yout);
+        FMM_CUDA_TRY(cudaGetLastError());
+        if (!yd) FMM_CUDA_TRY(cudaMemcpyAsync(ys, P->ybuf, sizeof(double2) * P->nf, cudaMemcpyDeviceToHost, P->stream));
+    }
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    return FMM_OK;
+}
+
 extern "C" int fmm_set_profiling(fmm_plan *plan, int on)
 {
     if (!plan) return FMM_ERR_ARG;

@@ -90,6 +90,14 @@ int fmm_plan_info(const fmm_plan *plan, fmm_info *info);
  * host or device pointers. */
 int fmm_matvec(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComplex *y, int nrhs, int precision);
 
+/* y = A^T x (conjugate = 0) or y = A^H x (conjugate = 1), the transposed / adjoint operator
+ * of fmm_matvec for reverse-mode derivatives (vector-Jacobian products) and adjoint solves.
+ * Same translation tables and lists; the near-field matrix is transposed on the first call
+ * (one extra CSR copy on the device).  No counterpart in the reference, whose operator is
+ * only applied forward. */
+int fmm_matvec_adjoint(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComplex *y, int nrhs, int precision,
+                       int conjugate);
+
 /* Solve A x = b with restarted GMRES (FP64 Arnoldi).  FMM_FP64 runs plain GMRES on the FP64
  * matvec; FMM_MIXED runs iterative refinement: FP64 outer residual, inner GMRES on the
  * mixed-precision matvec.  x holds the initial guess on entry.  iters/relres may be NULL. */

@@ -840,7 +840,22 @@ orc_fmm *orc_fmm_create(int nv, const double *V, int nf, const int *F, double k,
 long long orc_fmm_num_sr(const orc_fmm *f, int l) { return f->lev[l].sr_beg[f->lev[l].nb]; }
 long long orc_fmm_num_near(const orc_fmm *f) { return f->near_beg[f->nf]; }
 
-void orc_fmm_apply(orc_fmm *f, const double *xin, double *yout)
+/* Index of (n, -m) for the coefficient at nm_idx(n, m) = n^2 + n + m. */
+static size_t flip_nm(size_t i)
+{
+    size_t n = (size_t)sqrt((double)i);
+    while (n * n > i) n--;
+    while ((n + 1) * (n + 1) <= i) n++;
+    return 2 * (n * n + n) - i;
+}
+
+/* transpose = 0: y = A x as the reference's FMM pipeline computes it.
+ * transpose = 1: y = A^T x.  The reference has no transposed operator; this one follows from
+ * G(x, y) = G(y, x): the inputs become point sources at the element centroids (multipole
+ * coefficients ik x_i R_n^{-m}(y_i - c), the centroid basis read at (n, -m)), every
+ * translation is unchanged, the local expansion is integrated over the target element (the
+ * element moments read at (n, -m)), and the near-field matrix is applied transposed. */
+void orc_fmm_apply2(orc_fmm *f, const double *xin, double *yout, int transpose)
 {
     const cplx *x = (const cplx *)xin;
     cplx *y = (cplx *)yout;
@@ -861,8 +876,13 @@ void orc_fmm_apply(orc_fmm *f, const double *xin, double *yout)
         for (int s = f->leaf_beg[b]; s < f->leaf_beg[b + 1]; s++) {
             int e = f->leaf_elem[s];
             cplx xe = ik * x[e];
-            const cplx *U = f->U + e * ppl;
-            for (size_t i = 0; i < ppl; i++) C[i] += xe * U[i];
+            if (transpose) {
+                const cplx *Rv = f->Rv + e * ppl;
+                for (size_t i = 0; i < ppl; i++) C[i] += xe * Rv[flip_nm(i)];
+            } else {
+                const cplx *U = f->U + e * ppl;
+                for (size_t i = 0; i < ppl; i++) C[i] += xe * U[i];
+            }
         }
     }
     /* M2M, the parent owns its sum */
@@ -921,16 +941,30 @@ void orc_fmm_apply(orc_fmm *f, const double *xin, double *yout)
         }
     }
     /* near field + L2P + identity */
+    if (transpose) {
+        for (int e = 0; e < f->nf; e++) y[e] = f->a * x[e];
+        for (int i = 0; i < f->nf; i++)
+            for (int s = f->near_beg[i]; s < f->near_beg[i + 1]; s++) y[f->near_col[s]] += f->near_val[s] * x[i];
+    }
 #pragma omp parallel for num_threads(f->nthreads) schedule(dynamic, 64)
     for (int e = 0; e < f->nf; e++) {
-        cplx acc = f->a * x[e];
-        for (int s = f->near_beg[e]; s < f->near_beg[e + 1]; s++) acc += f->near_val[s] * x[f->near_col[s]];
         const cplx *D = LL->Dl + (size_t)f->elem_leaf[e] * ppl;
-        const cplx *R = f->Rv + e * ppl;
-        for (size_t i = 0; i < ppl; i++) acc += D[i] * R[i];
+        cplx acc;
+        if (transpose) {
+            acc = y[e];
+            const cplx *U = f->U + e * ppl;
+            for (size_t i = 0; i < ppl; i++) acc += D[i] * U[flip_nm(i)];
+        } else {
+            acc = f->a * x[e];
+            for (int s = f->near_beg[e]; s < f->near_beg[e + 1]; s++) acc += f->near_val[s] * x[f->near_col[s]];
+            const cplx *R = f->Rv + e * ppl;
+            for (size_t i = 0; i < ppl; i++) acc += D[i] * R[i];
+        }
         y[e] = acc;
     }
 }
+
+void orc_fmm_apply(orc_fmm *f, const double *xin, double *yout) { orc_fmm_apply2(f, xin, yout, 0); }
 
 void orc_fmm_destroy(orc_fmm *f)
 {
@@ -973,6 +1007,35 @@ void orc_dense_apply(int nv, const double *V, int nf, const int *F, double k,
             acc += v * x[j];
         }
         y[i] = acc;
+    }
+}
+
+/* The dense operator as an explicit nf x nf row-major matrix, entry (i, j) = a delta_ij +
+ * the quadrature of element j at the centroid of element i: the coefficients orc_dense_apply
+ * sums.  Used to check the transposed and adjoint operators on small meshes. */
+void orc_dense_matrix(int nv, const double *V, int nf, const int *F, double k,
+                      double a_re, double a_im, double b_re, double b_im, double c_re, double c_im,
+                      int rule, double *out, int nthreads)
+{
+    (void)nv;
+    cplx *A = (cplx *)out;
+    cplx a = a_re + I * a_im, b = b_re + I * b_im, c = c_re + I * c_im;
+#pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) schedule(dynamic, 16)
+    for (int i = 0; i < nf; i++) {
+        double nodi[9], yc[3];
+        for (int t = 0; t < 3; t++)
+            for (int q = 0; q < 3; q++) nodi[3 * t + q] = V[3 * F[3 * i + t] + q];
+        tri_centroid(nodi, yc);
+        for (int j = 0; j < nf; j++) {
+            double nod[9];
+            for (int t = 0; t < 3; t++)
+                for (int q = 0; q < 3; q++) nod[3 * t + q] = V[3 * F[3 * j + t] + q];
+            int sgl = (i == j);
+            cplx v = sgl ? a : 0.0;
+            if (b != 0.0) v += b * (sgl ? elem_integral_sgl(k, nod, 0) : elem_integral(k, nod, yc, rule, 0));
+            if (c != 0.0) v += c * (sgl ? elem_integral_sgl(k, nod, 1) : elem_integral(k, nod, yc, rule, 1));
+            A[(size_t)i * nf + j] = v;
+        }
     }
 }
 

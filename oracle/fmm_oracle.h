@@ -46,6 +46,8 @@ orc_fmm *orc_fmm_create(int nv, const double *V, int nf, const int *F, double k,
                         const int *elem_leaf, const int *p_level, double d, const double *pt_min,
                         int nthreads);
 void orc_fmm_apply(orc_fmm *f, const double *x, double *y);
+/* y = A x (transpose = 0) or y = A^T x (transpose = 1) */
+void orc_fmm_apply2(orc_fmm *f, const double *x, double *y, int transpose);
 void orc_fmm_destroy(orc_fmm *f);
 long long orc_fmm_num_sr(const orc_fmm *f, int l);
 long long orc_fmm_num_near(const orc_fmm *f);
@@ -54,6 +56,12 @@ long long orc_fmm_num_near(const orc_fmm *f);
 void orc_dense_apply(int nv, const double *V, int nf, const int *F, double k,
                      double a_re, double a_im, double b_re, double b_im, double c_re, double c_im,
                      int rule, const double *x, double *y, int nthreads);
+
+/* the same operator as an explicit row-major nf x nf matrix (entry (i, j): element j at
+ * the centroid of element i) */
+void orc_dense_matrix(int nv, const double *V, int nf, const int *F, double k,
+                      double a_re, double a_im, double b_re, double b_im, double c_re, double c_im,
+                      int rule, double *out, int nthreads);
 
 /* scattered field of a rigid body from surface pressure p: sum_e p_e int dG/dn_x(x, y) */
 void orc_far_field(int nv, const double *V, int nf, const int *F, double k, int rule,

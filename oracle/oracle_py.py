@@ -28,6 +28,7 @@ def lib():
         L.orc_fmm_create.argtypes = [ctypes.c_int, c_dp, ctypes.c_int, c_ip, ctypes.c_double] + [ctypes.c_double] * 6 + [
             ctypes.c_int, ctypes.c_int, c_ip, ctypes.POINTER(ctypes.c_longlong), c_ip, c_ip, ctypes.c_double, c_dp, ctypes.c_int]
         L.orc_fmm_apply.argtypes = [ctypes.c_void_p, c_dp, c_dp]
+        L.orc_fmm_apply2.argtypes = [ctypes.c_void_p, c_dp, c_dp, ctypes.c_int]
         L.orc_fmm_destroy.argtypes = [ctypes.c_void_p]
         L.orc_fmm_num_sr.restype = ctypes.c_longlong
         L.orc_fmm_num_sr.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -35,6 +36,7 @@ def lib():
         L.orc_fmm_num_near.argtypes = [ctypes.c_void_p]
         L.orc_dense_apply.argtypes = [ctypes.c_int, c_dp, ctypes.c_int, c_ip, ctypes.c_double] + [ctypes.c_double] * 6 + [
             ctypes.c_int, c_dp, c_dp, ctypes.c_int]
+        L.orc_dense_matrix.argtypes = L.orc_dense_apply.argtypes[:12] + [c_dp, ctypes.c_int]
         L.orc_far_field.argtypes = [ctypes.c_int, c_dp, ctypes.c_int, c_ip, ctypes.c_double, ctypes.c_int, c_dp,
                                     ctypes.c_int, c_dp, c_dp, ctypes.c_int]
         L.orc_mie_rigid.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, c_dp, c_dp]
@@ -191,10 +193,11 @@ class FMM:
     def num_near(self):
         return lib().orc_fmm_num_near(self.h)
 
-    def apply(self, x):
+    def apply(self, x, transpose=False):
+        """y = A x, or y = A^T x with transpose=True."""
         x = np.ascontiguousarray(x, dtype=np.complex128)
         y = np.zeros(self.nf, dtype=np.complex128)
-        lib().orc_fmm_apply(self.h, _d(x.view(np.float64)), _d(y.view(np.float64)))
+        lib().orc_fmm_apply2(self.h, _d(x.view(np.float64)), _d(y.view(np.float64)), 1 if transpose else 0)
         return y
 
     def __del__(self):
@@ -212,6 +215,17 @@ def dense_apply(V, F, k, x, a=0.0, b=0.0, c=0.0, rule=0, nthreads=None):
     lib().orc_dense_apply(len(V), _d(V), len(F), _i(F), k, a.real, a.imag, b.real, b.imag, c.real, c.imag, rule,
                           _d(x.view(np.float64)), _d(y.view(np.float64)), nthreads or os.cpu_count() or 1)
     return y
+
+
+def dense_matrix(V, F, k, a=0.0, b=0.0, c=0.0, rule=0, nthreads=None):
+    """The dense operator of dense_apply as an explicit complex nf x nf matrix (small meshes)."""
+    V = np.ascontiguousarray(V, dtype=np.float64)
+    F = np.ascontiguousarray(F, dtype=np.int32)
+    A = np.zeros((len(F), len(F)), dtype=np.complex128)
+    a, b, c = complex(a), complex(b), complex(c)
+    lib().orc_dense_matrix(len(V), _d(V), len(F), _i(F), k, a.real, a.imag, b.real, b.imag, c.real, c.imag, rule,
+                           _d(A.view(np.float64)), nthreads or os.cpu_count() or 1)
+    return A
 
 
 def far_field(V, F, k, p_surf, pts, rule=0, nthreads=None):

@@ -188,6 +188,25 @@ def test_fmm_oracle_converges_to_dense(oracle):
     assert errs[2] < 2e-6
 
 
+def test_transposed_fmm_oracle_matches_dense_transpose(oracle):
+    """The oracle's transposed FMM (no reference counterpart) against the transpose of the
+    dense operator, to the forward FMM's accuracy, and the bilinear identity."""
+    V, F = meshes.roundtrip(*meshes.icosphere(3, 0.1))
+    k = 2 * np.pi * 1000 / 343.0
+    T = oracle.tree_for_fmm(V, F, depth=3)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(len(F)) + 1j * rng.standard_normal(len(F))
+    y = rng.standard_normal(len(F)) + 1j * rng.standard_normal(len(F))
+    A = oracle.dense_matrix(V, F, k, a=0.3, b=0.7 + 0.2j, c=-1.0, rule=0)
+    assert np.allclose(A @ x, oracle.dense_apply(V, F, k, x, a=0.3, b=0.7 + 0.2j, c=-1.0, rule=0), rtol=0, atol=1e-13)
+    f = oracle.FMM(V, F, k, T, [12, 12], a=0.3, b=0.7 + 0.2j, c=-1.0, rule=0)
+    ax, aty = f.apply(x), f.apply(y, transpose=True)
+    fwd = np.linalg.norm(ax - A @ x) / np.linalg.norm(A @ x)
+    assert fwd < 1e-5
+    assert np.linalg.norm(aty - A.T @ y) / np.linalg.norm(A.T @ y) < 3 * fwd
+    assert abs(y @ ax - x @ aty) < 1e-9 * np.linalg.norm(x) * np.linalg.norm(y) * np.linalg.norm(A, 2)
+
+
 def test_bem_dense_solution_matches_mie(oracle):
     """Rigid sphere (ka = 0.9): dense BEM solve of (1/2 - M) p = p_inc, far field vs Mie."""
     V, F = meshes.roundtrip(*meshes.icosphere(3, 0.1))
