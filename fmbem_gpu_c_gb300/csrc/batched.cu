@@ -1,0 +1,416 @@
+// Batched translations for the mixed-precision matvec: M2M, M2L and L2L as direction-grouped
+// tiles of register-blocked small matrix products.
+//
+// Every translation is rotation - coaxial - rotation (RCR) as in transMatsVecsMul_SR_rcr
+// (reference translation.cu:1864-1961).  All translations of one level that share a
+// direction (one of 316 M2L offsets, or one of 8 octants for M2M/L2L) use the same real
+// rotation block H, the same phases e^{i m phi} and the same coaxial blocks.  A CTA takes TC
+// of them as the columns of a matrix:
+//   stage 0  gather the TC source vectors into shared memory as X[nm][t] and apply
+//            e^{i m phi} (zero-padded to order p, zero columns beyond the item's count);
+//   stage 1  W_n = H_n X_n for every degree n (H_n is (2n+1) x (2n+1), real);
+//   stage 2  X_m = C_|m| W_m for every order m (C_|m| is the (p-|m|)^2 coaxial block, complex;
+//            +m and -m share it);
+//   stage 3  Y_n = H_n X_n for n < pout, times e^{-i m' phi}, added into the destinations.
+// A thread computes R rows x CG columns of one block per unit of work (CG = TC, or 16-column
+// groups when TC is 32 or 64): the CG-wide rows of X and W are read as shared-memory
+// broadcasts and every H or C entry loaded from L1/L2 feeds 2 CG (real H) or 4 CG (complex
+// C) FMAs.  Units are ordered by cost within each column group so the long blocks start
+// first.  Destinations are added with FP32 vector atomics where several items reach
+// the same box (M2M, M2L), and with a plain read-add-write where every box is reached once
+// (L2L).
+#include "plan.h"
+#include <algorithm>
+#include <vector>
+
+namespace fmm {
+
+struct RcrPass {
+    int p, pin, pout, atomic;        // RCR order, source order, destination order
+    int hstride, phstride, phoff;    // per-direction strides of H and the phases; phase index m + phoff
+    const float *H;
+    const float2 *PH;
+    const float2 *Cc;                // coaxial blocks, item.w selects one (stride coax_size(p))
+    const float2 *src;               // [boxes][pin^2]
+    float2 *dst;                     // [boxes][pout^2]
+    const int4 *items;               // (direction, first, count, coaxial block)
+    const int *g_src, *g_dst;
+};
+
+static __device__ __forceinline__ void nm_of(int i, int &n, int &m)
+{
+    int q = (int)sqrtf((float)i);
+    while (q * q > i) q--;
+    while ((q + 1) * (q + 1) <= i) q++;
+    n = q;
+    m = i - q * q - q;
+}
+
+// Tiles X and W hold p^2 rows of TC complex columns.  The 16-byte chunks of row q are
+// XOR-swizzled by q mod 8 (mod TC/2 for TC = 8) so that units reading rows of different
+// degrees in one warp hit different banks.
+template <int TC>
+static __device__ __forceinline__ float4 *chunk(float2 *base, int row, int ch)
+{
+    constexpr int M = (TC / 2 < 8 ? TC / 2 : 8) - 1;
+    return reinterpret_cast<float4 *>(base + (size_t)row * TC) + (ch ^ (row & M));
+}
+
+// rows row0..row0+R-1 of W_n = H_n X_n (r = 2n+1 rows) for the CG columns starting at chunk
+// ch0; X row of step m is rb + m; Hn column-major (m', m).  The H entries of step m+1 are
+// loaded while step m computes.
+template <int TC, int CG, int R>
+static __device__ __forceinline__ void rot_rows(const float *__restrict__ Hn, int r, int row0, float2 *X, int rb,
+                                                int ch0, float2 (&acc)[R][CG])
+{
+#pragma unroll
+    for (int k = 0; k < R; k++)
+#pragma unroll
+        for (int t = 0; t < CG; t++) acc[k][t] = make_float2(0.f, 0.f);
+    float hn[R];
+#pragma unroll
+    for (int k = 0; k < R; k++) hn[k] = (row0 + k < r) ? Hn[row0 + k] : 0.f;
+    for (int m = 0; m < r; m++) {
+        float h[R];
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+            h[k] = hn[k];
+            hn[k] = (m + 1 < r && row0 + k < r) ? Hn[(m + 1) * r + row0 + k] : 0.f;
+        }
+#pragma unroll
+        for (int c = 0; c < CG / 2; c++) {
+            float4 x = *chunk<TC>(X, rb + m, ch0 + c);
+#pragma unroll
+            for (int k = 0; k < R; k++) {
+                acc[k][2 * c].x = fmaf(h[k], x.x, acc[k][2 * c].x);
+                acc[k][2 * c].y = fmaf(h[k], x.y, acc[k][2 * c].y);
+                acc[k][2 * c + 1].x = fmaf(h[k], x.z, acc[k][2 * c + 1].x);
+                acc[k][2 * c + 1].y = fmaf(h[k], x.w, acc[k][2 * c + 1].y);
+            }
+        }
+    }
+}
+
+static __device__ __forceinline__ void cmac(float2 &acc, float2 c, float ar, float ai)
+{
+    acc.x = fmaf(c.x, ar, acc.x);
+    acc.x = fmaf(-c.y, ai, acc.x);
+    acc.y = fmaf(c.x, ai, acc.y);
+    acc.y = fmaf(c.y, ar, acc.y);
+}
+
+// SHC also stages the direction's rotation block and coaxial block in shared memory, after
+// the two tiles.
+template <int TC, int CG, int R1, int R2, bool SHC>
+__global__ void __launch_bounds__(256, 2) rcr_tile_kernel(RcrPass ps)
+{
+    extern __shared__ float4 smem4[];
+    const int p = ps.p, pp = p * p;
+    float2 *X = reinterpret_cast<float2 *>(smem4);
+    float2 *W = X + (size_t)pp * TC;
+    float2 *sC = W + (size_t)pp * TC;
+    float *sH = reinterpret_cast<float *>(sC + coax_size(p));
+    __shared__ int s_src[TC], s_dst[TC];
+    const int4 it = ps.items[blockIdx.x];
+    const int cnt = it.z;
+    const float *Hg = ps.H + (size_t)it.x * ps.hstride;
+    const float2 *ph = ps.PH + (size_t)it.x * ps.phstride + ps.phoff;
+    const float2 *Cg = ps.Cc + (size_t)it.w * coax_size(p);
+    const float *H = SHC ? sH : Hg;
+    const float2 *Cc = SHC ? sC : Cg;
+    if (threadIdx.x < TC) {
+        bool v = (int)threadIdx.x < cnt;
+        s_src[threadIdx.x] = v ? ps.g_src[it.y + threadIdx.x] : -1;
+        s_dst[threadIdx.x] = v ? ps.g_dst[it.y + threadIdx.x] : -1;
+    }
+    if (SHC) {
+        const int rs = rot_size(p), cs = coax_size(p);
+        for (int i = threadIdx.x; i < rs; i += blockDim.x) sH[i] = __ldg(Hg + i);
+        for (int i = threadIdx.x; i < cs; i += blockDim.x) sC[i] = __ldg(Cg + i);
+    }
+    __syncthreads();
+
+    // stage 0: gather, phase, zero padding
+    const int pin = min(ps.pin, p), pin2 = pin * pin, sstride = ps.pin * ps.pin;
+    for (int i = threadIdx.x; i < pp * TC; i += blockDim.x) {
+        int nm = i / TC, t = i % TC;
+        float2 v = make_float2(0.f, 0.f);
+        int s = s_src[t];
+        if (s >= 0 && nm < pin2) {
+            int n, m;
+            nm_of(nm, n, m);
+            v = cmul(__ldg(ps.src + (size_t)s * sstride + nm), ph[m]);
+        }
+        reinterpret_cast<float2 *>(chunk<TC>(X, nm, t >> 1))[t & 1] = v;
+    }
+    __syncthreads();
+
+    // stage 1: W_n = H_n X_n, n < p; a unit is R1 rows x CG columns, longest blocks first
+    constexpr int G = TC / CG, HC = CG / 2;
+    int U = 0;
+    for (int n = 0; n < p; n++) U += (2 * n + R1) / R1;
+    for (int u = threadIdx.x; u < U * G; u += blockDim.x) {
+        const int g = u / U;
+        int n = p - 1, q = u - g * U;
+        while (q >= (2 * n + R1) / R1) {
+            q -= (2 * n + R1) / R1;
+            n--;
+        }
+        const int r = 2 * n + 1, row0 = q * R1;
+        float2 acc[R1][CG];
+        rot_rows<TC, CG, R1>(H + rot_off(n), r, row0, X, n * n, g * HC, acc);
+#pragma unroll
+        for (int k = 0; k < R1; k++)
+            if (row0 + k < r) {
+#pragma unroll
+                for (int c = 0; c < HC; c++)
+                    *chunk<TC>(W, n * n + row0 + k, g * HC + c) =
+                        make_float4(acc[k][2 * c].x, acc[k][2 * c].y, acc[k][2 * c + 1].x, acc[k][2 * c + 1].y);
+            }
+    }
+    __syncthreads();
+
+    // stage 2: X_{+-m} = C_|m| W_{+-m} for the rows n' < nq (the ones stage 3 reads)
+    const int nq = min(ps.pout, p);
+    U = 0;
+    for (int am = 0; am < nq; am++) U += (nq - am + R2 - 1) / R2;
+    for (int u = threadIdx.x; u < U * G; u += blockDim.x) {
+        const int g = u / U;
+        int am = 0, q = u - g * U;
+        while (q >= (nq - am + R2 - 1) / R2) {
+            q -= (nq - am + R2 - 1) / R2;
+            am++;
+        }
+        const int sz = p - am, nrow = nq - am, j0 = q * R2;
+        const float2 *Cb = Cc + coax_off(p, am);
+        float2 accP[R2][CG], accM[R2][CG];
+#pragma unroll
+        for (int k = 0; k < R2; k++)
+#pragma unroll
+            for (int t = 0; t < CG; t++) accP[k][t] = accM[k][t] = make_float2(0.f, 0.f);
+        float2 cn[R2];
+#pragma unroll
+        for (int k = 0; k < R2; k++) cn[k] = (j0 + k < nrow) ? Cb[j0 + k] : make_float2(0.f, 0.f);
+        for (int j = 0; j < sz; j++) {
+            float2 c[R2];
+#pragma unroll
+            for (int k = 0; k < R2; k++) {
+                c[k] = cn[k];
+                cn[k] = (j + 1 < sz && j0 + k < nrow) ? Cb[(j + 1) * sz + j0 + k] : make_float2(0.f, 0.f);
+            }
+            const int n = am + j, rp = n * n + n + am, rm = n * n + n - am;
+#pragma unroll
+            for (int cc = 0; cc < HC; cc++) {
+                float4 a = *chunk<TC>(W, rp, g * HC + cc), b = *chunk<TC>(W, rm, g * HC + cc);
+#pragma unroll
+                for (int k = 0; k < R2; k++) {
+                    cmac(accP[k][2 * cc], c[k], a.x, a.y);
+                    cmac(accP[k][2 * cc + 1], c[k], a.z, a.w);
+                    cmac(accM[k][2 * cc], c[k], b.x, b.y);
+                    cmac(accM[k][2 * cc + 1], c[k], b.z, b.w);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < R2; k++)
+            if (j0 + k < nrow) {
+                const int np = am + j0 + k;
+#pragma unroll
+                for (int cc = 0; cc < HC; cc++) {
+                    *chunk<TC>(X, np * np + np + am, g * HC + cc) =
+                        make_float4(accP[k][2 * cc].x, accP[k][2 * cc].y, accP[k][2 * cc + 1].x, accP[k][2 * cc + 1].y);
+                    if (am > 0)
+                        *chunk<TC>(X, np * np + np - am, g * HC + cc) = make_float4(
+                            accM[k][2 * cc].x, accM[k][2 * cc].y, accM[k][2 * cc + 1].x, accM[k][2 * cc + 1].y);
+                }
+            }
+    }
+    __syncthreads();
+
+    // stage 3: Y_n = e^{-i m' phi} H_n X_n for n < nq, into the destinations
+    const int po2 = ps.pout * ps.pout;
+    U = 0;
+    for (int n = 0; n < nq; n++) U += (2 * n + R1) / R1;
+    for (int u = threadIdx.x; u < U * G; u += blockDim.x) {
+        const int g = u / U;
+        int n = nq - 1, q = u - g * U;
+        while (q >= (2 * n + R1) / R1) {
+            q -= (2 * n + R1) / R1;
+            n--;
+        }
+        const int r = 2 * n + 1, row0 = q * R1;
+        float2 acc[R1][CG];
+        rot_rows<TC, CG, R1>(H + rot_off(n), r, row0, X, n * n, g * HC, acc);
+#pragma unroll
+        for (int k = 0; k < R1; k++) {
+            if (row0 + k >= r) continue;
+            const float2 e = ph[row0 + k - n];
+            const int idx = n * n + row0 + k;
+#pragma unroll
+            for (int c = 0; c < CG; c++) {
+                const int t = g * CG + c;
+                if (t >= cnt) break;
+                float2 a = acc[k][c];
+                float2 v = make_float2(e.x * a.x + e.y * a.y, e.x * a.y - e.y * a.x);
+                float2 *d = ps.dst + (size_t)s_dst[t] * po2 + idx;
+                if (ps.atomic) {
+                    atomicAdd(d, v);
+                } else {
+                    float2 o = *d;
+                    *d = make_float2(o.x + v.x, o.y + v.y);
+                }
+            }
+        }
+    }
+}
+
+size_t rcr_tile_smem(int p, int tc, int shc)
+{
+    size_t s = 2 * (size_t)p * p * tc * sizeof(float2);
+    if (shc) s += (size_t)coax_size(p) * sizeof(float2) + (size_t)rot_size(p) * sizeof(float);
+    return s;
+}
+
+template <int TC, int CG, int R1, int R2, bool SHC>
+static int launch_tile(const RcrPass &ps, int n_items, size_t sm, cudaStream_t st)
+{
+    static size_t attr = 0;
+    if (sm > attr) {
+        FMM_CUDA_TRY(cudaFuncSetAttribute(rcr_tile_kernel<TC, CG, R1, R2, SHC>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr = sm;
+    }
+    rcr_tile_kernel<TC, CG, R1, R2, SHC><<<n_items, 256, sm, st>>>(ps);
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
+int launch_rcr_pass(const RcrList &Lst, int p, int pin, int pout, int atomic, const float *H, int hstride,
+                    const float2 *PH, int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst,
+                    cudaStream_t st)
+{
+    if (Lst.n_items == 0) return FMM_OK;
+    RcrPass ps;
+    ps.p = p;
+    ps.pin = pin;
+    ps.pout = pout;
+    ps.atomic = atomic;
+    ps.hstride = hstride;
+    ps.phstride = phstride;
+    ps.phoff = phoff;
+    ps.H = H;
+    ps.PH = PH;
+    ps.Cc = Cc;
+    ps.src = src;
+    ps.dst = dst;
+    ps.items = Lst.items;
+    ps.g_src = Lst.src;
+    ps.g_dst = Lst.dst;
+    size_t sm = rcr_tile_smem(p, Lst.tc, Lst.shc);
+    if (Lst.shc) {
+        switch (Lst.tc) {
+        case 64: return launch_tile<64, 16, 2, 1, true>(ps, Lst.n_items, sm, st);
+        case 32: return launch_tile<32, 16, 2, 1, true>(ps, Lst.n_items, sm, st);
+        case 16: return launch_tile<16, 16, 2, 1, true>(ps, Lst.n_items, sm, st);
+        default: return launch_tile<8, 8, 4, 2, true>(ps, Lst.n_items, sm, st);
+        }
+    }
+    switch (Lst.tc) {
+    case 64: return launch_tile<64, 16, 2, 1, false>(ps, Lst.n_items, sm, st);
+    case 32: return launch_tile<32, 16, 2, 1, false>(ps, Lst.n_items, sm, st);
+    case 16: return launch_tile<16, 16, 2, 1, false>(ps, Lst.n_items, sm, st);
+    default: return launch_tile<8, 8, 4, 2, false>(ps, Lst.n_items, sm, st);
+    }
+}
+
+// Shared memory that keeps two CTAs on an SM: 228 KB per SM, 1 KB reserved and the static
+// arrays per CTA.
+static const size_t TWO_CTA_SMEM = (228 * 1024) / 2 - 1024 - 1024;
+
+// Columns per CTA: the largest of 64, 32, 16 whose tiles (and, where they also fit, the
+// staged rotation and coaxial blocks) keep two CTAs per SM, else 8 (one CTA per SM, p <= 42).
+// With 16-column groups that gives every thread of the CTA a unit of work down to p = 10.
+static void pick_tile(int p, int &tc, int &shc)
+{
+    for (tc = 64; tc >= 16; tc /= 2) {
+        if (rcr_tile_smem(p, tc, 1) <= TWO_CTA_SMEM) { shc = 1; return; }
+        if (rcr_tile_smem(p, tc, 0) <= TWO_CTA_SMEM) { shc = 0; return; }
+    }
+    tc = 8;
+    shc = 0;
+}
+
+static int upload_list(Plan *P, RcrList &Lst, const std::vector<int> &key, const std::vector<int> &src,
+                       const std::vector<int> &dst, int nkeys, const std::vector<int> &key_w, int p)
+{
+    int tc, shc;
+    pick_tile(p, tc, shc);
+    size_t T = key.size();
+    std::vector<int> cnt(nkeys + 1, 0);
+    for (size_t i = 0; i < T; i++) cnt[key[i] + 1]++;
+    for (int d = 0; d < nkeys; d++) cnt[d + 1] += cnt[d];
+    std::vector<int> gs(std::max<size_t>(T, 1)), gd(std::max<size_t>(T, 1)), fill(nkeys, 0);
+    for (size_t i = 0; i < T; i++) {
+        int pos = cnt[key[i]] + fill[key[i]]++;
+        gs[pos] = src[i];
+        gd[pos] = dst[i];
+    }
+    std::vector<int4> items;
+    for (int d = 0; d < nkeys; d++)
+        for (int a = cnt[d]; a < cnt[d + 1]; a += tc) items.push_back(make_int4(d, a, std::min(tc, cnt[d + 1] - a), key_w[d]));
+    Lst.n_items = (int)items.size();
+    Lst.tc = tc;
+    Lst.shc = shc;
+    if (items.empty()) return FMM_OK;
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&Lst.items, sizeof(int4) * items.size()));
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&Lst.src, sizeof(int) * T));
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&Lst.dst, sizeof(int) * T));
+    FMM_CUDA_TRY(cudaMemcpy(Lst.items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+    FMM_CUDA_TRY(cudaMemcpy(Lst.src, gs.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
+    FMM_CUDA_TRY(cudaMemcpy(Lst.dst, gd.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
+    return FMM_OK;
+}
+
+// Work lists of the batched passes: per level, the M2L translations grouped by direction,
+// the M2M pairs (box -> parent) and the L2L pairs (parent -> box) grouped by octant.
+int build_rcr_lists(Plan *P)
+{
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        LevelDev &L = P->lev[l];
+        if (L.num_sr > 0) {
+            long long T = L.num_sr;
+            std::vector<int> beg(L.nb + 1), src(T), dst(T), key(T);
+            std::vector<short> dir(T);
+            FMM_CUDA_TRY(cudaMemcpy(beg.data(), L.sr_beg, sizeof(int) * (L.nb + 1), cudaMemcpyDeviceToHost));
+            FMM_CUDA_TRY(cudaMemcpy(src.data(), L.sr_src, sizeof(int) * T, cudaMemcpyDeviceToHost));
+            FMM_CUDA_TRY(cudaMemcpy(dir.data(), L.sr_dir, sizeof(short) * T, cudaMemcpyDeviceToHost));
+            for (int b = 0; b < L.nb; b++)
+                for (int t = beg[b]; t < beg[b + 1]; t++) {
+                    dst[t] = b;
+                    key[t] = dir[t];
+                }
+            std::vector<int> kw(P->dir_dist, P->dir_dist + NDIR);
+            int st = upload_list(P, L.m2l, key, src, dst, NDIR, kw, L.p);
+            if (st) return st;
+        }
+        if (l > P->lmin) {
+            LevelDev &PL = P->lev[l - 1];
+            std::vector<int> par(L.nb), key(L.nb), self(L.nb);
+            std::vector<unsigned char> oct(L.nb);
+            FMM_CUDA_TRY(cudaMemcpy(par.data(), L.parent, sizeof(int) * L.nb, cudaMemcpyDeviceToHost));
+            FMM_CUDA_TRY(cudaMemcpy(oct.data(), L.octant, L.nb, cudaMemcpyDeviceToHost));
+            for (int b = 0; b < L.nb; b++) {
+                key[b] = oct[b];
+                self[b] = b;
+            }
+            std::vector<int> kw(8, 0);
+            int st = upload_list(P, L.m2m, key, self, par, 8, kw, PL.p);
+            if (st) return st;
+            st = upload_list(P, L.l2l, key, par, self, 8, kw, PL.p);
+            if (st) return st;
+        }
+    }
+    return FMM_OK;
+}
+
+} // namespace fmm

@@ -453,6 +453,8 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
         if (st) return st;
     }
     P->ntimers = 0;
+    P->have_total = 0;
+    if (P->profiling) cudaEventRecord(P->total.beg, st);
     const T *Hsr = f64 ? (const T *)P->Hsr64 : (const T *)P->Hsr32;
     const T *Hss = f64 ? (const T *)P->Hss64 : (const T *)P->Hss32;
     const T *Hrr = f64 ? (const T *)P->Hrr64 : (const T *)P->Hrr32;
@@ -478,7 +480,43 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
     p2m_kernel<T><<<LL.nb, 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, transpose ? Rv : U, x, P->opt.k, Cm(lmax),
                                          transpose);
     timer_end(P);
-    for (int l = lmax; l > lmin; l--) {
+    if (!f64) {
+        // mixed path: batched direction-grouped passes (batched.cu).  M2M and M2L add into
+        // zeroed expansions with atomics; L2L then adds the parents' locals top-down.
+        const int rs = rot_size(pmax), w = 2 * pmax - 1;
+        static const char *l2l_names[] = {"l2l_l0", "l2l_l1", "l2l_l2", "l2l_l3", "l2l_l4", "l2l_l5", "l2l_l6",
+                                          "l2l_l7", "l2l_l8", "l2l_l9", "l2l_l10", "l2l_l11", "l2l_l12", "l2l_l13"};
+        for (int l = lmin; l <= lmax; l++) {
+            size_t n = (size_t)P->lev[l].nb * P->lev[l].p * P->lev[l].p * sizeof(C);
+            if (l < lmax) FMM_CUDA_TRY(cudaMemsetAsync(Cm(l), 0, n, st));
+            FMM_CUDA_TRY(cudaMemsetAsync(Dl(l), 0, n, st));
+        }
+        for (int l = lmax; l > lmin; l--) {
+            LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
+            timer_begin(P, m2m_names[l]);
+            int e = launch_rcr_pass(L.m2m, PL.p, L.p, PL.p, 1, (const float *)Hss, rs, (const float2 *)PHss, w, pmax - 1,
+                                    (const float2 *)Crr(l), (const float2 *)Cm(l), (float2 *)Cm(l - 1), st);
+            if (e) return e;
+            timer_end(P);
+        }
+        for (int l = lmin; l <= lmax; l++) {
+            LevelDev &L = P->lev[l];
+            timer_begin(P, m2l_names[l]);
+            int e = launch_rcr_pass(L.m2l, L.p, L.p, L.p, 1, (const float *)Hsr, rs, (const float2 *)PHsr, w, pmax - 1,
+                                    (const float2 *)Csr(l), (const float2 *)Cm(l), (float2 *)Dl(l), st);
+            if (e) return e;
+            timer_end(P);
+        }
+        for (int l = lmin + 1; l <= lmax; l++) {
+            LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
+            timer_begin(P, l2l_names[l]);
+            int e = launch_rcr_pass(L.l2l, PL.p, PL.p, L.p, 0, (const float *)Hrr, rs, (const float2 *)PHrr, w, pmax - 1,
+                                    (const float2 *)Crr(l), (const float2 *)Dl(l - 1), (float2 *)Dl(l), st);
+            if (e) return e;
+            timer_end(P);
+        }
+    }
+    for (int l = lmax; l > lmin && f64; l--) {
         LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
         size_t sm = 4 * (size_t)PL.p * PL.p * sizeof(C);
         timer_begin(P, m2m_names[l]);
@@ -486,9 +524,8 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
                                                            PHss, Crr(l), Cm(l), Cm(l - 1));
         timer_end(P);
     }
-    for (int l = lmin; l <= lmax; l++) {
-        int st = launch_m2l_level<T>(P, l, f64 ? M2L_SCHED_OWNER : P->lev[l].sched32, f64 ? 1 : P->lev[l].split32,
-                                     m2l_names[l]);
+    for (int l = lmin; l <= lmax && f64; l++) {
+        int st = launch_m2l_level<T>(P, l, M2L_SCHED_OWNER, 1, m2l_names[l]);
         if (st) return st;
     }
     timer_begin(P, "l2p_near");
@@ -498,6 +535,10 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
         P->nf, LL.p, P->elem_leaf, Dl(lmax), transpose ? U : Rv, transpose ? P->nearT_beg : P->near_beg,
         transpose ? P->nearT_col : P->near_col, transpose ? nearT : nearv, x, a, y, transpose);
     timer_end(P);
+    if (P->profiling) {
+        cudaEventRecord(P->total.end, st);
+        P->have_total = 1;
+    }
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
@@ -516,7 +557,7 @@ int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpo
     }
     if (precision == FMM_MIXED) {
         if (!P->U32) {
-            fmm_set_error("plan was created without build_mixed");
+            fmm_set_error("%s", P->mixed_note);
             return FMM_ERR_ARG;
         }
         return run_matvec_t<float>(P, x, y, transpose);

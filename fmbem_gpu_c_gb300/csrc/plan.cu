@@ -68,14 +68,17 @@ static void free_plan(Plan *P)
         F(L.parent); F(L.octant); F(L.child_beg); F(L.child_list); F(L.sr_beg); F(L.sr_src); F(L.sr_dir);
         F(L.Cm64); F(L.Dl64); F(L.Cm32); F(L.Dl32); F(L.Csr64); F(L.Csr32); F(L.Crr64); F(L.Crr32);
         F(L.dir_items); F(L.g_src); F(L.g_dst);
+        for (RcrList *R : {&L.m2l, &L.m2m, &L.l2l}) { F(R->items); F(R->src); F(R->dst); }
     }
     F(P->Hsr64); F(P->PHsr64); F(P->Hsr32); F(P->PHsr32);
     F(P->V_dev); F(P->F_dev); F(P->elem_leaf); F(P->leaf_beg); F(P->leaf_elem);
     F(P->U64); F(P->Rv64); F(P->U32); F(P->Rv32); F(P->near_beg); F(P->near_col); F(P->near64); F(P->near32);
+    F(P->nearT_beg); F(P->nearT_col); F(P->nearT64); F(P->nearT32);
     F(P->xbuf); F(P->ybuf);
     F(P->gm_V); F(P->gm_w); F(P->gm_r); F(P->gm_x); F(P->gm_b); F(P->gm_d); F(P->gm_dev_h);
     if (P->timers_created)
         for (int i = 0; i < MAX_TIMERS; i++) { cudaEventDestroy(P->timers[i].beg); cudaEventDestroy(P->timers[i].end); }
+    if (P->timers_created) { cudaEventDestroy(P->total.beg); cudaEventDestroy(P->total.end); }
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
 }
@@ -127,6 +130,12 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
         P->pmax = std::max(P->pmax, p);
     }
     P->pleaf = P->lev[P->lmax].p;
+    if (P->opt.build_mixed && rcr_tile_smem(P->pmax, 8, 0) > 227 * 1024) {
+        // the batched FP32 translations keep two p^2 x 8 complex tiles in shared memory
+        P->opt.build_mixed = 0;
+        snprintf(P->mixed_note, sizeof(P->mixed_note),
+                 "mixed precision needs truncation orders <= 42 (this plan has %d); use FMM_FP64", P->pmax);
+    }
     if (P->pleaf > 40) { fmm_set_error("leaf truncation order %d above 40", P->pleaf); free_plan(P); return FMM_ERR_ARG; }
     CTRY(dev_alloc(P, (void **)&P->V_dev, sizeof(double) * P->V.size()));
     CTRY(dev_alloc(P, (void **)&P->F_dev, sizeof(int) * P->F.size()));
@@ -143,16 +152,16 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
         size_t n = (size_t)L.nb * L.p * L.p;
         CTRY(dev_alloc(P, (void **)&L.Cm64, sizeof(double2) * n));
         CTRY(dev_alloc(P, (void **)&L.Dl64, sizeof(double2) * n));
-        if (opt->build_mixed) {
+        if (P->opt.build_mixed) {
             CTRY(dev_alloc(P, (void **)&L.Cm32, sizeof(float2) * n));
             CTRY(dev_alloc(P, (void **)&L.Dl32, sizeof(float2) * n));
         }
     }
     TRY(gen_element_tables(P));
     TRY(gen_near_field(P));
-    if (opt->build_mixed) {
-        TRY(build_dir_groups(P));
-        TRY(tune_m2l(P));
+    if (P->opt.build_mixed) {
+        TRY(build_rcr_lists(P));
+        for (int l = P->lmin; l <= P->lmax; l++) P->lev[l].sched32 = M2L_SCHED_BATCHED;
     }
     CTRY(dev_alloc(P, (void **)&P->xbuf, sizeof(double2) * nf));
     CTRY(dev_alloc(P, (void **)&P->ybuf, sizeof(double2) * nf));
@@ -161,6 +170,8 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
         CTRY(cudaEventCreate(&P->timers[i].beg));
         CTRY(cudaEventCreate(&P->timers[i].end));
     }
+    CTRY(cudaEventCreate(&P->total.beg));
+    CTRY(cudaEventCreate(&P->total.end));
     P->timers_created = 1;
     CTRY(cudaStreamSynchronize(P->stream));
     P->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -296,15 +307,17 @@ extern "C" int fmm_last_timings(const fmm_plan *plan, const char **names, double
 {
     const Plan *P = (const Plan *)plan;
     if (!P || !count) return FMM_ERR_ARG;
-    int n = std::min(*count, P->ntimers);
+    int total = P->ntimers + (P->have_total ? 1 : 0);
+    int n = std::min(*count, total);
     for (int i = 0; i < n; i++) {
+        const Timer &tm = i < P->ntimers ? P->timers[i] : P->total;
         float t = 0.f;
-        cudaEventSynchronize(P->timers[i].end);
-        cudaEventElapsedTime(&t, P->timers[i].beg, P->timers[i].end);
-        if (names) names[i] = P->timers[i].name;
+        cudaEventSynchronize(tm.end);
+        cudaEventElapsedTime(&t, tm.beg, tm.end);
+        if (names) names[i] = i < P->ntimers ? tm.name : "matvec";
         if (ms) ms[i] = t;
     }
-    *count = P->ntimers;
+    *count = total;
     return FMM_OK;
 }
 

@@ -11,6 +11,14 @@ constexpr int NDIR = 316;      // M2L offsets (dx,dy,dz) in [-3,3]^3 with max |d
 constexpr int NDIST = 15;      // distinct squared lengths of those offsets
 constexpr int MAX_TIMERS = 64;
 
+// Work list of one batched translation pass: items (direction, first, count, coaxial
+// block) over translations sorted by direction, TC translations per item at most.
+struct RcrList {
+    int4 *items = nullptr;
+    int *src = nullptr, *dst = nullptr;
+    int n_items = 0, tc = 8, shc = 0; // columns per item; rotation/coaxial blocks staged in shared memory
+};
+
 struct LevelDev {
     int nb = 0, p = 0;
     int *parent = nullptr;        // [nb], index in level l-1 (l > lmin)
@@ -34,9 +42,12 @@ struct LevelDev {
     int n_items = 0;              // direction-grouped work items
     int4 *dir_items = nullptr;    // (direction, first, count, 0)
     int *g_src = nullptr, *g_dst = nullptr; // translations sorted by direction
+    // batched passes of the mixed path: M2L of this level, M2M (this level -> parents),
+    // L2L (parents -> this level)
+    RcrList m2l, m2m, l2l;
 };
 
-enum { M2L_SCHED_OWNER = 0, M2L_SCHED_SPLIT = 1, M2L_SCHED_DIR = 2 };
+enum { M2L_SCHED_OWNER = 0, M2L_SCHED_SPLIT = 1, M2L_SCHED_DIR = 2, M2L_SCHED_BATCHED = 3 };
 
 struct Timer {
     const char *name;
@@ -76,10 +87,13 @@ struct Plan {
     int nrhs_cap = 0;
     cudaStream_t stream = nullptr;
     size_t device_bytes = 0;
+    char mixed_note[160] = "plan was created without build_mixed";
     double setup_seconds = 0.0;
     // profiling
     int profiling = 0;
     Timer timers[MAX_TIMERS];
+    Timer total;                  // whole matvec, recorded when profiling
+    int have_total = 0;
     int ntimers = 0, timers_created = 0;
     // GMRES workspace
     double2 *gm_V = nullptr, *gm_w = nullptr, *gm_r = nullptr, *gm_x = nullptr, *gm_b = nullptr, *gm_d = nullptr;
@@ -109,5 +123,12 @@ int build_transpose(Plan *P);
 void launch_conj(Plan *P, const double2 *x, double2 *y);
 int build_dir_groups(Plan *P);
 int tune_m2l(Plan *P);
+
+// batched.cu
+int build_rcr_lists(Plan *P);
+size_t rcr_tile_smem(int p, int tc, int shc);
+int launch_rcr_pass(const RcrList &Lst, int p, int pin, int pout, int atomic, const float *H, int hstride,
+                    const float2 *PH, int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst,
+                    cudaStream_t st);
 
 } // namespace fmm

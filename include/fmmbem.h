@@ -142,7 +142,8 @@ int fmm_coax_matrices_noalloc(double k, const double *t, int n, int p, int sr, c
 const char *fmm_last_error(void);
 
 /* Per-kernel timing of the last matvec on the plan's stream (milliseconds), filled when
- * profiling is enabled with fmm_set_profiling(plan, 1).  names[i] are static strings. */
+ * profiling is enabled with fmm_set_profiling(plan, 1).  names[i] are static strings; the
+ * last entry, "matvec", spans the whole matvec (kernels, memsets and the gaps between them). */
 int fmm_set_profiling(fmm_plan *plan, int on);
 int fmm_last_timings(const fmm_plan *plan, const char **names, double *ms, int *count);
 
