@@ -8,9 +8,8 @@
 // table H per direction serves both rotations and the phases are applied elementwise.
 // The FP64 path is owner-computes: each destination box is owned by one CTA that accumulates
 // all its translations in shared memory and writes once (no atomics, bit-reproducible).
-// The mixed path picks per level, by timing at plan creation, between that, a source-split
-// variant and a direction-grouped variant; the latter two add into the locals with FP32
-// atomics, so mixed results vary in the last bits from run to run.
+// The mixed path runs the batched direction-grouped tiles of batched.cu, which add into the
+// expansions with FP32 atomics, so mixed results vary in the last bits from run to run.
 #include "plan.h"
 #include <algorithm>
 #include <vector>
@@ -167,17 +166,8 @@ __global__ void to_float_kernel2(const double *in, float *out, size_t n)
         out[i] = (float)in[i];
 }
 
-enum { M2L_OWNER = 0, M2L_L2L_ONLY = 1, M2L_SPLIT = 2 };
-
-__device__ __forceinline__ void atomic_add_c(float2 *a, float2 v) { atomicAdd(a, v); }
-__device__ __forceinline__ void atomic_add_c(double2 *a, double2 v)
-{
-    atomicAdd(&a->x, v.x);
-    atomicAdd(&a->y, v.y);
-}
-
 template <typename T>
-__global__ void m2l_kernel(int mode, int p, int pmax, int pp, const int *__restrict__ sr_beg, const int *__restrict__ sr_src,
+__global__ void m2l_kernel(int p, int pmax, int pp, const int *__restrict__ sr_beg, const int *__restrict__ sr_src,
                            const short *__restrict__ sr_dir, const T *__restrict__ Hsr,
                            const typename Cx<T>::t *__restrict__ PHsr, const typename Cx<T>::t *__restrict__ Csr,
                            const typename Cx<T>::t *__restrict__ Cm, const int *__restrict__ parent,
@@ -191,141 +181,24 @@ __global__ void m2l_kernel(int mode, int p, int pmax, int pp, const int *__restr
     C *sX = (C *)smraw;
     C *sW1 = sX + E2, *sW2 = sW1 + E2, *sY = sW2 + E2;
     int b = blockIdx.x, rs = rot_size(pmax), w = 2 * pmax - 1, cs = coax_size(p);
-    // mode M2L_OWNER: L2L + every M2L source, written once.  M2L_L2L_ONLY: the L2L part
-    // (zeros at the top level), written once.  M2L_SPLIT: sources of chunk blockIdx.y,
-    // added with atomics onto what M2L_L2L_ONLY wrote.
+    // owner-computes: the L2L from the parent and every M2L source, accumulated in shared
+    // memory and written once
     for (int i = threadIdx.x; i < P2; i += blockDim.x) sY[i] = mk2((T)0, (T)0);
     __syncthreads();
-    if (pp > 0 && mode != M2L_SPLIT) {
+    if (pp > 0) {
         // L2L: parent local (order pp) translated to this box, truncated to p
         int o = octant[b];
         rcr_block<T>(pp, pmax, Hrr + (size_t)o * rs, PHrr + (size_t)o * w, Crr, Dpar + (size_t)parent[b] * pp * pp, pp,
                      sX, sW1, sW2, sY, p);
     }
-    if (mode != M2L_L2L_ONLY) {
-        int s0 = sr_beg[b], s1 = sr_beg[b + 1];
-        if (mode == M2L_SPLIT) {
-            int chunk = (s1 - s0 + gridDim.y - 1) / gridDim.y;
-            s0 = s0 + blockIdx.y * chunk;
-            s1 = min(s1, s0 + chunk);
-        }
-        for (int s = s0; s < s1; s++) {
-            int src = sr_src[s], dir = sr_dir[s];
-            rcr_block<T>(p, pmax, Hsr + (size_t)dir * rs, PHsr + (size_t)dir * w, Csr + (size_t)c_dir_dist[dir] * cs,
-                         Cm + (size_t)src * P2, p, sX, sW1, sW2, sY, p);
-        }
+    for (int s = sr_beg[b]; s < sr_beg[b + 1]; s++) {
+        int src = sr_src[s], dir = sr_dir[s];
+        rcr_block<T>(p, pmax, Hsr + (size_t)dir * rs, PHsr + (size_t)dir * w, Csr + (size_t)c_dir_dist[dir] * cs,
+                     Cm + (size_t)src * P2, p, sX, sW1, sW2, sY, p);
     }
-    if (mode == M2L_SPLIT) {
-        for (int i = threadIdx.x; i < P2; i += blockDim.x) atomic_add_c(&Dl[(size_t)b * P2 + i], sY[i]);
-    } else {
-        for (int i = threadIdx.x; i < P2; i += blockDim.x) Dl[(size_t)b * P2 + i] = sY[i];
-    }
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) Dl[(size_t)b * P2 + i] = sY[i];
 }
 
-// Direction-grouped M2L: every CTA takes one work item (direction, range of translations
-// with that offset), stages the direction's rotation coefficients, coaxial blocks and
-// phases in shared memory once, and streams the translations through its warps -- one warp
-// per translation, warp-synchronous stages, results added to the destination locals with
-// vector atomics.  The tables are read from HBM/L2 once per item instead of once per
-// translation.
-template <typename T>
-__device__ __forceinline__ void rcr_warp(int p, const T *__restrict__ sH, const typename Cx<T>::t *__restrict__ sPh,
-                                         const typename Cx<T>::t *__restrict__ sC, const typename Cx<T>::t *__restrict__ xin,
-                                         typename Cx<T>::t *sX, typename Cx<T>::t *sW1, typename Cx<T>::t *sW2,
-                                         typename Cx<T>::t *__restrict__ yout, int lane)
-{
-    typedef typename Cx<T>::t C;
-    const int pp = p * p, off = p - 1;
-    for (int i = lane; i < pp; i += 32) {
-        int n, m;
-        decode_nm(i, n, m);
-        sX[i] = cmul(xin[i], sPh[m + off]);
-    }
-    __syncwarp();
-    for (int i = lane; i < pp; i += 32) {
-        int n, mp;
-        decode_nm(i, n, mp);
-        const T *col = sH + rot_off(n) + (mp + n);
-        const int w = 2 * n + 1, base = n * n;
-        T ar = 0, ai = 0;
-        for (int m = 0; m < w; m++) {
-            T h = col[m * w];
-            C v = sX[base + m];
-            ar += h * v.x;
-            ai += h * v.y;
-        }
-        sW1[i] = mk2(ar, ai);
-    }
-    __syncwarp();
-    for (int i = lane; i < pp; i += 32) {
-        int np, m;
-        decode_nm(i, np, m);
-        int am = m < 0 ? -m : m, sz = p - am;
-        const C *col = sC + coax_off(p, am) + (np - am);
-        T ar = 0, ai = 0;
-        for (int n = am; n < p; n++) {
-            C c = col[(n - am) * sz];
-            C v = sW1[n * n + n + m];
-            ar += c.x * v.x - c.y * v.y;
-            ai += c.x * v.y + c.y * v.x;
-        }
-        sW2[i] = mk2(ar, ai);
-    }
-    __syncwarp();
-    for (int i = lane; i < pp; i += 32) {
-        int n, mp;
-        decode_nm(i, n, mp);
-        const T *col = sH + rot_off(n) + (mp + n);
-        const int w = 2 * n + 1, base = n * n;
-        T ar = 0, ai = 0;
-        for (int m = 0; m < w; m++) {
-            T h = col[m * w];
-            C v = sW2[base + m];
-            ar += h * v.x;
-            ai += h * v.y;
-        }
-        C e = sPh[mp + off];
-        atomic_add_c(&yout[i], mk2(e.x * ar + e.y * ai, e.x * ai - e.y * ar));
-    }
-    __syncwarp();
-}
-
-template <typename T>
-__global__ void m2l_dir_kernel(int p, int pmax, const int4 *__restrict__ items, const int *__restrict__ g_src,
-                               const int *__restrict__ g_dst, const T *__restrict__ Hsr,
-                               const typename Cx<T>::t *__restrict__ PHsr, const typename Cx<T>::t *__restrict__ Csr,
-                               const typename Cx<T>::t *__restrict__ Cm, typename Cx<T>::t *__restrict__ Dl)
-{
-    typedef typename Cx<T>::t C;
-    extern __shared__ unsigned char smraw[];
-    const int4 it = items[blockIdx.x];
-    const int dir = it.x, rs = rot_size(p), cs = coax_size(p), w = 2 * p - 1, P2 = p * p;
-    // layout: coax (C), phases (C), per-warp X/W1/W2 (C), then H (T)
-    C *sC = (C *)smraw;
-    C *sPh = sC + cs;
-    C *sWarp = sPh + w;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    T *sH = (T *)(sWarp + (size_t)nw * 3 * P2);
-    const T *Hg = Hsr + (size_t)dir * rot_size(pmax);
-    const C *Cg = Csr + (size_t)c_dir_dist[dir] * cs;
-    const C *Pg = PHsr + (size_t)dir * (2 * pmax - 1) + (pmax - p);
-    for (int i = threadIdx.x; i < rs; i += blockDim.x) sH[i] = Hg[i];
-    for (int i = threadIdx.x; i < cs; i += blockDim.x) sC[i] = Cg[i];
-    for (int i = threadIdx.x; i < w; i += blockDim.x) sPh[i] = Pg[i];
-    __syncthreads();
-    C *sX = sWarp + (size_t)warp * 3 * P2, *sW1 = sX + P2, *sW2 = sW1 + P2;
-    for (int t = it.y + warp; t < it.y + it.z; t += nw) {
-        int src = g_src[t], dst = g_dst[t];
-        rcr_warp<T>(p, sH, sPh, sC, Cm + (size_t)src * P2, sX, sW1, sW2, Dl + (size_t)dst * P2, lane);
-    }
-}
-
-template <typename T>
-size_t m2l_dir_smem(int p, int nwarps)
-{
-    typedef typename Cx<T>::t C;
-    return sizeof(C) * ((size_t)coax_size(p) + (2 * p - 1) + (size_t)nwarps * 3 * p * p) + sizeof(T) * (size_t)rot_size(p);
-}
 
 template <typename T>
 __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_leaf, const typename Cx<T>::t *__restrict__ Dl,
@@ -385,8 +258,8 @@ static void timer_end(Plan *P)
     P->ntimers++;
 }
 
-// Raise the dynamic shared-memory limit of the translation kernels to what order pmax needs
-// (4 p^2 complex for the CTA-level RCR, up to 220 KiB for the direction-grouped kernel).
+// Raise the dynamic shared-memory limit of the owner-computes translation kernels to what
+// order pmax needs (4 p^2 complex for the CTA-level RCR).
 template <typename T>
 static int set_smem_attrs(int pmax)
 {
@@ -397,13 +270,12 @@ static int set_smem_attrs(int pmax)
     if (done[slot] >= smax) return FMM_OK;
     FMM_CUDA_TRY(cudaFuncSetAttribute(m2m_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
     FMM_CUDA_TRY(cudaFuncSetAttribute(m2l_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
-    FMM_CUDA_TRY(cudaFuncSetAttribute(m2l_dir_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     done[slot] = smax;
     return FMM_OK;
 }
 
 template <typename T>
-static int launch_m2l_level(Plan *P, int l, int sched, int split, const char *tname)
+static int launch_m2l_level(Plan *P, int l, const char *tname)
 {
     typedef typename Cx<T>::t C;
     const bool f64 = sizeof(T) == 8;
@@ -423,19 +295,8 @@ static int launch_m2l_level(Plan *P, int l, int sched, int split, const char *tn
     int pe = pp > L.p ? pp : L.p;
     size_t sm = 4 * (size_t)pe * pe * sizeof(C);
     timer_begin(P, tname);
-    int first_mode = (sched == M2L_SCHED_OWNER) ? M2L_OWNER : M2L_L2L_ONLY;
-    m2l_kernel<T><<<L.nb, block_for(pe), sm, st>>>(first_mode, L.p, pmax, pp, L.sr_beg, L.sr_src, L.sr_dir, Hsr, PHsr,
-                                                     Csr, Cm, L.parent, L.octant, Hrr, PHrr, Crr, Dpar, Dl);
-    if (sched == M2L_SCHED_SPLIT) {
-        size_t sm2 = 4 * (size_t)L.p * L.p * sizeof(C);
-        m2l_kernel<T><<<dim3(L.nb, split), block_for(L.p), sm2, st>>>(M2L_SPLIT, L.p, pmax, 0, L.sr_beg, L.sr_src,
-                                                                      L.sr_dir, Hsr, PHsr, Csr, Cm, L.parent, L.octant,
-                                                                      Hrr, PHrr, Crr, Dpar, Dl);
-    } else if (sched == M2L_SCHED_DIR) {
-        size_t sm3 = m2l_dir_smem<T>(L.p, L.dir_warps);
-        m2l_dir_kernel<T><<<L.n_items, 32 * L.dir_warps, sm3, st>>>(L.p, pmax, L.dir_items, L.g_src, L.g_dst, Hsr,
-                                                                    PHsr, Csr, Cm, Dl);
-    }
+    m2l_kernel<T><<<L.nb, block_for(pe), sm, st>>>(L.p, pmax, pp, L.sr_beg, L.sr_src, L.sr_dir, Hsr, PHsr, Csr, Cm,
+                                                     L.parent, L.octant, Hrr, PHrr, Crr, Dpar, Dl);
     timer_end(P);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
@@ -525,7 +386,7 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
         timer_end(P);
     }
     for (int l = lmin; l <= lmax && f64; l++) {
-        int st = launch_m2l_level<T>(P, l, M2L_SCHED_OWNER, 1, m2l_names[l]);
+        int st = launch_m2l_level<T>(P, l, m2l_names[l]);
         if (st) return st;
     }
     timer_begin(P, "l2p_near");
@@ -622,99 +483,5 @@ int build_transpose(Plan *P)
     return FMM_OK;
 }
 
-
-// Translations of each level sorted by direction, cut into work items of at most `chunk`
-// translations (one CTA each).
-int build_dir_groups(Plan *P)
-{
-    for (int l = P->lmin; l <= P->lmax; l++) {
-        LevelDev &L = P->lev[l];
-        long long T = L.num_sr;
-        if (T == 0) continue;
-        std::vector<int> beg(L.nb + 1), src(T);
-        std::vector<short> dir(T);
-        FMM_CUDA_TRY(cudaMemcpy(beg.data(), L.sr_beg, sizeof(int) * (L.nb + 1), cudaMemcpyDeviceToHost));
-        FMM_CUDA_TRY(cudaMemcpy(src.data(), L.sr_src, sizeof(int) * T, cudaMemcpyDeviceToHost));
-        FMM_CUDA_TRY(cudaMemcpy(dir.data(), L.sr_dir, sizeof(short) * T, cudaMemcpyDeviceToHost));
-        std::vector<int> cnt(NDIR + 1, 0);
-        for (long long t = 0; t < T; t++) cnt[dir[t] + 1]++;
-        for (int d = 0; d < NDIR; d++) cnt[d + 1] += cnt[d];
-        std::vector<int> gs(T), gd(T), fill(NDIR, 0);
-        for (int b = 0; b < L.nb; b++)
-            for (int t = beg[b]; t < beg[b + 1]; t++) {
-                int d = dir[t], pos = cnt[d] + fill[d]++;
-                gs[pos] = src[t];
-                gd[pos] = b;
-            }
-        const int chunk = 128;
-        std::vector<int4> items;
-        for (int d = 0; d < NDIR; d++)
-            for (int a = cnt[d]; a < cnt[d + 1]; a += chunk) items.push_back(make_int4(d, a, std::min(chunk, cnt[d + 1] - a), 0));
-        L.n_items = (int)items.size();
-        L.dir_warps = L.p <= 14 ? 8 : 4;
-        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.dir_items, sizeof(int4) * items.size()));
-        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.g_src, sizeof(int) * T));
-        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.g_dst, sizeof(int) * T));
-        FMM_CUDA_TRY(cudaMemcpy(L.dir_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
-        FMM_CUDA_TRY(cudaMemcpy(L.g_src, gs.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
-        FMM_CUDA_TRY(cudaMemcpy(L.g_dst, gd.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
-    }
-    return FMM_OK;
-}
-
-// Per-level schedule of the mixed-precision M2L picked by timing the candidates on this
-// plan's own tables: owner-computes, source-split with atomics (2..16 chunks), and the
-// direction-grouped kernel where its shared-memory footprint fits (p <= 20).
-int tune_m2l(Plan *P)
-{
-    if (!P->U32) return FMM_OK;
-    {
-        int st = set_smem_attrs<float>(P->pmax);
-        if (st) return st;
-    }
-    cudaEvent_t a, b;
-    FMM_CUDA_TRY(cudaEventCreate(&a));
-    FMM_CUDA_TRY(cudaEventCreate(&b));
-    int saved = P->profiling;
-    P->profiling = 0;
-    // representative inputs: unit coefficients (the timing does not depend on the values)
-    for (int l = P->lmin; l <= P->lmax; l++) {
-        LevelDev &L = P->lev[l];
-        std::vector<float2> ones((size_t)L.nb * L.p * L.p, make_float2(1e-3f, 0.f));
-        FMM_CUDA_TRY(cudaMemcpy(L.Cm32, ones.data(), sizeof(float2) * ones.size(), cudaMemcpyHostToDevice));
-        FMM_CUDA_TRY(cudaMemcpy(L.Dl32, ones.data(), sizeof(float2) * ones.size(), cudaMemcpyHostToDevice));
-    }
-    for (int l = P->lmin; l <= P->lmax; l++) {
-        LevelDev &L = P->lev[l];
-        struct Cand { int sched, split; };
-        std::vector<Cand> cands = {{M2L_SCHED_OWNER, 1}};
-        for (int s = 2; s <= 16; s *= 2)
-            if ((long long)L.nb * s <= 152LL * 64 && L.num_sr / std::max(1, L.nb) >= 2 * s) cands.push_back({M2L_SCHED_SPLIT, s});
-        if (L.p <= 20 && L.n_items > 0 && m2l_dir_smem<float>(L.p, L.dir_warps) <= 220 * 1024) cands.push_back({M2L_SCHED_DIR, 1});
-        float best = 1e30f;
-        for (auto &c : cands) {
-            float tsum = 0.f;
-            for (int rep = 0; rep < 3; rep++) {
-                FMM_CUDA_TRY(cudaEventRecord(a, P->stream));
-                int st = launch_m2l_level<float>(P, l, c.sched, c.split, "tune");
-                if (st) return st;
-                FMM_CUDA_TRY(cudaEventRecord(b, P->stream));
-                FMM_CUDA_TRY(cudaEventSynchronize(b));
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, a, b);
-                if (rep > 0) tsum += ms;
-            }
-            if (tsum < best) {
-                best = tsum;
-                L.sched32 = c.sched;
-                L.split32 = c.split;
-            }
-        }
-    }
-    P->profiling = saved;
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    return FMM_OK;
-}
 
 } // namespace fmm

@@ -67,7 +67,6 @@ static void free_plan(Plan *P)
         LevelDev &L = P->lev[l];
         F(L.parent); F(L.octant); F(L.child_beg); F(L.child_list); F(L.sr_beg); F(L.sr_src); F(L.sr_dir);
         F(L.Cm64); F(L.Dl64); F(L.Cm32); F(L.Dl32); F(L.Csr64); F(L.Csr32); F(L.Crr64); F(L.Crr32);
-        F(L.dir_items); F(L.g_src); F(L.g_dst);
         for (RcrList *R : {&L.m2l, &L.m2m, &L.l2l}) { F(R->items); F(R->src); F(R->dst); }
     }
     F(P->Hsr64); F(P->PHsr64); F(P->Hsr32); F(P->PHsr32);
@@ -161,7 +160,6 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
     TRY(gen_near_field(P));
     if (P->opt.build_mixed) {
         TRY(build_rcr_lists(P));
-        for (int l = P->lmin; l <= P->lmax; l++) P->lev[l].sched32 = M2L_SCHED_BATCHED;
     }
     CTRY(dev_alloc(P, (void **)&P->xbuf, sizeof(double2) * nf));
     CTRY(dev_alloc(P, (void **)&P->ybuf, sizeof(double2) * nf));
@@ -218,8 +216,7 @@ extern "C" int fmm_plan_info(const fmm_plan *plan, fmm_info *info)
         info->p_level[l] = P->lev[l].p;
         info->num_box[l] = P->lev[l].nb;
         info->num_m2l[l] = P->lev[l].num_sr;
-        info->m2l_schedule[l] = P->lev[l].sched32;
-        info->m2l_split[l] = P->lev[l].split32;
+        info->m2l_columns[l] = P->opt.build_mixed ? P->lev[l].m2l.tc : 0;
     }
     info->num_near = P->num_near;
     info->device_bytes = P->device_bytes;

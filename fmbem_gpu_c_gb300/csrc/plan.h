@@ -35,19 +35,10 @@ struct LevelDev {
     float2 *Csr32 = nullptr;
     double2 *Crr64 = nullptr;     // coaxial (R|R) at order p_{l-1} for M2M into / L2L out of level l-1
     float2 *Crr32 = nullptr;
-    // mixed-precision M2L schedule chosen by the autotuner (tune_m2l)
-    int sched32 = 0;              // M2L_SCHED_OWNER, _SPLIT or _DIR
-    int split32 = 1;              // source chunks per destination for _SPLIT
-    int dir_warps = 8;            // warps per CTA for _DIR
-    int n_items = 0;              // direction-grouped work items
-    int4 *dir_items = nullptr;    // (direction, first, count, 0)
-    int *g_src = nullptr, *g_dst = nullptr; // translations sorted by direction
     // batched passes of the mixed path: M2L of this level, M2M (this level -> parents),
     // L2L (parents -> this level)
     RcrList m2l, m2m, l2l;
 };
-
-enum { M2L_SCHED_OWNER = 0, M2L_SCHED_SPLIT = 1, M2L_SCHED_DIR = 2, M2L_SCHED_BATCHED = 3 };
 
 struct Timer {
     const char *name;
@@ -121,8 +112,6 @@ int build_lists(Plan *P);
 int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpose = 0);
 int build_transpose(Plan *P);
 void launch_conj(Plan *P, const double2 *x, double2 *y);
-int build_dir_groups(Plan *P);
-int tune_m2l(Plan *P);
 
 // batched.cu
 int build_rcr_lists(Plan *P);

@@ -65,8 +65,7 @@ typedef struct {
     long long num_near;
     size_t device_bytes;
     double setup_seconds;
-    int m2l_schedule[FMM_MAX_LEVEL + 1]; /* mixed-path M2L per level: 0 owner, 1 split, 2 direction-grouped */
-    int m2l_split[FMM_MAX_LEVEL + 1];    /* source chunks per box for schedule 1 */
+    int m2l_columns[FMM_MAX_LEVEL + 1];  /* mixed path: M2L translations per CTA tile (0 without mixed tables) */
 } fmm_info;
 
 typedef struct fmm_plan fmm_plan;
