@@ -295,6 +295,26 @@ def gpu_arm(args, world, rank, local):
     rel_err = float((torch.linalg.norm(y - y64) / torch.linalg.norm(y64)).item())
     fp64_rate = 1.0 / float(np.median(t64))
 
+    # batching path: NB columns in one mixed pass (device buffers), columns per second
+    NB = 16
+    xb = torch.from_numpy(np.concatenate([np.roll(xh, 7 * r) for r in range(NB)])).to("cuda")
+    yb = torch.empty_like(xb)
+    plan.matvec(xb, fm.FMM_MIXED, out=yb)
+    torch.cuda.synchronize()
+    plan.set_profiling(True)
+    tb = []
+    for _ in range(3):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        plan.matvec(xb, fm.FMM_MIXED, out=yb)
+        tb.append(dict(plan.timings())["matvec"])
+    plan.set_profiling(False)
+    y0 = yb[:nf]
+    batched_err = float((torch.linalg.norm(y0 - y) / torch.linalg.norm(y)).item())
+    batched = {"nrhs": NB, "value": NB / (float(np.mean(tb)) / 1e3), "unit": "matvec/s (columns)",
+               "ms_per_batch": float(np.mean(tb)), "column0_vs_single_rel_err": batched_err}
+    del xb, yb
+
     # end to end through the C ABI with host buffers
     yh = np.empty_like(xh)
     plan.matvec(xh, fm.FMM_MIXED, out=yh)
@@ -352,6 +372,7 @@ def gpu_arm(args, world, rank, local):
                      "traffic": ncu_traffic(), "algorithmic_flops_per_matvec": rcr_flops,
                      "ms_per_matvec": rcr_ms},
         "kernels_ms": {n: float(np.mean(v)) for n, v in kernel_ms.items()},
+        "batched": batched,
         "fp64_plain": {"value": fp64_rate, "unit": UNIT, "mixed_speedup": value / world / fp64_rate,
                        "mixed_vs_fp64_rel_err": rel_err},
         "solve": solve,

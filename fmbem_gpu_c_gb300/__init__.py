@@ -68,6 +68,8 @@ def lib():
         L.fmm_matvec_adjoint.argtypes = [c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.fmm_gmres.argtypes = [c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                 c_ip, c_dp]
+        L.fmm_solve_batched.argtypes = [c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, c_ip, c_dp]
         L.fmm_far_field.argtypes = [c_vp, c_vp, c_dp, ctypes.c_int, c_vp]
         L.fmm_plane_wave_rhs.argtypes = [c_vp, c_dp, c_vp]
         L.fmm_mesh_icosphere.argtypes = [ctypes.c_int, ctypes.c_double, c_dp, c_ip, c_ip, c_ip]
@@ -172,6 +174,19 @@ class Plan:
         if st not in (0, 6):
             _check(st)
         return x, it.value, rr.value, st == 0
+
+    def solve_batched(self, B, X0=None, tol=1e-6, maxit=500, restart=50, precision=FMM_FP64):
+        """Solve A X = B for the rows of B (nrhs x nf) at once; returns (X, iters, relres, ok)."""
+        B = np.ascontiguousarray(B, dtype=np.complex128)
+        nrhs = B.shape[0]
+        X = np.zeros_like(B) if X0 is None else np.ascontiguousarray(X0, dtype=np.complex128).copy()
+        it = np.zeros(nrhs, dtype=np.int32)
+        rr = np.zeros(nrhs, dtype=np.float64)
+        st = lib().fmm_solve_batched(self.h, _ptr(B), _ptr(X), nrhs, tol, maxit, restart, precision,
+                                     it.ctypes.data_as(c_ip), rr.ctypes.data_as(c_dp))
+        if st not in (0, 6):
+            _check(st)
+        return X, it, rr, st == 0
 
     def far_field(self, p, pts):
         p = np.ascontiguousarray(p, dtype=np.complex128)

@@ -27,13 +27,14 @@ namespace fmm {
 
 struct RcrPass {
     int p, pin, pout, atomic;        // RCR order, source order, destination order
+    int nrhs, nsrc, ndst;            // right-hand sides; boxes per right-hand side in src and dst
     int hstride, phstride, phoff;    // per-direction strides of H and the phases; phase index m + phoff
     const float *H;
     const float2 *PH;
     const float2 *Cc;                // coaxial blocks, item.w selects one (stride coax_size(p))
     const float2 *src;               // [boxes][pin^2]
     float2 *dst;                     // [boxes][pout^2]
-    const int4 *items;               // (direction, first, count, coaxial block)
+    const int4 *items;               // (direction, first, count, coaxial block) over columns e = t nrhs + r
     const int *g_src, *g_dst;
 };
 
@@ -119,9 +120,12 @@ __global__ void __launch_bounds__(256, 2) rcr_tile_kernel(RcrPass ps)
     const float *H = SHC ? sH : Hg;
     const float2 *Cc = SHC ? sC : Cg;
     if (threadIdx.x < TC) {
+        // column e = translation t x nrhs + right-hand side r; each right-hand side has its own
+        // copy of the source and destination levels
         bool v = (int)threadIdx.x < cnt;
-        s_src[threadIdx.x] = v ? ps.g_src[it.y + threadIdx.x] : -1;
-        s_dst[threadIdx.x] = v ? ps.g_dst[it.y + threadIdx.x] : -1;
+        int e = it.y + threadIdx.x, t = e / ps.nrhs, r = e - t * ps.nrhs;
+        s_src[threadIdx.x] = v ? ps.g_src[t] + r * ps.nsrc : -1;
+        s_dst[threadIdx.x] = v ? ps.g_dst[t] + r * ps.ndst : -1;
     }
     if (SHC) {
         const int rs = rot_size(p), cs = coax_size(p);
@@ -285,16 +289,48 @@ static int launch_tile(const RcrPass &ps, int n_items, size_t sm, cudaStream_t s
     return FMM_OK;
 }
 
-int launch_rcr_pass(const RcrList &Lst, int p, int pin, int pout, int atomic, const float *H, int hstride,
-                    const float2 *PH, int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst,
-                    cudaStream_t st)
+// Items of a pass for nrhs right-hand sides: each direction's translations x right-hand
+// sides, cut into groups of at most tc columns.  Rebuilt when nrhs changes.
+static int ensure_items(RcrList &Lst, int nrhs)
 {
-    if (Lst.n_items == 0) return FMM_OK;
+    if (Lst.items_nrhs == nrhs) return FMM_OK;
+    std::vector<int4> items;
+    int nkeys = (int)Lst.key_beg.size() - 1;
+    for (int d = 0; d < nkeys; d++) {
+        long long e0 = (long long)Lst.key_beg[d] * nrhs, e1 = (long long)Lst.key_beg[d + 1] * nrhs;
+        for (long long a = e0; a < e1; a += Lst.tc)
+            items.push_back(make_int4(d, (int)a, (int)std::min<long long>(Lst.tc, e1 - a), Lst.key_w[d]));
+    }
+    if (items.size() > Lst.items_cap) {
+        if (Lst.items) cudaFree(Lst.items);
+        Lst.items = nullptr;
+        FMM_CUDA_TRY(cudaMalloc(&Lst.items, sizeof(int4) * items.size()));
+        Lst.items_cap = items.size();
+    }
+    if (!items.empty())
+        FMM_CUDA_TRY(cudaMemcpy(Lst.items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+    Lst.n_items = (int)items.size();
+    Lst.items_nrhs = nrhs;
+    return FMM_OK;
+}
+
+int launch_rcr_pass(RcrList &Lst, int p, int pin, int pout, int atomic, const float *H, int hstride,
+                    const float2 *PH, int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst,
+                    int nrhs, int nsrc, int ndst, cudaStream_t st)
+{
+    if (Lst.key_beg.empty() || Lst.key_beg.back() == 0) return FMM_OK;
+    {
+        int e = ensure_items(Lst, nrhs);
+        if (e) return e;
+    }
     RcrPass ps;
     ps.p = p;
     ps.pin = pin;
     ps.pout = pout;
     ps.atomic = atomic;
+    ps.nrhs = nrhs;
+    ps.nsrc = nsrc;
+    ps.ndst = ndst;
     ps.hstride = hstride;
     ps.phstride = phstride;
     ps.phoff = phoff;
@@ -355,17 +391,16 @@ static int upload_list(Plan *P, RcrList &Lst, const std::vector<int> &key, const
         gs[pos] = src[i];
         gd[pos] = dst[i];
     }
-    std::vector<int4> items;
-    for (int d = 0; d < nkeys; d++)
-        for (int a = cnt[d]; a < cnt[d + 1]; a += tc) items.push_back(make_int4(d, a, std::min(tc, cnt[d + 1] - a), key_w[d]));
-    Lst.n_items = (int)items.size();
+    Lst.key_beg.assign(cnt.begin(), cnt.end());
+    Lst.key_w = key_w;
     Lst.tc = tc;
     Lst.shc = shc;
-    if (items.empty()) return FMM_OK;
-    FMM_CUDA_TRY(dev_alloc(P, (void **)&Lst.items, sizeof(int4) * items.size()));
+    Lst.items_nrhs = 0;
+    if (T == 0) return FMM_OK;
+    int e = ensure_items(Lst, 1);
+    if (e) return e;
     FMM_CUDA_TRY(dev_alloc(P, (void **)&Lst.src, sizeof(int) * T));
     FMM_CUDA_TRY(dev_alloc(P, (void **)&Lst.dst, sizeof(int) * T));
-    FMM_CUDA_TRY(cudaMemcpy(Lst.items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
     FMM_CUDA_TRY(cudaMemcpy(Lst.src, gs.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
     FMM_CUDA_TRY(cudaMemcpy(Lst.dst, gd.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
     return FMM_OK;

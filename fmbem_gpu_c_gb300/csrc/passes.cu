@@ -113,10 +113,12 @@ __device__ void rcr_block(int p, int pmax, const T *__restrict__ H, const typena
 template <typename T>
 __global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *__restrict__ leaf_elem,
                            const typename Cx<T>::t *__restrict__ U, const double2 *__restrict__ x, double k,
-                           typename Cx<T>::t *__restrict__ Cm, int flip)
+                           typename Cx<T>::t *__restrict__ Cm, int flip, int nf, int nb)
 {
     typedef typename Cx<T>::t C;
     int b = blockIdx.x, ppl = pl * pl;
+    x += (size_t)blockIdx.y * nf; // right-hand side blockIdx.y
+    Cm += (size_t)blockIdx.y * nb * ppl;
     int s0 = leaf_beg[b], s1 = leaf_beg[b + 1];
     for (int i = threadIdx.x; i < ppl; i += blockDim.x) {
         int q = i;
@@ -204,13 +206,16 @@ template <typename T>
 __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_leaf, const typename Cx<T>::t *__restrict__ Dl,
                                 const typename Cx<T>::t *__restrict__ Rv, const int *__restrict__ near_beg,
                                 const int *__restrict__ near_col, const typename Cx<T>::t *__restrict__ nearv,
-                                const double2 *__restrict__ x, double2 a, double2 *__restrict__ y, int flip)
+                                const double2 *__restrict__ x, double2 a, double2 *__restrict__ y, int flip, int nb)
 {
     typedef typename Cx<T>::t C;
     int lane = threadIdx.x & 31;
     int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (e >= nf) return;
     int ppl = pl * pl;
+    x += (size_t)blockIdx.y * nf; // right-hand side blockIdx.y
+    y += (size_t)blockIdx.y * nf;
+    Dl += (size_t)blockIdx.y * nb * ppl;
     T ar = 0, ai = 0;
     for (int s = near_beg[e] + lane; s < near_beg[e + 1]; s += 32) {
         C v = nearv[s];
@@ -303,7 +308,7 @@ static int launch_m2l_level(Plan *P, int l, const char *tname)
 }
 
 template <typename T>
-static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
+static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, int nrhs)
 {
     typedef typename Cx<T>::t C;
     const bool f64 = sizeof(T) == 8;
@@ -338,8 +343,8 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
     timer_begin(P, "p2m");
     // the transposed operator swaps the roles of the element moments and the centroid basis
     // (index-flipped), keeps every translation, and uses the transposed near-field matrix
-    p2m_kernel<T><<<LL.nb, 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, transpose ? Rv : U, x, P->opt.k, Cm(lmax),
-                                         transpose);
+    p2m_kernel<T><<<dim3(LL.nb, nrhs), 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, transpose ? Rv : U, x, P->opt.k,
+                                                     Cm(lmax), transpose, P->nf, LL.nb);
     timer_end(P);
     if (!f64) {
         // mixed path: batched direction-grouped passes (batched.cu).  M2M and M2L add into
@@ -348,7 +353,7 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
         static const char *l2l_names[] = {"l2l_l0", "l2l_l1", "l2l_l2", "l2l_l3", "l2l_l4", "l2l_l5", "l2l_l6",
                                           "l2l_l7", "l2l_l8", "l2l_l9", "l2l_l10", "l2l_l11", "l2l_l12", "l2l_l13"};
         for (int l = lmin; l <= lmax; l++) {
-            size_t n = (size_t)P->lev[l].nb * P->lev[l].p * P->lev[l].p * sizeof(C);
+            size_t n = (size_t)P->lev[l].nb * P->lev[l].p * P->lev[l].p * sizeof(C) * nrhs;
             if (l < lmax) FMM_CUDA_TRY(cudaMemsetAsync(Cm(l), 0, n, st));
             FMM_CUDA_TRY(cudaMemsetAsync(Dl(l), 0, n, st));
         }
@@ -356,7 +361,8 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
             LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
             timer_begin(P, m2m_names[l]);
             int e = launch_rcr_pass(L.m2m, PL.p, L.p, PL.p, 1, (const float *)Hss, rs, (const float2 *)PHss, w, pmax - 1,
-                                    (const float2 *)Crr(l), (const float2 *)Cm(l), (float2 *)Cm(l - 1), st);
+                                    (const float2 *)Crr(l), (const float2 *)Cm(l), (float2 *)Cm(l - 1), nrhs, L.nb,
+                                    PL.nb, st);
             if (e) return e;
             timer_end(P);
         }
@@ -364,7 +370,7 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
             LevelDev &L = P->lev[l];
             timer_begin(P, m2l_names[l]);
             int e = launch_rcr_pass(L.m2l, L.p, L.p, L.p, 1, (const float *)Hsr, rs, (const float2 *)PHsr, w, pmax - 1,
-                                    (const float2 *)Csr(l), (const float2 *)Cm(l), (float2 *)Dl(l), st);
+                                    (const float2 *)Csr(l), (const float2 *)Cm(l), (float2 *)Dl(l), nrhs, L.nb, L.nb, st);
             if (e) return e;
             timer_end(P);
         }
@@ -372,7 +378,8 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
             LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
             timer_begin(P, l2l_names[l]);
             int e = launch_rcr_pass(L.l2l, PL.p, PL.p, L.p, 0, (const float *)Hrr, rs, (const float2 *)PHrr, w, pmax - 1,
-                                    (const float2 *)Crr(l), (const float2 *)Dl(l - 1), (float2 *)Dl(l), st);
+                                    (const float2 *)Crr(l), (const float2 *)Dl(l - 1), (float2 *)Dl(l), nrhs, PL.nb,
+                                    L.nb, st);
             if (e) return e;
             timer_end(P);
         }
@@ -392,9 +399,9 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose)
     timer_begin(P, "l2p_near");
     double2 a = make_double2(P->opt.a_re, P->opt.a_im);
     const C *nearT = f64 ? (const C *)P->nearT64 : (const C *)P->nearT32;
-    l2p_near_kernel<T><<<(P->nf * 32 + 255) / 256, 256, 0, st>>>(
+    l2p_near_kernel<T><<<dim3((P->nf * 32 + 255) / 256, nrhs), 256, 0, st>>>(
         P->nf, LL.p, P->elem_leaf, Dl(lmax), transpose ? U : Rv, transpose ? P->nearT_beg : P->near_beg,
-        transpose ? P->nearT_col : P->near_col, transpose ? nearT : nearv, x, a, y, transpose);
+        transpose ? P->nearT_col : P->near_col, transpose ? nearT : nearv, x, a, y, transpose, LL.nb);
     timer_end(P);
     if (P->profiling) {
         cudaEventRecord(P->total.end, st);
@@ -410,7 +417,26 @@ int set_dir_dist(const int *dd)
     return FMM_OK;
 }
 
-int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpose)
+// The FP32 expansions hold rhs_cap32 right-hand sides, level by level ([rhs][box][p^2]).
+static int ensure_rhs32(Plan *P, int nrhs)
+{
+    if (nrhs <= P->rhs_cap32) return FMM_OK;
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        LevelDev &L = P->lev[l];
+        size_t n = (size_t)L.nb * L.p * L.p;
+        cudaFree(L.Cm32);
+        cudaFree(L.Dl32);
+        L.Cm32 = nullptr;
+        L.Dl32 = nullptr;
+        P->device_bytes -= 2 * sizeof(float2) * n * P->rhs_cap32;
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Cm32, sizeof(float2) * n * nrhs));
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Dl32, sizeof(float2) * n * nrhs));
+    }
+    P->rhs_cap32 = nrhs;
+    return FMM_OK;
+}
+
+int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpose, int nrhs)
 {
     if (transpose && !P->nearT_beg) {
         fmm_set_error("transposed near field not built");
@@ -421,9 +447,15 @@ int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpo
             fmm_set_error("%s", P->mixed_note);
             return FMM_ERR_ARG;
         }
-        return run_matvec_t<float>(P, x, y, transpose);
+        int st = ensure_rhs32(P, nrhs);
+        if (st) return st;
+        return run_matvec_t<float>(P, x, y, transpose, nrhs);
     }
-    return run_matvec_t<double>(P, x, y, transpose);
+    for (int r = 0; r < nrhs; r++) {
+        int st = run_matvec_t<double>(P, x + (size_t)r * P->nf, y + (size_t)r * P->nf, transpose, 1);
+        if (st) return st;
+    }
+    return FMM_OK;
 }
 
 __global__ void gather_kernel(const double2 *src, const long long *perm, long long n, double2 *dst)
@@ -432,14 +464,15 @@ __global__ void gather_kernel(const double2 *src, const long long *perm, long lo
         dst[i] = src[perm[i]];
 }
 
-__global__ void conj_kernel(const double2 *x, double2 *y, int n)
+__global__ void conj_kernel(const double2 *x, double2 *y, size_t n)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = make_double2(x[i].x, -x[i].y);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        y[i] = make_double2(x[i].x, -x[i].y);
 }
 
-void launch_conj(Plan *P, const double2 *x, double2 *y)
+void launch_conj(Plan *P, const double2 *x, double2 *y, size_t n)
 {
-    conj_kernel<<<(P->nf + 255) / 256, 256, 0, P->stream>>>(x, y, P->nf);
+    conj_kernel<<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 8), 256, 0, P->stream>>>(x, y, n);
 }
 
 // Near-field matrix transposed (CSR by source element), built on first use of the

@@ -74,7 +74,7 @@ static void free_plan(Plan *P)
     F(P->U64); F(P->Rv64); F(P->U32); F(P->Rv32); F(P->near_beg); F(P->near_col); F(P->near64); F(P->near32);
     F(P->nearT_beg); F(P->nearT_col); F(P->nearT64); F(P->nearT32);
     F(P->xbuf); F(P->ybuf);
-    F(P->gm_V); F(P->gm_w); F(P->gm_r); F(P->gm_x); F(P->gm_b); F(P->gm_d); F(P->gm_dev_h);
+    F(P->gm_V); F(P->gm_w); F(P->gm_r); F(P->gm_x); F(P->gm_b); F(P->gm_d); F(P->gm_dev_h); F(P->gm_alpha);
     if (P->timers_created)
         for (int i = 0; i < MAX_TIMERS; i++) { cudaEventDestroy(P->timers[i].beg); cudaEventDestroy(P->timers[i].end); }
     if (P->timers_created) { cudaEventDestroy(P->total.beg); cudaEventDestroy(P->total.end); }
@@ -231,28 +231,58 @@ static bool is_device_ptr(const void *p)
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-extern "C" int fmm_matvec(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComplex *y, int nrhs, int precision)
+// Staging buffers for host inputs and outputs, ncols columns of nf.
+static int ensure_io(Plan *P, int ncols)
 {
-    Plan *P = (Plan *)plan;
+    if (ncols <= P->nrhs_cap) return FMM_OK;
+    cudaFree(P->xbuf);
+    cudaFree(P->ybuf);
+    P->xbuf = P->ybuf = nullptr;
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->xbuf, sizeof(double2) * (size_t)P->nf * ncols));
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->ybuf, sizeof(double2) * (size_t)P->nf * ncols));
+    P->nrhs_cap = ncols;
+    return FMM_OK;
+}
+
+// y = A x, A^T x or A^H x for nrhs columns; host or device buffers.  The mixed path applies
+// the operator to all columns in one batched pass.
+static int apply_operator(Plan *P, const cuDoubleComplex *x, cuDoubleComplex *y, int nrhs, int precision, int transpose,
+                          int conjugate)
+{
     if (!P || !x || !y || nrhs < 1) { fmm_set_error("invalid argument"); return FMM_ERR_ARG; }
     if (precision != FMM_FP64 && precision != FMM_MIXED) { fmm_set_error("unknown precision %d", precision); return FMM_ERR_ARG; }
-    bool xd = is_device_ptr(x), yd = is_device_ptr(y);
-    for (int r = 0; r < nrhs; r++) {
-        const double2 *xs = (const double2 *)x + (size_t)r * P->nf;
-        double2 *ys = (double2 *)y + (size_t)r * P->nf;
-        const double2 *xin = xs;
-        double2 *yout = ys;
-        if (!xd) {
-            FMM_CUDA_TRY(cudaMemcpyAsync(P->xbuf, xs, sizeof(double2) * P->nf, cudaMemcpyHostToDevice, P->stream));
-            xin = P->xbuf;
-        }
-        if (!yd) yout = P->ybuf;
-        int st = run_matvec(P, xin, yout, precision);
+    if (transpose) {
+        int st = build_transpose(P);
         if (st) return st;
-        if (!yd) FMM_CUDA_TRY(cudaMemcpyAsync(ys, P->ybuf, sizeof(double2) * P->nf, cudaMemcpyDeviceToHost, P->stream));
     }
+    bool xd = is_device_ptr(x), yd = is_device_ptr(y);
+    size_t n = (size_t)P->nf * nrhs;
+    if (!xd || !yd || conjugate) {
+        int st = ensure_io(P, nrhs);
+        if (st) return st;
+    }
+    const double2 *xin = (const double2 *)x;
+    double2 *yout = yd ? (double2 *)y : P->ybuf;
+    if (!xd) {
+        FMM_CUDA_TRY(cudaMemcpyAsync(P->xbuf, x, sizeof(double2) * n, cudaMemcpyHostToDevice, P->stream));
+        xin = P->xbuf;
+    }
+    if (conjugate) {
+        launch_conj(P, xin, P->xbuf, n);
+        xin = P->xbuf;
+    }
+    int st = run_matvec(P, xin, yout, precision, transpose, nrhs);
+    if (st) return st;
+    if (conjugate) launch_conj(P, yout, yout, n);
+    FMM_CUDA_TRY(cudaGetLastError());
+    if (!yd) FMM_CUDA_TRY(cudaMemcpyAsync(y, P->ybuf, sizeof(double2) * n, cudaMemcpyDeviceToHost, P->stream));
     FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
     return FMM_OK;
+}
+
+extern "C" int fmm_matvec(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComplex *y, int nrhs, int precision)
+{
+    return apply_operator((Plan *)plan, x, y, nrhs, precision, 0, 0);
 }
 
 // Transposed operator: the sources become point sources at the centroids (multipole
@@ -262,35 +292,7 @@ extern "C" int fmm_matvec(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComp
 extern "C" int fmm_matvec_adjoint(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComplex *y, int nrhs, int precision,
                                   int conjugate)
 {
-    Plan *P = (Plan *)plan;
-    if (!P || !x || !y || nrhs < 1) { fmm_set_error("invalid argument"); return FMM_ERR_ARG; }
-    if (precision != FMM_FP64 && precision != FMM_MIXED) { fmm_set_error("unknown precision %d", precision); return FMM_ERR_ARG; }
-    {
-        int st = build_transpose(P);
-        if (st) return st;
-    }
-    bool xd = is_device_ptr(x), yd = is_device_ptr(y);
-    for (int r = 0; r < nrhs; r++) {
-        const double2 *xs = (const double2 *)x + (size_t)r * P->nf;
-        double2 *ys = (double2 *)y + (size_t)r * P->nf;
-        const double2 *xin = xs;
-        double2 *yout = yd ? ys : P->ybuf;
-        if (!xd) {
-            FMM_CUDA_TRY(cudaMemcpyAsync(P->xbuf, xs, sizeof(double2) * P->nf, cudaMemcpyHostToDevice, P->stream));
-            xin = P->xbuf;
-        }
-        if (conjugate) {
-            launch_conj(P, xin, P->xbuf);
-            xin = P->xbuf;
-        }
-        int st = run_matvec(P, xin, yout, precision, 1);
-        if (st) return st;
-        if (conjugate) launch_conj(P, yout, yout);
-        FMM_CUDA_TRY(cudaGetLastError());
-        if (!yd) FMM_CUDA_TRY(cudaMemcpyAsync(ys, P->ybuf, sizeof(double2) * P->nf, cudaMemcpyDeviceToHost, P->stream));
-    }
-    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
-    return FMM_OK;
+    return apply_operator((Plan *)plan, x, y, nrhs, precision, 1, conjugate ? 1 : 0);
 }
 
 extern "C" int fmm_set_profiling(fmm_plan *plan, int on)
@@ -318,16 +320,19 @@ extern "C" int fmm_last_timings(const fmm_plan *plan, const char **names, double
     return FMM_OK;
 }
 
-// ---------------------------------------------------------------------------- BLAS-1 kernels
+// ---------------------------------------------------------------------------- batched BLAS-1
+// Column r of a batch of R vectors of length n; V holds Krylov vectors as [j][r][n].
 namespace fmm {
-__global__ void multi_dot_kernel(const double2 *V, size_t ld, int nvec, const double2 *w, int n, double2 *out)
+// out[r * nvec + j] += conj(V_j,r) . W_r   (grid: x over n, y = j, z = r)
+__global__ void bdot_kernel(const double2 *V, size_t vj, size_t vr, const double2 *W, size_t wr, int n, int nvec,
+                            double2 *out)
 {
-    int j = blockIdx.y;
-    const double2 *v = V + (size_t)j * ld;
+    int j = blockIdx.y, r = blockIdx.z;
+    const double2 *v = V + (size_t)j * vj + (size_t)r * vr, *w = W + (size_t)r * wr;
     double ar = 0, ai = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double2 a = v[i], b = w[i];
-        ar += a.x * b.x + a.y * b.y; // conj(a) b
+        ar += a.x * b.x + a.y * b.y;
         ai += a.x * b.y - a.y * b.x;
     }
     __shared__ double sr[256], si[256];
@@ -338,238 +343,327 @@ __global__ void multi_dot_kernel(const double2 *V, size_t ld, int nvec, const do
         if (threadIdx.x < s) { sr[threadIdx.x] += sr[threadIdx.x + s]; si[threadIdx.x] += si[threadIdx.x + s]; }
         __syncthreads();
     }
-    if (threadIdx.x == 0) { atomicAdd(&out[j].x, sr[0]); atomicAdd(&out[j].y, si[0]); }
+    if (threadIdx.x == 0) {
+        atomicAdd(&out[(size_t)r * nvec + j].x, sr[0]);
+        atomicAdd(&out[(size_t)r * nvec + j].y, si[0]);
+    }
 }
 
-// w -= sum_j V_j h_j
-__global__ void multi_axpy_kernel(const double2 *V, size_t ld, int nvec, const double2 *h, double2 *w, int n)
+// W_r -= sum_{j < nvec} V_j,r h[r * hs + j]   (grid: x over n, z = r)
+__global__ void baxpy_kernel(const double2 *V, size_t vj, size_t vr, int nvec, const double2 *h, int hs, double2 *W,
+                             size_t wr, int n)
 {
+    int r = blockIdx.z;
+    const double2 *v = V + (size_t)r * vr, *c = h + (size_t)r * hs;
+    double2 *w = W + (size_t)r * wr;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double2 acc = w[i];
         for (int j = 0; j < nvec; j++) {
-            double2 v = V[(size_t)j * ld + i], c = h[j];
-            acc.x -= v.x * c.x - v.y * c.y;
-            acc.y -= v.x * c.y + v.y * c.x;
+            double2 a = v[(size_t)j * vj + i], b = c[j];
+            acc.x -= a.x * b.x - a.y * b.y;
+            acc.y -= a.x * b.y + a.y * b.x;
         }
         w[i] = acc;
     }
 }
 
-// y = alpha x + beta y (alpha, beta complex)
-__global__ void axpby_kernel(double2 alpha, const double2 *x, double2 beta, double2 *y, int n)
+// Y_r = alpha[r] X_r   (alpha real per column; grid: x over n, z = r)
+__global__ void bscale_kernel(const double *alpha, const double2 *X, size_t xr, double2 *Y, size_t yr, int n)
 {
+    int r = blockIdx.z;
+    double a = alpha[r];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double2 v = X[(size_t)r * xr + i];
+        Y[(size_t)r * yr + i] = make_double2(a * v.x, a * v.y);
+    }
+}
+
+// y = alpha x + beta y over n entries (alpha, beta real)
+__global__ void axpby_kernel(double alpha, const double2 *x, double beta, double2 *y, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         double2 a = x[i], b = y[i];
-        y[i] = make_double2(alpha.x * a.x - alpha.y * a.y + beta.x * b.x - beta.y * b.y,
-                            alpha.x * a.y + alpha.y * a.x + beta.x * b.y + beta.y * b.x);
+        y[i] = make_double2(alpha * a.x + beta * b.x, alpha * a.y + beta * b.y);
     }
 }
 } // namespace fmm
 
 static const int BLAS_BLOCKS = 152 * 2;
 
-static int dev_dots(Plan *P, const double2 *V, int nvec, const double2 *w, double2 *hdev, std::vector<double2> &hhost)
+static unsigned blas_grid(size_t n) { return (unsigned)std::min<size_t>(BLAS_BLOCKS, (n + 255) / 256); }
+
+// Workspace of the batched solver for R columns and restart m.
+static int ensure_gmres(Plan *P, int restart, int R)
 {
-    FMM_CUDA_TRY(cudaMemsetAsync(hdev, 0, sizeof(double2) * nvec, P->stream));
-    dim3 grid(std::min(BLAS_BLOCKS, (P->nf + 255) / 256), nvec);
-    multi_dot_kernel<<<grid, 256, 0, P->stream>>>(V, P->nf, nvec, w, P->nf, hdev);
-    hhost.resize(nvec);
-    FMM_CUDA_TRY(cudaMemcpyAsync(hhost.data(), hdev, sizeof(double2) * nvec, cudaMemcpyDeviceToHost, P->stream));
+    if (P->gm_restart >= restart && P->gm_cols >= R) return FMM_OK;
+    restart = std::max(restart, P->gm_restart);
+    R = std::max(R, P->gm_cols);
+    for (double2 **q : {&P->gm_V, &P->gm_w, &P->gm_r, &P->gm_x, &P->gm_b, &P->gm_d, &P->gm_dev_h}) {
+        cudaFree(*q);
+        *q = nullptr;
+    }
+    cudaFree(P->gm_alpha);
+    P->gm_alpha = nullptr;
+    size_t n = (size_t)P->nf * R;
+    FMM_CUDA_TRY(cudaMalloc(&P->gm_V, sizeof(double2) * n * (restart + 1)));
+    FMM_CUDA_TRY(cudaMalloc(&P->gm_w, sizeof(double2) * n));
+    FMM_CUDA_TRY(cudaMalloc(&P->gm_r, sizeof(double2) * n));
+    FMM_CUDA_TRY(cudaMalloc(&P->gm_x, sizeof(double2) * n));
+    FMM_CUDA_TRY(cudaMalloc(&P->gm_b, sizeof(double2) * n));
+    FMM_CUDA_TRY(cudaMalloc(&P->gm_d, sizeof(double2) * n));
+    FMM_CUDA_TRY(cudaMalloc(&P->gm_dev_h, sizeof(double2) * (size_t)R * (restart + 1)));
+    FMM_CUDA_TRY(cudaMalloc(&P->gm_alpha, sizeof(double) * R));
+    P->gm_restart = restart;
+    P->gm_cols = R;
+    return FMM_OK;
+}
+
+// out[r * nvec + j] = <V_j,r, W_r> for the R columns, copied to the host
+static int bdots(Plan *P, const double2 *V, size_t vj, size_t vr, const double2 *W, size_t wr, int nvec, int R,
+                 std::vector<double2> &out)
+{
+    FMM_CUDA_TRY(cudaMemsetAsync(P->gm_dev_h, 0, sizeof(double2) * (size_t)R * nvec, P->stream));
+    dim3 grid(std::min(BLAS_BLOCKS / 2, (P->nf + 255) / 256), nvec, R);
+    bdot_kernel<<<grid, 256, 0, P->stream>>>(V, vj, vr, W, wr, P->nf, nvec, P->gm_dev_h);
+    out.resize((size_t)R * nvec);
+    FMM_CUDA_TRY(cudaMemcpyAsync(out.data(), P->gm_dev_h, sizeof(double2) * out.size(), cudaMemcpyDeviceToHost, P->stream));
     FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
     return FMM_OK;
 }
 
-static int dev_norm(Plan *P, const double2 *w, double *out)
+static int bnorms(Plan *P, const double2 *W, int R, std::vector<double> &out)
 {
     std::vector<double2> h;
-    int st = dev_dots(P, w, 1, w, P->gm_dev_h, h);
+    int st = bdots(P, W, 0, P->nf, W, P->nf, 1, R, h);
     if (st) return st;
-    *out = sqrt(std::max(0.0, h[0].x));
+    out.resize(R);
+    for (int r = 0; r < R; r++) out[r] = sqrt(std::max(0.0, h[r].x));
     return FMM_OK;
 }
 
-static void axpby(Plan *P, double2 a, const double2 *x, double2 b, double2 *y)
+static int bscale(Plan *P, const std::vector<double> &alpha, const double2 *X, double2 *Y, int R)
 {
-    axpby_kernel<<<std::min(BLAS_BLOCKS, (P->nf + 255) / 256), 256, 0, P->stream>>>(a, x, b, y, P->nf);
-}
-
-static int ensure_gmres(Plan *P, int restart)
-{
-    if (P->gm_restart >= restart) return FMM_OK;
-    if (P->gm_V) cudaFree(P->gm_V);
-    if (!P->gm_w) {
-        FMM_CUDA_TRY(cudaMalloc(&P->gm_w, sizeof(double2) * P->nf));
-        FMM_CUDA_TRY(cudaMalloc(&P->gm_r, sizeof(double2) * P->nf));
-        FMM_CUDA_TRY(cudaMalloc(&P->gm_x, sizeof(double2) * P->nf));
-        FMM_CUDA_TRY(cudaMalloc(&P->gm_b, sizeof(double2) * P->nf));
-        FMM_CUDA_TRY(cudaMalloc(&P->gm_d, sizeof(double2) * P->nf));
-        FMM_CUDA_TRY(cudaMalloc(&P->gm_dev_h, sizeof(double2) * 512));
-    }
-    FMM_CUDA_TRY(cudaMalloc(&P->gm_V, sizeof(double2) * (size_t)P->nf * (restart + 1)));
-    P->gm_restart = restart;
+    FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_alpha, alpha.data(), sizeof(double) * R, cudaMemcpyHostToDevice, P->stream));
+    bscale_kernel<<<dim3(blas_grid(P->nf) / 2 + 1, 1, R), 256, 0, P->stream>>>(P->gm_alpha, X, P->nf, Y, P->nf, P->nf);
     return FMM_OK;
 }
 
-// Restarted GMRES with classical Gram-Schmidt applied twice (CGS2); all vectors FP64 on the
-// device; Hessenberg least squares by Givens rotations on the host.  Solves A x = b where
-// the matvec runs at `precision`; x (device) holds the initial guess.  Convergence is
-// relative to bnorm_ref.
-static int gmres_core(Plan *P, const double2 *b, double2 *x, double tol, int maxit, int restart, int precision,
-                      double bnorm_ref, int *iters, double *relres)
+static void axpby(Plan *P, double a, const double2 *x, double b, double2 *y, size_t n)
 {
-    int n = P->nf, m = restart;
-    std::vector<double2> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), hcol, h2;
+    axpby_kernel<<<blas_grid(n), 256, 0, P->stream>>>(a, x, b, y, n);
+}
+
+// Restarted GMRES on R columns at once (lockstep): every Krylov step applies the operator to
+// all R columns in one batched matvec; classical Gram-Schmidt applied twice (CGS2), FP64
+// vectors on the device, Hessenberg least squares by Givens rotations on the host per
+// column.  A column stops extending its basis once its residual estimate is below tol[r]
+// (its new basis vectors are zero).  Solves A X = B at `precision`; X (device) holds the
+// initial guess.  Convergence of column r is relative to bref[r].
+static int gmres_batch(Plan *P, const double2 *B, double2 *X, int R, const std::vector<double> &tol, int maxit,
+                       int restart, int precision, const std::vector<double> &bref, std::vector<int> &iters,
+                       std::vector<double> &res)
+{
+    const int n = P->nf, m = restart;
+    const size_t vj = (size_t)R * n; // Krylov vector j of column r at j * vj + r * n
+    std::vector<std::vector<double2>> H(R, std::vector<double2>((size_t)(m + 1) * m)), g(R, std::vector<double2>(m + 1)),
+        cs(R, std::vector<double2>(m)), sn(R, std::vector<double2>(m));
+    std::vector<double2> h1, h2;
+    std::vector<double> beta, hn, alpha(R);
+    std::vector<int> kdim(R), running(R);
+    iters.assign(R, 0);
+    res.assign(R, 0.0);
     int total = 0;
-    double res = 0.0;
     while (true) {
-        // r = b - A x
-        int st = run_matvec(P, x, P->gm_r, precision);
+        // R = B - A X, its norms, and which columns still need work
+        int st = run_matvec(P, X, P->gm_r, precision, 0, R);
         if (st) return st;
-        axpby(P, make_double2(1, 0), b, make_double2(-1, 0), P->gm_r);
-        double beta;
-        if ((st = dev_norm(P, P->gm_r, &beta))) return st;
-        res = beta / bnorm_ref;
-        if (!std::isfinite(res)) { fmm_set_error("GMRES residual is not finite"); return FMM_ERR_BREAKDOWN; }
-        if (res <= tol || total >= maxit) break;
-        axpby(P, make_double2(1.0 / beta, 0), P->gm_r, make_double2(0, 0), P->gm_V);
-        std::fill(g.begin(), g.end(), make_double2(0, 0));
-        g[0] = make_double2(beta, 0);
+        axpby(P, 1.0, B, -1.0, P->gm_r, (size_t)R * n);
+        if ((st = bnorms(P, P->gm_r, R, beta))) return st;
+        int any = 0;
+        for (int r = 0; r < R; r++) {
+            res[r] = bref[r] > 0 ? beta[r] / bref[r] : 0.0;
+            if (!std::isfinite(res[r])) { fmm_set_error("GMRES residual of column %d is not finite", r); return FMM_ERR_BREAKDOWN; }
+            running[r] = res[r] > tol[r];
+            any |= running[r];
+            alpha[r] = running[r] ? 1.0 / beta[r] : 0.0;
+            kdim[r] = 0;
+            std::fill(g[r].begin(), g[r].end(), make_double2(0, 0));
+            g[r][0] = make_double2(beta[r], 0);
+        }
+        if (!any || total >= maxit) break;
+        if ((st = bscale(P, alpha, P->gm_r, P->gm_V, R))) return st;
         int j = 0;
         for (; j < m && total < maxit; j++) {
-            double2 *vj = P->gm_V + (size_t)j * n, *w = P->gm_w;
-            if ((st = run_matvec(P, vj, w, precision))) return st;
-            // two passes of classical Gram-Schmidt
-            if ((st = dev_dots(P, P->gm_V, j + 1, w, P->gm_dev_h, hcol))) return st;
-            multi_axpy_kernel<<<std::min(BLAS_BLOCKS, (n + 255) / 256), 256, 0, P->stream>>>(P->gm_V, n, j + 1, P->gm_dev_h, w, n);
-            if ((st = dev_dots(P, P->gm_V, j + 1, w, P->gm_dev_h, h2))) return st;
-            multi_axpy_kernel<<<std::min(BLAS_BLOCKS, (n + 255) / 256), 256, 0, P->stream>>>(P->gm_V, n, j + 1, P->gm_dev_h, w, n);
-            for (int i = 0; i <= j; i++) { hcol[i].x += h2[i].x; hcol[i].y += h2[i].y; }
-            double hn;
-            if ((st = dev_norm(P, w, &hn))) return st;
+            double2 *Vj = P->gm_V + (size_t)j * vj, *W = P->gm_w;
+            if ((st = run_matvec(P, Vj, W, precision, 0, R))) return st;
+            if ((st = bdots(P, P->gm_V, vj, n, W, n, j + 1, R, h1))) return st;
+            baxpy_kernel<<<dim3(blas_grid(n) / 2 + 1, 1, R), 256, 0, P->stream>>>(P->gm_V, vj, n, j + 1, P->gm_dev_h, j + 1, W, n, n);
+            if ((st = bdots(P, P->gm_V, vj, n, W, n, j + 1, R, h2))) return st;
+            baxpy_kernel<<<dim3(blas_grid(n) / 2 + 1, 1, R), 256, 0, P->stream>>>(P->gm_V, vj, n, j + 1, P->gm_dev_h, j + 1, W, n, n);
+            if ((st = bnorms(P, W, R, hn))) return st;
             total++;
-            for (int i = 0; i <= j; i++) H[(size_t)i * m + j] = hcol[i];
-            H[(size_t)(j + 1) * m + j] = make_double2(hn, 0);
-            // apply previous rotations
-            for (int i = 0; i < j; i++) {
-                double2 a = H[(size_t)i * m + j], bq = H[(size_t)(i + 1) * m + j];
-                double2 c = cs[i], s = sn[i];
-                // [c  s; -conj(s) c] with c real
-                double2 na = make_double2(c.x * a.x + s.x * bq.x - s.y * bq.y, c.x * a.y + s.x * bq.y + s.y * bq.x);
-                double2 nb = make_double2(-(s.x * a.x + s.y * a.y) + c.x * bq.x, -(s.x * a.y - s.y * a.x) + c.x * bq.y);
-                H[(size_t)i * m + j] = na;
-                H[(size_t)(i + 1) * m + j] = nb;
+            any = 0;
+            for (int r = 0; r < R; r++) {
+                alpha[r] = 0.0;
+                if (!running[r]) continue;
+                iters[r]++;
+                std::vector<double2> &Hr = H[r], &gr = g[r], &c_ = cs[r], &s_ = sn[r];
+                for (int i = 0; i <= j; i++) {
+                    double2 a = h1[(size_t)r * (j + 1) + i], b = h2[(size_t)r * (j + 1) + i];
+                    Hr[(size_t)i * m + j] = make_double2(a.x + b.x, a.y + b.y);
+                }
+                double h = hn[r];
+                // previous rotations [c s; -conj(s) c], c real
+                for (int i = 0; i < j; i++) {
+                    double2 a = Hr[(size_t)i * m + j], bq = Hr[(size_t)(i + 1) * m + j], c = c_[i], sv = s_[i];
+                    Hr[(size_t)i * m + j] = make_double2(c.x * a.x + sv.x * bq.x - sv.y * bq.y, c.x * a.y + sv.x * bq.y + sv.y * bq.x);
+                    Hr[(size_t)(i + 1) * m + j] =
+                        make_double2(-(sv.x * a.x + sv.y * a.y) + c.x * bq.x, -(sv.x * a.y - sv.y * a.x) + c.x * bq.y);
+                }
+                double2 a = Hr[(size_t)j * m + j];
+                double an = hypot(a.x, a.y), den = hypot(an, h);
+                kdim[r] = j + 1;
+                if (den == 0.0) { // the basis is exhausted: nothing more to add for this column
+                    kdim[r] = j;
+                    running[r] = 0;
+                    continue;
+                }
+                double2 c, sv;
+                if (an == 0.0) { c = make_double2(0, 0); sv = make_double2(1, 0); }
+                else { c = make_double2(an / den, 0); sv = make_double2(a.x / an * h / den, a.y / an * h / den); }
+                c_[j] = c;
+                s_[j] = sv;
+                Hr[(size_t)j * m + j] = make_double2(c.x * a.x + sv.x * h, c.x * a.y + sv.y * h);
+                double2 gj = gr[j];
+                gr[j + 1] = make_double2(-(sv.x * gj.x + sv.y * gj.y), -(sv.x * gj.y - sv.y * gj.x));
+                gr[j] = make_double2(c.x * gj.x, c.x * gj.y);
+                res[r] = hypot(gr[j + 1].x, gr[j + 1].y) / bref[r];
+                if (h == 0.0 || res[r] <= tol[r]) { running[r] = 0; continue; }
+                alpha[r] = 1.0 / h;
+                any = 1;
             }
-            double2 a = H[(size_t)j * m + j];
-            double an = hypot(a.x, a.y), den = hypot(an, hn);
-            double2 c, s;
-            if (den == 0.0) { fmm_set_error("GMRES breakdown"); return FMM_ERR_BREAKDOWN; }
-            if (an == 0.0) { c = make_double2(0, 0); s = make_double2(1, 0); }
-            else {
-                c = make_double2(an / den, 0);
-                // s = (a/|a|) * conj(hn) / den ; hn real
-                s = make_double2(a.x / an * hn / den, a.y / an * hn / den);
+            if (j + 1 < m) {
+                if ((st = bscale(P, alpha, W, P->gm_V + (size_t)(j + 1) * vj, R))) return st;
             }
-            cs[j] = c;
-            sn[j] = s;
-            H[(size_t)j * m + j] = make_double2(c.x * a.x + s.x * hn, c.x * a.y + s.y * hn);
-            H[(size_t)(j + 1) * m + j] = make_double2(0, 0);
-            double2 gj = g[j];
-            g[j + 1] = make_double2(-(s.x * gj.x + s.y * gj.y), -(s.x * gj.y - s.y * gj.x));
-            g[j] = make_double2(c.x * gj.x, c.x * gj.y);
-            res = hypot(g[j + 1].x, g[j + 1].y) / bnorm_ref;
-            if (hn == 0.0 || res <= tol) { j++; break; }
-            axpby(P, make_double2(1.0 / hn, 0), w, make_double2(0, 0), P->gm_V + (size_t)(j + 1) * n);
+            if (!any) { j++; break; }
         }
-        // back substitution, x += V y
-        int kdim = j;
-        std::vector<double2> yv(kdim);
-        for (int i = kdim - 1; i >= 0; i--) {
-            double2 acc = g[i];
-            for (int q = i + 1; q < kdim; q++) {
-                double2 h = H[(size_t)i * m + q];
-                acc.x -= h.x * yv[q].x - h.y * yv[q].y;
-                acc.y -= h.x * yv[q].y + h.y * yv[q].x;
+        // X_r += V_r y_r, y_r from the triangular systems (zero beyond kdim[r])
+        int kmax = 0;
+        for (int r = 0; r < R; r++) kmax = std::max(kmax, kdim[r]);
+        std::vector<double2> Y((size_t)R * std::max(kmax, 1), make_double2(0, 0));
+        for (int r = 0; r < R; r++) {
+            std::vector<double2> &Hr = H[r];
+            for (int i = kdim[r] - 1; i >= 0; i--) {
+                double2 acc = g[r][i];
+                for (int q = i + 1; q < kdim[r]; q++) {
+                    double2 hq = Hr[(size_t)i * m + q], yq = Y[(size_t)r * kmax + q];
+                    acc.x -= hq.x * yq.x - hq.y * yq.y;
+                    acc.y -= hq.x * yq.y + hq.y * yq.x;
+                }
+                double2 d = Hr[(size_t)i * m + i];
+                double dd = d.x * d.x + d.y * d.y;
+                Y[(size_t)r * kmax + i] = make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd);
             }
-            double2 d = H[(size_t)i * m + i];
-            double dd = d.x * d.x + d.y * d.y;
-            yv[i] = make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd);
         }
-        FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_dev_h, yv.data(), sizeof(double2) * kdim, cudaMemcpyHostToDevice, P->stream));
-        // x -= V (-y)
-        for (int i = 0; i < kdim; i++) yv[i] = make_double2(-yv[i].x, -yv[i].y);
-        FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_dev_h, yv.data(), sizeof(double2) * kdim, cudaMemcpyHostToDevice, P->stream));
-        multi_axpy_kernel<<<std::min(BLAS_BLOCKS, (n + 255) / 256), 256, 0, P->stream>>>(P->gm_V, n, kdim, P->gm_dev_h, x, n);
+        if (kmax > 0) {
+            for (auto &v : Y) v = make_double2(-v.x, -v.y); // baxpy subtracts
+            FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_dev_h, Y.data(), sizeof(double2) * Y.size(), cudaMemcpyHostToDevice, P->stream));
+            baxpy_kernel<<<dim3(blas_grid(n) / 2 + 1, 1, R), 256, 0, P->stream>>>(P->gm_V, vj, n, kmax, P->gm_dev_h, kmax, X, n, n);
+        }
         FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
-        if (res <= tol || total >= maxit) {
-            // recompute the true residual once more at the top of the loop
-            int st2 = run_matvec(P, x, P->gm_r, precision);
-            if (st2) return st2;
-            axpby(P, make_double2(1, 0), b, make_double2(-1, 0), P->gm_r);
-            double bt;
-            if ((st2 = dev_norm(P, P->gm_r, &bt))) return st2;
-            res = bt / bnorm_ref;
-            break;
-        }
     }
-    if (iters) *iters = total;
-    if (relres) *relres = res;
     return FMM_OK;
+}
+
+// Solve for R columns at `precision`.  FMM_MIXED runs iterative refinement: FP64 residual
+// B - A X, inner batched GMRES on the mixed-precision matvec for the correction, X += D.
+static int solve_batch(Plan *P, int R, double tol, int maxit, int restart, int precision, std::vector<int> &iters,
+                       std::vector<double> &relres)
+{
+    int n = P->nf, st;
+    std::vector<double> bnorm;
+    if ((st = bnorms(P, P->gm_b, R, bnorm))) return st;
+    for (auto &b : bnorm) if (b == 0.0) b = 1.0;
+    std::vector<double> tolv(R, tol);
+    if (precision == FMM_FP64) return gmres_batch(P, P->gm_b, P->gm_x, R, tolv, maxit, restart, FMM_FP64, bnorm, iters, relres);
+    iters.assign(R, 0);
+    relres.assign(R, 0.0);
+    std::vector<double> rn, itol(R);
+    std::vector<int> it_in;
+    std::vector<double> rr_in;
+    int total = 0;
+    for (int outer = 0; outer < 20; outer++) {
+        // residual in FP64; columns already below tol get a zero right-hand side
+        if ((st = run_matvec(P, P->gm_x, P->gm_w, FMM_FP64, 0, R))) return st;
+        axpby(P, 1.0, P->gm_b, -1.0, P->gm_w, (size_t)R * n);
+        if ((st = bnorms(P, P->gm_w, R, rn))) return st;
+        int any = 0;
+        std::vector<double> keep(R);
+        for (int r = 0; r < R; r++) {
+            relres[r] = rn[r] / bnorm[r];
+            keep[r] = relres[r] > tol ? 1.0 : 0.0;
+            any |= relres[r] > tol;
+            itol[r] = std::min(0.1, std::max(1e-5, 0.5 * tol / std::max(relres[r], 1e-300)));
+        }
+        if (!any || total >= maxit) break;
+        // inner right-hand sides in gm_d's partner slot: scale converged columns to zero
+        if ((st = bscale(P, keep, P->gm_w, P->gm_w, R))) return st;
+        FMM_CUDA_TRY(cudaMemsetAsync(P->gm_d, 0, sizeof(double2) * (size_t)R * n, P->stream));
+        std::vector<double> rref(rn);
+        for (auto &v : rref) if (v == 0.0) v = 1.0;
+        // gmres_batch uses gm_r, gm_w (as W), gm_V: move the right-hand sides out of gm_w
+        double2 *rhs = nullptr;
+        FMM_CUDA_TRY(cudaMallocAsync(&rhs, sizeof(double2) * (size_t)R * n, P->stream));
+        FMM_CUDA_TRY(cudaMemcpyAsync(rhs, P->gm_w, sizeof(double2) * (size_t)R * n, cudaMemcpyDeviceToDevice, P->stream));
+        st = gmres_batch(P, rhs, P->gm_d, R, itol, maxit - total, restart, FMM_MIXED, rref, it_in, rr_in);
+        cudaFreeAsync(rhs, P->stream);
+        if (st) return st;
+        int step = 0;
+        for (int r = 0; r < R; r++) {
+            iters[r] += it_in[r];
+            step = std::max(step, it_in[r]);
+        }
+        total += std::max(step, 1);
+        axpby(P, 1.0, P->gm_d, 1.0, P->gm_x, (size_t)R * n);
+    }
+    return FMM_OK;
+}
+
+static int solve_entry(Plan *P, const cuDoubleComplex *b, cuDoubleComplex *x, int R, double tol, int maxit, int restart,
+                       int precision, int *iters, double *relres)
+{
+    if (!P || !b || !x || R < 1 || !(tol > 0) || maxit < 1 || restart < 1 || restart > 500) { fmm_set_error("invalid argument"); return FMM_ERR_ARG; }
+    if (precision != FMM_FP64 && precision != FMM_MIXED) { fmm_set_error("unknown precision"); return FMM_ERR_ARG; }
+    int st = ensure_gmres(P, restart, R);
+    if (st) return st;
+    size_t n = (size_t)P->nf * R;
+    bool bd = is_device_ptr(b), xd = is_device_ptr(x);
+    FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_b, b, sizeof(double2) * n, bd ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, P->stream));
+    FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_x, x, sizeof(double2) * n, xd ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, P->stream));
+    std::vector<int> it;
+    std::vector<double> rr;
+    if ((st = solve_batch(P, R, tol, maxit, restart, precision, it, rr))) return st;
+    FMM_CUDA_TRY(cudaMemcpyAsync(x, P->gm_x, sizeof(double2) * n, xd ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, P->stream));
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    bool ok = true;
+    for (int r = 0; r < R; r++) {
+        if (iters) iters[r] = it[r];
+        if (relres) relres[r] = rr[r];
+        ok = ok && rr[r] <= tol;
+    }
+    return ok ? FMM_OK : FMM_ERR_NOT_CONVERGED;
 }
 
 extern "C" int fmm_gmres(fmm_plan *plan, const cuDoubleComplex *b, cuDoubleComplex *x, double tol, int maxit,
                          int restart, int precision, int *iters, double *relres)
 {
-    Plan *P = (Plan *)plan;
-    if (!P || !b || !x || !(tol > 0) || maxit < 1 || restart < 1 || restart > 500) { fmm_set_error("invalid argument"); return FMM_ERR_ARG; }
-    if (precision != FMM_FP64 && precision != FMM_MIXED) { fmm_set_error("unknown precision"); return FMM_ERR_ARG; }
-    int st = ensure_gmres(P, restart);
-    if (st) return st;
-    int n = P->nf;
-    bool bd = is_device_ptr(b), xd = is_device_ptr(x);
-    FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_b, b, sizeof(double2) * n, bd ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, P->stream));
-    FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_x, x, sizeof(double2) * n, xd ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, P->stream));
-    double bnorm;
-    if ((st = dev_norm(P, P->gm_b, &bnorm))) return st;
-    if (bnorm == 0.0) bnorm = 1.0;
-    int it = 0;
-    double rr = 0.0;
-    if (precision == FMM_FP64) {
-        st = gmres_core(P, P->gm_b, P->gm_x, tol, maxit, restart, FMM_FP64, bnorm, &it, &rr);
-    } else {
-        // iterative refinement: r = b - A64 x (FP64), solve A32 d = r, x += d
-        double2 *d = P->gm_d;
-        int total = 0;
-        for (int outer = 0; outer < 20; outer++) {
-            if ((st = run_matvec(P, P->gm_x, P->gm_w, FMM_FP64))) return st;
-            // gm_w = b - A x  (kept in gm_w; gmres_core uses gm_r and gm_w as work, so copy to d's rhs slot)
-            axpby(P, make_double2(1, 0), P->gm_b, make_double2(-1, 0), P->gm_w);
-            double rn;
-            if ((st = dev_norm(P, P->gm_w, &rn))) return st;
-            rr = rn / bnorm;
-            if (rr <= tol || total >= maxit) break;
-            // inner solve on a copy of the residual
-            double2 *rhs = nullptr;
-            FMM_CUDA_TRY(cudaMalloc(&rhs, sizeof(double2) * n));
-            FMM_CUDA_TRY(cudaMemcpyAsync(rhs, P->gm_w, sizeof(double2) * n, cudaMemcpyDeviceToDevice, P->stream));
-            FMM_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(double2) * n, P->stream));
-            double inner_tol = std::max(1e-5, 0.5 * tol / rr);
-            if (inner_tol > 0.1) inner_tol = 0.1;
-            int iti = 0;
-            double rri = 0;
-            st = gmres_core(P, rhs, d, inner_tol, maxit - total, restart, FMM_MIXED, rn, &iti, &rri);
-            cudaFree(rhs);
-            if (st) return st;
-            total += iti;
-            axpby(P, make_double2(1, 0), d, make_double2(1, 0), P->gm_x);
-        }
-        it = total;
-    }
-    if (st) return st;
-    FMM_CUDA_TRY(cudaMemcpyAsync(x, P->gm_x, sizeof(double2) * n, xd ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, P->stream));
-    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
-    if (iters) *iters = it;
-    if (relres) *relres = rr;
-    return rr <= tol ? FMM_OK : FMM_ERR_NOT_CONVERGED;
+    return solve_entry((Plan *)plan, b, x, 1, tol, maxit, restart, precision, iters, relres);
+}
+
+extern "C" int fmm_solve_batched(fmm_plan *plan, const cuDoubleComplex *B, cuDoubleComplex *X, int nrhs, double tol,
+                                 int maxit, int restart, int precision, int *iters, double *relres)
+{
+    return solve_entry((Plan *)plan, B, X, nrhs, tol, maxit, restart, precision, iters, relres);
 }
 
 extern "C" int fmm_far_field(fmm_plan *plan, const cuDoubleComplex *p, const double *pts, int npts, cuDoubleComplex *out)

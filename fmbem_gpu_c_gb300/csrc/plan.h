@@ -11,12 +11,17 @@ constexpr int NDIR = 316;      // M2L offsets (dx,dy,dz) in [-3,3]^3 with max |d
 constexpr int NDIST = 15;      // distinct squared lengths of those offsets
 constexpr int MAX_TIMERS = 64;
 
-// Work list of one batched translation pass: items (direction, first, count, coaxial
-// block) over translations sorted by direction, TC translations per item at most.
+// Work list of one batched translation pass: translations sorted by direction (src, dst,
+// key_beg per direction, key_w = coaxial block per direction) and the device items
+// (direction, first column, count, coaxial block) for items_nrhs right-hand sides, tc
+// columns per item at most.
 struct RcrList {
     int4 *items = nullptr;
+    size_t items_cap = 0;
     int *src = nullptr, *dst = nullptr;
-    int n_items = 0, tc = 8, shc = 0; // columns per item; rotation/coaxial blocks staged in shared memory
+    std::vector<int> key_beg, key_w;
+    int n_items = 0, items_nrhs = 0;
+    int tc = 8, shc = 0;          // columns per item; rotation/coaxial blocks staged in shared memory
 };
 
 struct LevelDev {
@@ -75,7 +80,8 @@ struct Plan {
     float2 *nearT32 = nullptr;
     // work vectors
     double2 *xbuf = nullptr, *ybuf = nullptr;
-    int nrhs_cap = 0;
+    int nrhs_cap = 0;             // columns of xbuf / ybuf
+    int rhs_cap32 = 1;            // right-hand sides the FP32 expansions (Cm32, Dl32) hold
     cudaStream_t stream = nullptr;
     size_t device_bytes = 0;
     char mixed_note[160] = "plan was created without build_mixed";
@@ -89,7 +95,8 @@ struct Plan {
     // GMRES workspace
     double2 *gm_V = nullptr, *gm_w = nullptr, *gm_r = nullptr, *gm_x = nullptr, *gm_b = nullptr, *gm_d = nullptr;
     double2 *gm_dev_h = nullptr;
-    int gm_restart = 0;
+    double *gm_alpha = nullptr;
+    int gm_restart = 0, gm_cols = 0; // workspace for restart length and right-hand sides
 };
 
 // allocation tracking
@@ -109,15 +116,16 @@ int gen_coax_matrices_f32(double k, const double *t, int n, int p, int sr, float
 int build_lists(Plan *P);
 
 // passes.cu
-int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpose = 0);
+// y = A x (or A^T x) for nrhs columns of nf entries, device pointers
+int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpose = 0, int nrhs = 1);
 int build_transpose(Plan *P);
-void launch_conj(Plan *P, const double2 *x, double2 *y);
+void launch_conj(Plan *P, const double2 *x, double2 *y, size_t n);
 
 // batched.cu
 int build_rcr_lists(Plan *P);
 size_t rcr_tile_smem(int p, int tc, int shc);
-int launch_rcr_pass(const RcrList &Lst, int p, int pin, int pout, int atomic, const float *H, int hstride,
+int launch_rcr_pass(RcrList &Lst, int p, int pin, int pout, int atomic, const float *H, int hstride,
                     const float2 *PH, int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst,
-                    cudaStream_t st);
+                    int nrhs, int nsrc, int ndst, cudaStream_t st);
 
 } // namespace fmm

@@ -85,8 +85,8 @@ int fmm_plan_destroy(fmm_plan *plan);
 int fmm_plan_info(const fmm_plan *plan, fmm_info *info);
 
 /* y = A x for nrhs right-hand sides stored one after another (nf each).  precision is
- * FMM_FP64 (plain path) or FMM_MIXED (FP32 translations and near field).  x and y may be
- * host or device pointers. */
+ * FMM_FP64 (plain path, one column after another) or FMM_MIXED (FP32 translations and near
+ * field, all columns in one batched pass).  x and y may be host or device pointers. */
 int fmm_matvec(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComplex *y, int nrhs, int precision);
 
 /* y = A^T x (conjugate = 0) or y = A^H x (conjugate = 1), the transposed / adjoint operator
@@ -102,6 +102,16 @@ int fmm_matvec_adjoint(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComplex
  * mixed-precision matvec.  x holds the initial guess on entry.  iters/relres may be NULL. */
 int fmm_gmres(fmm_plan *plan, const cuDoubleComplex *b, cuDoubleComplex *x, double tol, int maxit,
               int restart, int precision, int *iters, double *relres);
+
+/* Solve A X = B for nrhs right-hand sides at once (B and X hold nrhs columns of nf, one
+ * after another; X holds the initial guesses).  The columns advance in lockstep: every Krylov
+ * step applies the operator to all of them in one batched matvec (FMM_MIXED: one pass of the
+ * translation tiles over all columns), with FMM_MIXED running FP64-residual iterative
+ * refinement as fmm_gmres does.  iters[nrhs] and relres[nrhs] (may be NULL) receive each
+ * column's Krylov iterations and final relative residual.  FMM_ERR_NOT_CONVERGED if any
+ * column misses tol.  No counterpart in the reference, which solves nothing. */
+int fmm_solve_batched(fmm_plan *plan, const cuDoubleComplex *B, cuDoubleComplex *X, int nrhs, double tol, int maxit,
+                      int restart, int precision, int *iters, double *relres);
 
 /* Scattered pressure of a rigid body at npts exterior points from the surface pressure p:
  * sum_j p_j int_{T_j} dG/dn_x(x, y) dS(x), regular rule of the plan. */

@@ -42,3 +42,26 @@ def test_gmres_reports_non_convergence(fm):
     x, it, rr, ok = plan.gmres(b, tol=1e-14, maxit=2, restart=2, precision=fm.FMM_FP64)
     assert not ok and it == 2 and rr > 1e-14
     plan.close()
+
+
+def test_batched_solve_matches_single_solves(fm, oracle):
+    """Four plane-wave directions solved at once (lockstep GMRES, batched matvecs) against one
+    solve per direction; the z-direction far field against the Mie series."""
+    V, F = fm.icosphere(3, 0.1)
+    plan = fm.Plan(V, F, k=K1, depth=3, p_levels={2: 8, 3: 8}, rule=fm.RULE_DUNAVANT7, a=0.5, b=0.0, c=-1.0)
+    dirs = [(0.0, 0.0, 1.0), (1.0, 0.0, 0.0), (0.0, 0.6, 0.8), (-0.48, 0.6, 0.64)]
+    B = np.stack([plan.plane_wave(d) for d in dirs])
+    pts = fm.fibonacci_sphere(100, 1.0)
+    for prec in (fm.FMM_FP64, fm.FMM_MIXED):
+        X, it, rr, ok = plan.solve_batched(B, tol=1e-6, restart=40, precision=prec)
+        assert ok and (rr <= 1e-6).all() and (it > 0).all()
+        for r in range(len(dirs)):
+            xs, _, rrs, oks = plan.gmres(B[r], tol=1e-6, restart=40, precision=prec)
+            assert oks and rel(X[r], xs) < 2e-5
+        assert rel(plan.far_field(X[0], pts), oracle.mie_rigid(K1, 0.1, pts)) < 0.02
+    # a column that starts at its solution stops at once while the others iterate
+    X0 = np.zeros_like(B)
+    X0[2] = X[2]
+    X, it, rr, ok = plan.solve_batched(B, X0=X0, tol=1e-5, restart=40, precision=fm.FMM_FP64)
+    assert ok and it[2] == 0 and (it[[0, 1, 3]] > 0).all()
+    plan.close()
