@@ -70,6 +70,7 @@ def lib():
                                 c_ip, c_dp]
         L.fmm_solve_batched.argtypes = [c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, c_ip, c_dp]
+        L.fmm_vjp.argtypes = [c_vp, c_vp, c_dp, c_dp, ctypes.c_int, c_vp, ctypes.c_double, ctypes.c_int, c_dp, c_vp]
         L.fmm_far_field.argtypes = [c_vp, c_vp, c_dp, ctypes.c_int, c_vp]
         L.fmm_plane_wave_rhs.argtypes = [c_vp, c_dp, c_vp]
         L.fmm_mesh_icosphere.argtypes = [ctypes.c_int, ctypes.c_double, c_dp, c_ip, c_ip, c_ip]
@@ -134,6 +135,7 @@ class Plan:
         self.h = h
         self.info = self._info()
         self.nf = self.info.num_elem
+        self.nv = self.info.num_vert
 
     def _info(self):
         i = Info()
@@ -187,6 +189,19 @@ class Plan:
         if st not in (0, 6):
             _check(st)
         return X, it, rr, st == 0
+
+    def vjp(self, x, pts, pbar, direction=(0.0, 0.0, 1.0), tol=1e-10, precision=FMM_FP64):
+        """dJ/dV (nv x 3) for dJ = 2 Re(pbar^H dp), p = far_field(x, pts), x solving A x = plane_wave(direction)
+        (direction None: a right-hand side that does not move with the mesh).  Returns (grad, lambda)."""
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        pts = np.ascontiguousarray(pts, dtype=np.float64)
+        pbar = np.ascontiguousarray(pbar, dtype=np.complex128)
+        grad = np.zeros((self.nv, 3), dtype=np.float64)
+        lam = np.zeros(self.nf, dtype=np.complex128)
+        d = None if direction is None else np.ascontiguousarray(direction, dtype=np.float64)
+        _check(lib().fmm_vjp(self.h, _ptr(x), None if d is None else d.ctypes.data_as(c_dp), pts.ctypes.data_as(c_dp),
+                             len(pts), _ptr(pbar), tol, precision, grad.ctypes.data_as(c_dp), _ptr(lam)))
+        return grad, lam
 
     def far_field(self, p, pts):
         p = np.ascontiguousarray(p, dtype=np.complex128)

@@ -461,7 +461,7 @@ static void axpby(Plan *P, double a, const double2 *x, double b, double2 *y, siz
 // initial guess.  Convergence of column r is relative to bref[r].
 static int gmres_batch(Plan *P, const double2 *B, double2 *X, int R, const std::vector<double> &tol, int maxit,
                        int restart, int precision, const std::vector<double> &bref, std::vector<int> &iters,
-                       std::vector<double> &res)
+                       std::vector<double> &res, int transpose)
 {
     const int n = P->nf, m = restart;
     const size_t vj = (size_t)R * n; // Krylov vector j of column r at j * vj + r * n
@@ -475,7 +475,7 @@ static int gmres_batch(Plan *P, const double2 *B, double2 *X, int R, const std::
     int total = 0;
     while (true) {
         // R = B - A X, its norms, and which columns still need work
-        int st = run_matvec(P, X, P->gm_r, precision, 0, R);
+        int st = run_matvec(P, X, P->gm_r, precision, transpose, R);
         if (st) return st;
         axpby(P, 1.0, B, -1.0, P->gm_r, (size_t)R * n);
         if ((st = bnorms(P, P->gm_r, R, beta))) return st;
@@ -495,7 +495,7 @@ static int gmres_batch(Plan *P, const double2 *B, double2 *X, int R, const std::
         int j = 0;
         for (; j < m && total < maxit; j++) {
             double2 *Vj = P->gm_V + (size_t)j * vj, *W = P->gm_w;
-            if ((st = run_matvec(P, Vj, W, precision, 0, R))) return st;
+            if ((st = run_matvec(P, Vj, W, precision, transpose, R))) return st;
             if ((st = bdots(P, P->gm_V, vj, n, W, n, j + 1, R, h1))) return st;
             baxpy_kernel<<<dim3(blas_grid(n) / 2 + 1, 1, R), 256, 0, P->stream>>>(P->gm_V, vj, n, j + 1, P->gm_dev_h, j + 1, W, n, n);
             if ((st = bdots(P, P->gm_V, vj, n, W, n, j + 1, R, h2))) return st;
@@ -578,14 +578,15 @@ static int gmres_batch(Plan *P, const double2 *B, double2 *X, int R, const std::
 // Solve for R columns at `precision`.  FMM_MIXED runs iterative refinement: FP64 residual
 // B - A X, inner batched GMRES on the mixed-precision matvec for the correction, X += D.
 static int solve_batch(Plan *P, int R, double tol, int maxit, int restart, int precision, std::vector<int> &iters,
-                       std::vector<double> &relres)
+                       std::vector<double> &relres, int transpose = 0)
 {
     int n = P->nf, st;
     std::vector<double> bnorm;
     if ((st = bnorms(P, P->gm_b, R, bnorm))) return st;
     for (auto &b : bnorm) if (b == 0.0) b = 1.0;
     std::vector<double> tolv(R, tol);
-    if (precision == FMM_FP64) return gmres_batch(P, P->gm_b, P->gm_x, R, tolv, maxit, restart, FMM_FP64, bnorm, iters, relres);
+    if (precision == FMM_FP64)
+        return gmres_batch(P, P->gm_b, P->gm_x, R, tolv, maxit, restart, FMM_FP64, bnorm, iters, relres, transpose);
     iters.assign(R, 0);
     relres.assign(R, 0.0);
     std::vector<double> rn, itol(R);
@@ -594,7 +595,7 @@ static int solve_batch(Plan *P, int R, double tol, int maxit, int restart, int p
     int total = 0;
     for (int outer = 0; outer < 20; outer++) {
         // residual in FP64; columns already below tol get a zero right-hand side
-        if ((st = run_matvec(P, P->gm_x, P->gm_w, FMM_FP64, 0, R))) return st;
+        if ((st = run_matvec(P, P->gm_x, P->gm_w, FMM_FP64, transpose, R))) return st;
         axpby(P, 1.0, P->gm_b, -1.0, P->gm_w, (size_t)R * n);
         if ((st = bnorms(P, P->gm_w, R, rn))) return st;
         int any = 0;
@@ -615,7 +616,7 @@ static int solve_batch(Plan *P, int R, double tol, int maxit, int restart, int p
         double2 *rhs = nullptr;
         FMM_CUDA_TRY(cudaMallocAsync(&rhs, sizeof(double2) * (size_t)R * n, P->stream));
         FMM_CUDA_TRY(cudaMemcpyAsync(rhs, P->gm_w, sizeof(double2) * (size_t)R * n, cudaMemcpyDeviceToDevice, P->stream));
-        st = gmres_batch(P, rhs, P->gm_d, R, itol, maxit - total, restart, FMM_MIXED, rref, it_in, rr_in);
+        st = gmres_batch(P, rhs, P->gm_d, R, itol, maxit - total, restart, FMM_MIXED, rref, it_in, rr_in, transpose);
         cudaFreeAsync(rhs, P->stream);
         if (st) return st;
         int step = 0;
@@ -653,6 +654,28 @@ static int solve_entry(Plan *P, const cuDoubleComplex *b, cuDoubleComplex *x, in
     }
     return ok ? FMM_OK : FMM_ERR_NOT_CONVERGED;
 }
+
+namespace fmm {
+// A^T x = rhs for one column, device buffers (the adjoint solve of fmm_vjp)
+int solve_transposed(Plan *P, const double2 *rhs_dev, double2 *x_dev, double tol, int maxit, int restart, int precision,
+                     int *iters, double *relres)
+{
+    int st = build_transpose(P);
+    if (st) return st;
+    if ((st = ensure_gmres(P, restart, 1))) return st;
+    size_t n = P->nf;
+    FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_b, rhs_dev, sizeof(double2) * n, cudaMemcpyDeviceToDevice, P->stream));
+    FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_x, x_dev, sizeof(double2) * n, cudaMemcpyDeviceToDevice, P->stream));
+    std::vector<int> it;
+    std::vector<double> rr;
+    if ((st = solve_batch(P, 1, tol, maxit, restart, precision, it, rr, 1))) return st;
+    FMM_CUDA_TRY(cudaMemcpyAsync(x_dev, P->gm_x, sizeof(double2) * n, cudaMemcpyDeviceToDevice, P->stream));
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    if (iters) *iters = it[0];
+    if (relres) *relres = rr[0];
+    return rr[0] <= tol ? FMM_OK : FMM_ERR_NOT_CONVERGED;
+}
+} // namespace fmm
 
 extern "C" int fmm_gmres(fmm_plan *plan, const cuDoubleComplex *b, cuDoubleComplex *x, double tol, int maxit,
                          int restart, int precision, int *iters, double *relres)

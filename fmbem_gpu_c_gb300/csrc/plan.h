@@ -104,6 +104,7 @@ cudaError_t dev_alloc(Plan *P, void **ptr, size_t bytes);
 
 // tables.cu
 int gen_rotation_tables(Plan *P);
+void rule_tables(double bary[2][48], double w[2][16], int n[2]);
 int gen_coax_tables(Plan *P);
 int gen_element_tables(Plan *P);
 int gen_near_field(Plan *P);

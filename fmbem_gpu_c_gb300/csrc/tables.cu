@@ -39,10 +39,13 @@ static void gauss_legendre(int n, double *x, double *w)
     }
 }
 
-static int upload_rules()
+// The two regular rules as host tables (barycentric points, weights in units of J, counts).
+void rule_tables(double bary[2][48], double w[2][16], int n[2])
 {
-    double bary[2][48] = {{0}}, w[2][16] = {{0}};
-    int n[2];
+    for (int r = 0; r < 2; r++)
+        for (int i = 0; i < 48; i++) bary[r][i] = 0.0;
+    for (int r = 0; r < 2; r++)
+        for (int i = 0; i < 16; i++) w[r][i] = 0.0;
     double x[3], wt[3];
     gauss_legendre(3, x, wt);
     int q = 0;
@@ -68,6 +71,13 @@ static int upload_rules()
         w[1][t] = 0.5 * ww[t];
     }
     n[1] = 7;
+}
+
+static int upload_rules()
+{
+    double bary[2][48], w[2][16];
+    int n[2];
+    rule_tables(bary, w, n);
     FMM_CUDA_TRY(cudaMemcpyToSymbol(c_rule_bary, bary, sizeof(bary)));
     FMM_CUDA_TRY(cudaMemcpyToSymbol(c_rule_w, w, sizeof(w)));
     FMM_CUDA_TRY(cudaMemcpyToSymbol(c_rule_n, n, sizeof(n)));

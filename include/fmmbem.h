@@ -113,6 +113,18 @@ int fmm_gmres(fmm_plan *plan, const cuDoubleComplex *b, cuDoubleComplex *x, doub
 int fmm_solve_batched(fmm_plan *plan, const cuDoubleComplex *B, cuDoubleComplex *X, int nrhs, double tol, int maxit,
                       int restart, int precision, int *iters, double *relres);
 
+/* Reverse-mode derivative of a far-field objective with respect to the vertex positions.
+ * x solves A x = b, b the plane wave exp(i k dir.c) at the centroids (dir NULL: b does not
+ * depend on the mesh); p = F x is the scattered field at the npts points pts (fmm_far_field).
+ * Given pbar with dJ = 2 Re(pbar^H dp) (pbar = p for J = sum |p|^2), grad[3*nv] receives
+ *     dJ/dV = 2 Re[ pbar^H (dF/dV) x + lambda^H (db/dV - (dA/dV) x) ],
+ * lambda solving A^H lambda = F^H pbar by GMRES to tol at `precision`; lambda[nf] (may be
+ * NULL) receives it.  dA/dV is the derivative of the operator fmm_matvec applies, with the
+ * octree, truncation orders and box centres held fixed.  Host or device buffers.  Leaf
+ * orders up to 23.  No counterpart in the reference. */
+int fmm_vjp(fmm_plan *plan, const cuDoubleComplex *x, const double *dir, const double *pts, int npts,
+            const cuDoubleComplex *pbar, double tol, int precision, double *grad, cuDoubleComplex *lambda);
+
 /* Scattered pressure of a rigid body at npts exterior points from the surface pressure p:
  * sum_j p_j int_{T_j} dG/dn_x(x, y) dS(x), regular rule of the plan. */
 int fmm_far_field(fmm_plan *plan, const cuDoubleComplex *p, const double *pts, int npts, cuDoubleComplex *out);
