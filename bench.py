@@ -151,8 +151,8 @@ def peaks():
 
 
 def ncu_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "m2l_kernel_cfg2.md")
+    """DRAM bytes of the dominant kernel per matvec (all its launches) from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "rcr_tile_kernel_traffic_cfg2.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
