@@ -249,17 +249,17 @@ __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_lea
 
 static inline int block_for(int p) { return p >= 16 ? 256 : 128; }
 
-static void timer_begin(Plan *P, const char *name)
+static void timer_begin(Plan *P, const char *name, cudaStream_t st = nullptr)
 {
     if (!P->profiling || P->ntimers >= MAX_TIMERS) return;
     Timer &t = P->timers[P->ntimers];
     t.name = name;
-    cudaEventRecord(t.beg, P->stream);
+    cudaEventRecord(t.beg, st ? st : P->stream);
 }
-static void timer_end(Plan *P)
+static void timer_end(Plan *P, cudaStream_t st = nullptr)
 {
     if (!P->profiling || P->ntimers >= MAX_TIMERS) return;
-    cudaEventRecord(P->timers[P->ntimers].end, P->stream);
+    cudaEventRecord(P->timers[P->ntimers].end, st ? st : P->stream);
     P->ntimers++;
 }
 
@@ -366,13 +366,22 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
             if (e) return e;
             timer_end(P);
         }
+        // the M2L passes of different levels are independent: fork them onto the plan's
+        // side streams so that one level's tail overlaps the next level's work, then join
+        FMM_CUDA_TRY(cudaEventRecord(P->fork_ev, st));
         for (int l = lmin; l <= lmax; l++) {
             LevelDev &L = P->lev[l];
-            timer_begin(P, m2l_names[l]);
+            cudaStream_t sl = P->side[(l - lmin) % NSIDE];
+            FMM_CUDA_TRY(cudaStreamWaitEvent(sl, P->fork_ev, 0));
+            timer_begin(P, m2l_names[l], sl);
             int e = launch_rcr_pass(L.m2l, L.p, L.p, L.p, 1, (const float *)Hsr, rs, (const float2 *)PHsr, w, pmax - 1,
-                                    (const float2 *)Csr(l), (const float2 *)Cm(l), (float2 *)Dl(l), nrhs, L.nb, L.nb, st);
+                                    (const float2 *)Csr(l), (const float2 *)Cm(l), (float2 *)Dl(l), nrhs, L.nb, L.nb, sl);
             if (e) return e;
-            timer_end(P);
+            timer_end(P, sl);
+        }
+        for (int i = 0; i < NSIDE; i++) {
+            FMM_CUDA_TRY(cudaEventRecord(P->join_ev[i], P->side[i]));
+            FMM_CUDA_TRY(cudaStreamWaitEvent(st, P->join_ev[i], 0));
         }
         for (int l = lmin + 1; l <= lmax; l++) {
             LevelDev &L = P->lev[l], &PL = P->lev[l - 1];

@@ -79,6 +79,11 @@ static void free_plan(Plan *P)
         for (int i = 0; i < MAX_TIMERS; i++) { cudaEventDestroy(P->timers[i].beg); cudaEventDestroy(P->timers[i].end); }
     if (P->timers_created) { cudaEventDestroy(P->total.beg); cudaEventDestroy(P->total.end); }
     if (P->stream) cudaStreamDestroy(P->stream);
+    for (int i = 0; i < NSIDE; i++) {
+        if (P->side[i]) cudaStreamDestroy(P->side[i]);
+        if (P->join_ev[i]) cudaEventDestroy(P->join_ev[i]);
+    }
+    if (P->fork_ev) cudaEventDestroy(P->fork_ev);
     delete P;
 }
 
@@ -113,6 +118,11 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
     // a blocking stream: setup code mixes kernels on this stream with default-stream
     // cudaMemcpy read-backs (list counts), which must wait for those kernels
     CTRY(cudaStreamCreate(&P->stream));
+    for (int i = 0; i < NSIDE; i++) {
+        CTRY(cudaStreamCreateWithFlags(&P->side[i], cudaStreamNonBlocking));
+        CTRY(cudaEventCreateWithFlags(&P->join_ev[i], cudaEventDisableTiming));
+    }
+    CTRY(cudaEventCreateWithFlags(&P->fork_ev, cudaEventDisableTiming));
     if (build_tree(P->V, P->F, opt->s, opt->depth, P->tree) != 0 || P->tree.lmax > FMM_MAX_LEVEL) {
         fmm_set_error("octree build failed (lmax=%d)", P->tree.lmax);
         free_plan(P);

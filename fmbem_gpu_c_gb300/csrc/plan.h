@@ -10,6 +10,7 @@ namespace fmm {
 constexpr int NDIR = 316;      // M2L offsets (dx,dy,dz) in [-3,3]^3 with max |d| >= 2
 constexpr int NDIST = 15;      // distinct squared lengths of those offsets
 constexpr int MAX_TIMERS = 64;
+constexpr int NSIDE = 3;      // side streams for the independent M2L passes
 
 // Work list of one batched translation pass: translations sorted by direction (src, dst,
 // key_beg per direction, key_w = coaxial block per direction) and the device items
@@ -83,6 +84,8 @@ struct Plan {
     int nrhs_cap = 0;             // columns of xbuf / ybuf
     int rhs_cap32 = 1;            // right-hand sides the FP32 expansions (Cm32, Dl32) hold
     cudaStream_t stream = nullptr;
+    cudaStream_t side[NSIDE] = {};  // non-blocking side streams, forked from and joined to `stream`
+    cudaEvent_t fork_ev = nullptr, join_ev[NSIDE] = {};
     size_t device_bytes = 0;
     char mixed_note[160] = "plan was created without build_mixed";
     double setup_seconds = 0.0;
