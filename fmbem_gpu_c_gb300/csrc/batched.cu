@@ -355,6 +355,7 @@ int launch_rcr_pass(RcrList &Lst, int p, int pin, int pout, int atomic, const fl
     case 64: return launch_tile<64, 16, 2, 1, false>(ps, Lst.n_items, sm, st);
     case 32: return launch_tile<32, 16, 2, 1, false>(ps, Lst.n_items, sm, st);
     case 16: return launch_tile<16, 16, 2, 1, false>(ps, Lst.n_items, sm, st);
+    case 4: return launch_tile<4, 4, 8, 4, false>(ps, Lst.n_items, sm, st);
     default: return launch_tile<8, 8, 4, 2, false>(ps, Lst.n_items, sm, st);
     }
 }
@@ -448,4 +449,61 @@ int build_rcr_lists(Plan *P)
     return FMM_OK;
 }
 
+} // namespace fmm
+
+namespace fmm {
+// Tile width per pass, chosen at plan creation by timing the candidates on this plan's own
+// lists and tables (one right-hand side): the default from pick_tile and a narrower tile --
+// 4 columns where the default is 8 (large p, few items per direction: more CTAs, two per
+// SM), half the width where it is 32 or 64.  The winner is kept; matvec results do not
+// depend on the choice beyond FP32 rounding.
+int tune_rcr_tiles(Plan *P)
+{
+    cudaEvent_t a, b;
+    FMM_CUDA_TRY(cudaEventCreate(&a));
+    FMM_CUDA_TRY(cudaEventCreate(&b));
+    int rc = FMM_OK;
+    for (int l = P->lmin; l <= P->lmax && rc == FMM_OK; l++) {
+        LevelDev &L = P->lev[l];
+        for (int which = PASS_M2M; which <= PASS_L2L && rc == FMM_OK; which++) {
+            if (which != PASS_M2L && l == P->lmin) continue;
+            RcrList &Lst = which == PASS_M2M ? L.m2m : which == PASS_M2L ? L.m2l : L.l2l;
+            if (Lst.key_beg.empty() || Lst.key_beg.back() == 0) continue;
+            int p = which == PASS_M2L ? L.p : P->lev[l - 1].p;
+            std::vector<std::pair<int, int>> cand = {{Lst.tc, Lst.shc}};
+            if (Lst.tc == 8) cand.push_back({4, 0});
+            if (Lst.tc >= 32) cand.push_back({Lst.tc / 2, rcr_tile_smem(p, Lst.tc / 2, 1) <= TWO_CTA_SMEM ? 1 : 0});
+            if (cand.size() < 2) continue;
+            float best = 1e30f;
+            std::pair<int, int> pick = cand[0];
+            for (auto &c : cand) {
+                Lst.tc = c.first;
+                Lst.shc = c.second;
+                Lst.items_nrhs = 0;
+                float tot = 0.f;
+                for (int rep = 0; rep < 4 && rc == FMM_OK; rep++) {
+                    if (cudaEventRecord(a, P->stream) != cudaSuccess) rc = FMM_ERR_CUDA;
+                    if (rc == FMM_OK) rc = launch_pass32(P, l, which, 1, P->stream);
+                    if (rc == FMM_OK && cudaEventRecord(b, P->stream) != cudaSuccess) rc = FMM_ERR_CUDA;
+                    if (rc == FMM_OK && cudaEventSynchronize(b) != cudaSuccess) rc = FMM_ERR_CUDA;
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, a, b);
+                    if (rep > 0) tot += ms;
+                }
+                if (rc != FMM_OK) break;
+                if (tot < best) {
+                    best = tot;
+                    pick = c;
+                }
+            }
+            Lst.tc = pick.first;
+            Lst.shc = pick.second;
+            Lst.items_nrhs = 0;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc == FMM_ERR_CUDA) fmm_set_error("tile tuning: %s", cudaGetErrorString(cudaGetLastError()));
+    return rc;
+}
 } // namespace fmm

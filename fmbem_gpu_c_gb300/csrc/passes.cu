@@ -307,6 +307,23 @@ static int launch_m2l_level(Plan *P, int l, const char *tname)
     return FMM_OK;
 }
 
+// One batched FP32 pass of the mixed path for level l: PASS_M2M (level l into its parents),
+// PASS_M2L (level l), PASS_L2L (parents into level l).
+int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st)
+{
+    const int pmax = P->pmax, rs = rot_size(pmax), w = 2 * pmax - 1;
+    LevelDev &L = P->lev[l];
+    if (which == PASS_M2L)
+        return launch_rcr_pass(L.m2l, L.p, L.p, L.p, 1, P->Hsr32, rs, P->PHsr32, w, pmax - 1, L.Csr32, L.Cm32, L.Dl32,
+                               nrhs, L.nb, L.nb, st);
+    LevelDev &PL = P->lev[l - 1];
+    if (which == PASS_M2M)
+        return launch_rcr_pass(L.m2m, PL.p, L.p, PL.p, 1, P->Hss32, rs, P->PHss32, w, pmax - 1, L.Crr32, L.Cm32, PL.Cm32,
+                               nrhs, L.nb, PL.nb, st);
+    return launch_rcr_pass(L.l2l, PL.p, PL.p, L.p, 0, P->Hrr32, rs, P->PHrr32, w, pmax - 1, L.Crr32, PL.Dl32, L.Dl32, nrhs,
+                           PL.nb, L.nb, st);
+}
+
 template <typename T>
 static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, int nrhs)
 {
@@ -349,7 +366,6 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
     if (!f64) {
         // mixed path: batched direction-grouped passes (batched.cu).  M2M and M2L add into
         // zeroed expansions with atomics; L2L then adds the parents' locals top-down.
-        const int rs = rot_size(pmax), w = 2 * pmax - 1;
         static const char *l2l_names[] = {"l2l_l0", "l2l_l1", "l2l_l2", "l2l_l3", "l2l_l4", "l2l_l5", "l2l_l6",
                                           "l2l_l7", "l2l_l8", "l2l_l9", "l2l_l10", "l2l_l11", "l2l_l12", "l2l_l13"};
         for (int l = lmin; l <= lmax; l++) {
@@ -359,10 +375,10 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
         }
         for (int l = lmax; l > lmin; l--) {
             LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
+            (void)L;
+            (void)PL;
             timer_begin(P, m2m_names[l]);
-            int e = launch_rcr_pass(L.m2m, PL.p, L.p, PL.p, 1, (const float *)Hss, rs, (const float2 *)PHss, w, pmax - 1,
-                                    (const float2 *)Crr(l), (const float2 *)Cm(l), (float2 *)Cm(l - 1), nrhs, L.nb,
-                                    PL.nb, st);
+            int e = launch_pass32(P, l, PASS_M2M, nrhs, st);
             if (e) return e;
             timer_end(P);
         }
@@ -374,8 +390,8 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
             cudaStream_t sl = P->side[(l - lmin) % NSIDE];
             FMM_CUDA_TRY(cudaStreamWaitEvent(sl, P->fork_ev, 0));
             timer_begin(P, m2l_names[l], sl);
-            int e = launch_rcr_pass(L.m2l, L.p, L.p, L.p, 1, (const float *)Hsr, rs, (const float2 *)PHsr, w, pmax - 1,
-                                    (const float2 *)Csr(l), (const float2 *)Cm(l), (float2 *)Dl(l), nrhs, L.nb, L.nb, sl);
+            (void)L;
+            int e = launch_pass32(P, l, PASS_M2L, nrhs, sl);
             if (e) return e;
             timer_end(P, sl);
         }
@@ -385,10 +401,10 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
         }
         for (int l = lmin + 1; l <= lmax; l++) {
             LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
+            (void)L;
+            (void)PL;
             timer_begin(P, l2l_names[l]);
-            int e = launch_rcr_pass(L.l2l, PL.p, PL.p, L.p, 0, (const float *)Hrr, rs, (const float2 *)PHrr, w, pmax - 1,
-                                    (const float2 *)Crr(l), (const float2 *)Dl(l - 1), (float2 *)Dl(l), nrhs, PL.nb,
-                                    L.nb, st);
+            int e = launch_pass32(P, l, PASS_L2L, nrhs, st);
             if (e) return e;
             timer_end(P);
         }

@@ -170,6 +170,7 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
     TRY(gen_near_field(P));
     if (P->opt.build_mixed) {
         TRY(build_rcr_lists(P));
+        TRY(tune_rcr_tiles(P));
     }
     CTRY(dev_alloc(P, (void **)&P->xbuf, sizeof(double2) * nf));
     CTRY(dev_alloc(P, (void **)&P->ybuf, sizeof(double2) * nf));

@@ -125,8 +125,12 @@ int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpo
 int build_transpose(Plan *P);
 void launch_conj(Plan *P, const double2 *x, double2 *y, size_t n);
 
+enum { PASS_M2M = 0, PASS_M2L = 1, PASS_L2L = 2 };
+int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st);
+
 // batched.cu
 int build_rcr_lists(Plan *P);
+int tune_rcr_tiles(Plan *P);
 size_t rcr_tile_smem(int p, int tc, int shc);
 int launch_rcr_pass(RcrList &Lst, int p, int pin, int pout, int atomic, const float *H, int hstride,
                     const float2 *PH, int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst,
