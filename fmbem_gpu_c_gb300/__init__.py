@@ -217,14 +217,16 @@ class Plan:
         return out
 
     def set_profiling(self, on=True):
-        _check(lib().fmm_set_profiling(self.h, 1 if on else 0))
+        """True or 1: per-kernel timers (direct launches); 2: whole-matvec timer only; False or 0: off."""
+        _check(lib().fmm_set_profiling(self.h, int(on) if not isinstance(on, bool) else (1 if on else 0)))
 
     def timings(self):
-        n = ctypes.c_int(64)
-        names = (ctypes.c_char_p * 64)()
-        ms = (ctypes.c_double * 64)()
+        cap = 80
+        n = ctypes.c_int(cap)
+        names = (ctypes.c_char_p * cap)()
+        ms = (ctypes.c_double * cap)()
         _check(lib().fmm_last_timings(self.h, names, ms, ctypes.byref(n)))
-        return [(names[i].decode(), ms[i]) for i in range(n.value)]
+        return [(names[i].decode(), ms[i]) for i in range(min(n.value, cap))]
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:

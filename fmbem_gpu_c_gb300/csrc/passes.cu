@@ -251,14 +251,14 @@ static inline int block_for(int p) { return p >= 16 ? 256 : 128; }
 
 static void timer_begin(Plan *P, const char *name, cudaStream_t st = nullptr)
 {
-    if (!P->profiling || P->ntimers >= MAX_TIMERS) return;
+    if (P->profiling != 1 || P->ntimers >= MAX_TIMERS) return;
     Timer &t = P->timers[P->ntimers];
     t.name = name;
     cudaEventRecord(t.beg, st ? st : P->stream);
 }
 static void timer_end(Plan *P, cudaStream_t st = nullptr)
 {
-    if (!P->profiling || P->ntimers >= MAX_TIMERS) return;
+    if (P->profiling != 1 || P->ntimers >= MAX_TIMERS) return;
     cudaEventRecord(P->timers[P->ntimers].end, st ? st : P->stream);
     P->ntimers++;
 }
@@ -324,6 +324,108 @@ int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st)
                            PL.nb, L.nb, st);
 }
 
+// The mixed path's translation passes for nrhs columns: zero the expansions, M2M up, the
+// M2L of every level forked onto the side streams (one level's tail overlaps the next
+// level's work), join, L2L down.  M2M and M2L add into zeroed expansions with atomics; L2L
+// then adds the parents' locals top-down.
+static int translate32_direct(Plan *P, int nrhs)
+{
+    const int lmin = P->lmin, lmax = P->lmax;
+    cudaStream_t st = P->stream;
+    if (P->profiling == 1) {
+        cudaEventRecord(P->phase.beg, st);
+        P->have_phase = 1;
+    }
+    static const char *m2m_names[] = {"m2m_l0", "m2m_l1", "m2m_l2", "m2m_l3", "m2m_l4", "m2m_l5", "m2m_l6",
+                                      "m2m_l7", "m2m_l8", "m2m_l9", "m2m_l10", "m2m_l11", "m2m_l12", "m2m_l13"};
+    static const char *m2l_names[] = {"m2l_l0", "m2l_l1", "m2l_l2", "m2l_l3", "m2l_l4", "m2l_l5", "m2l_l6",
+                                      "m2l_l7", "m2l_l8", "m2l_l9", "m2l_l10", "m2l_l11", "m2l_l12", "m2l_l13"};
+    static const char *l2l_names[] = {"l2l_l0", "l2l_l1", "l2l_l2", "l2l_l3", "l2l_l4", "l2l_l5", "l2l_l6",
+                                      "l2l_l7", "l2l_l8", "l2l_l9", "l2l_l10", "l2l_l11", "l2l_l12", "l2l_l13"};
+    for (int l = lmin; l <= lmax; l++) {
+        size_t n = (size_t)P->lev[l].nb * P->lev[l].p * P->lev[l].p * sizeof(float2) * nrhs;
+        if (l < lmax) FMM_CUDA_TRY(cudaMemsetAsync(P->lev[l].Cm32, 0, n, st));
+        FMM_CUDA_TRY(cudaMemsetAsync(P->lev[l].Dl32, 0, n, st));
+    }
+    for (int l = lmax; l > lmin; l--) {
+        timer_begin(P, m2m_names[l]);
+        int e = launch_pass32(P, l, PASS_M2M, nrhs, st);
+        if (e) return e;
+        timer_end(P);
+    }
+    // every side stream waits on the fork, also one that gets no pass, so that all of them
+    // join a graph capture
+    FMM_CUDA_TRY(cudaEventRecord(P->fork_ev, st));
+    for (int i = 0; i < NSIDE; i++) FMM_CUDA_TRY(cudaStreamWaitEvent(P->side[i], P->fork_ev, 0));
+    for (int l = lmin; l <= lmax; l++) {
+        cudaStream_t sl = P->side[(l - lmin) % NSIDE];
+        timer_begin(P, m2l_names[l], sl);
+        int e = launch_pass32(P, l, PASS_M2L, nrhs, sl);
+        if (e) return e;
+        timer_end(P, sl);
+    }
+    for (int i = 0; i < NSIDE; i++) {
+        FMM_CUDA_TRY(cudaEventRecord(P->join_ev[i], P->side[i]));
+        FMM_CUDA_TRY(cudaStreamWaitEvent(st, P->join_ev[i], 0));
+    }
+    for (int l = lmin + 1; l <= lmax; l++) {
+        timer_begin(P, l2l_names[l]);
+        int e = launch_pass32(P, l, PASS_L2L, nrhs, st);
+        if (e) return e;
+        timer_end(P);
+    }
+    if (P->profiling == 1) cudaEventRecord(P->phase.end, st);
+    return FMM_OK;
+}
+
+void drop_graph(Plan *P)
+{
+    if (P->graph_exec) cudaGraphExecDestroy(P->graph_exec);
+    P->graph_exec = nullptr;
+    P->graph_nrhs = 0;
+    P->graph_seen = 0;
+}
+
+// Translation passes as a CUDA graph: the second call with the same number of columns
+// captures them (the first has built the work items and set the kernels' attributes), later
+// calls replay the graph, which saves the ~25 launches and memsets per matvec.  Per-pass
+// profiling (mode 1) runs the passes directly so that each pass gets its own timer.
+static int translate32(Plan *P, int nrhs)
+{
+    if (P->profiling == 1) return translate32_direct(P, nrhs);
+    if (P->graph_exec && P->graph_nrhs == nrhs) {
+        FMM_CUDA_TRY(cudaGraphLaunch(P->graph_exec, P->stream));
+        return FMM_OK;
+    }
+    if (P->graph_seen != nrhs) {
+        drop_graph(P);
+        P->graph_seen = nrhs;
+        return translate32_direct(P, nrhs);
+    }
+    cudaGraph_t g = nullptr;
+    FMM_CUDA_TRY(cudaStreamBeginCapture(P->stream, cudaStreamCaptureModeThreadLocal));
+    int e = translate32_direct(P, nrhs);
+    cudaError_t ce = cudaStreamEndCapture(P->stream, &g);
+    if (e) {
+        if (g) cudaGraphDestroy(g);
+        return e;
+    }
+    if (ce != cudaSuccess) {
+        fmm_set_error("capturing the translation passes: %s", cudaGetErrorString(ce));
+        return FMM_ERR_CUDA;
+    }
+    ce = cudaGraphInstantiate(&P->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+        P->graph_exec = nullptr;
+        fmm_set_error("instantiating the translation graph: %s", cudaGetErrorString(ce));
+        return FMM_ERR_CUDA;
+    }
+    P->graph_nrhs = nrhs;
+    FMM_CUDA_TRY(cudaGraphLaunch(P->graph_exec, P->stream));
+    return FMM_OK;
+}
+
 template <typename T>
 static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, int nrhs)
 {
@@ -337,6 +439,7 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
     }
     P->ntimers = 0;
     P->have_total = 0;
+    P->have_phase = 0;
     if (P->profiling) cudaEventRecord(P->total.beg, st);
     const T *Hsr = f64 ? (const T *)P->Hsr64 : (const T *)P->Hsr32;
     const T *Hss = f64 ? (const T *)P->Hss64 : (const T *)P->Hss32;
@@ -364,50 +467,8 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
                                                      Cm(lmax), transpose, P->nf, LL.nb);
     timer_end(P);
     if (!f64) {
-        // mixed path: batched direction-grouped passes (batched.cu).  M2M and M2L add into
-        // zeroed expansions with atomics; L2L then adds the parents' locals top-down.
-        static const char *l2l_names[] = {"l2l_l0", "l2l_l1", "l2l_l2", "l2l_l3", "l2l_l4", "l2l_l5", "l2l_l6",
-                                          "l2l_l7", "l2l_l8", "l2l_l9", "l2l_l10", "l2l_l11", "l2l_l12", "l2l_l13"};
-        for (int l = lmin; l <= lmax; l++) {
-            size_t n = (size_t)P->lev[l].nb * P->lev[l].p * P->lev[l].p * sizeof(C) * nrhs;
-            if (l < lmax) FMM_CUDA_TRY(cudaMemsetAsync(Cm(l), 0, n, st));
-            FMM_CUDA_TRY(cudaMemsetAsync(Dl(l), 0, n, st));
-        }
-        for (int l = lmax; l > lmin; l--) {
-            LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
-            (void)L;
-            (void)PL;
-            timer_begin(P, m2m_names[l]);
-            int e = launch_pass32(P, l, PASS_M2M, nrhs, st);
-            if (e) return e;
-            timer_end(P);
-        }
-        // the M2L passes of different levels are independent: fork them onto the plan's
-        // side streams so that one level's tail overlaps the next level's work, then join
-        FMM_CUDA_TRY(cudaEventRecord(P->fork_ev, st));
-        for (int l = lmin; l <= lmax; l++) {
-            LevelDev &L = P->lev[l];
-            cudaStream_t sl = P->side[(l - lmin) % NSIDE];
-            FMM_CUDA_TRY(cudaStreamWaitEvent(sl, P->fork_ev, 0));
-            timer_begin(P, m2l_names[l], sl);
-            (void)L;
-            int e = launch_pass32(P, l, PASS_M2L, nrhs, sl);
-            if (e) return e;
-            timer_end(P, sl);
-        }
-        for (int i = 0; i < NSIDE; i++) {
-            FMM_CUDA_TRY(cudaEventRecord(P->join_ev[i], P->side[i]));
-            FMM_CUDA_TRY(cudaStreamWaitEvent(st, P->join_ev[i], 0));
-        }
-        for (int l = lmin + 1; l <= lmax; l++) {
-            LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
-            (void)L;
-            (void)PL;
-            timer_begin(P, l2l_names[l]);
-            int e = launch_pass32(P, l, PASS_L2L, nrhs, st);
-            if (e) return e;
-            timer_end(P);
-        }
+        int e = translate32(P, nrhs);
+        if (e) return e;
     }
     for (int l = lmax; l > lmin && f64; l--) {
         LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
@@ -446,6 +507,7 @@ int set_dir_dist(const int *dd)
 static int ensure_rhs32(Plan *P, int nrhs)
 {
     if (nrhs <= P->rhs_cap32) return FMM_OK;
+    drop_graph(P); // the captured passes address the old expansions
     for (int l = P->lmin; l <= P->lmax; l++) {
         LevelDev &L = P->lev[l];
         size_t n = (size_t)L.nb * L.p * L.p;

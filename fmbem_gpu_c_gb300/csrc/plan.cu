@@ -77,7 +77,11 @@ static void free_plan(Plan *P)
     F(P->gm_V); F(P->gm_w); F(P->gm_r); F(P->gm_x); F(P->gm_b); F(P->gm_d); F(P->gm_dev_h); F(P->gm_alpha);
     if (P->timers_created)
         for (int i = 0; i < MAX_TIMERS; i++) { cudaEventDestroy(P->timers[i].beg); cudaEventDestroy(P->timers[i].end); }
-    if (P->timers_created) { cudaEventDestroy(P->total.beg); cudaEventDestroy(P->total.end); }
+    if (P->timers_created) {
+        cudaEventDestroy(P->total.beg); cudaEventDestroy(P->total.end);
+        cudaEventDestroy(P->phase.beg); cudaEventDestroy(P->phase.end);
+    }
+    drop_graph(P);
     if (P->stream) cudaStreamDestroy(P->stream);
     for (int i = 0; i < NSIDE; i++) {
         if (P->side[i]) cudaStreamDestroy(P->side[i]);
@@ -181,6 +185,8 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
     }
     CTRY(cudaEventCreate(&P->total.beg));
     CTRY(cudaEventCreate(&P->total.end));
+    CTRY(cudaEventCreate(&P->phase.beg));
+    CTRY(cudaEventCreate(&P->phase.end));
     P->timers_created = 1;
     CTRY(cudaStreamSynchronize(P->stream));
     P->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -309,7 +315,8 @@ extern "C" int fmm_matvec_adjoint(fmm_plan *plan, const cuDoubleComplex *x, cuDo
 extern "C" int fmm_set_profiling(fmm_plan *plan, int on)
 {
     if (!plan) return FMM_ERR_ARG;
-    ((Plan *)plan)->profiling = on ? 1 : 0;
+    if (on < 0 || on > 2) { fmm_set_error("profiling mode %d not in 0..2", on); return FMM_ERR_ARG; }
+    ((Plan *)plan)->profiling = on;
     return FMM_OK;
 }
 
@@ -317,14 +324,17 @@ extern "C" int fmm_last_timings(const fmm_plan *plan, const char **names, double
 {
     const Plan *P = (const Plan *)plan;
     if (!P || !count) return FMM_ERR_ARG;
-    int total = P->ntimers + (P->have_total ? 1 : 0);
+    std::vector<std::pair<const Timer *, const char *>> all;
+    for (int i = 0; i < P->ntimers; i++) all.push_back({&P->timers[i], P->timers[i].name});
+    if (P->have_phase) all.push_back({&P->phase, "translations"});
+    if (P->have_total) all.push_back({&P->total, "matvec"});
+    int total = (int)all.size();
     int n = std::min(*count, total);
     for (int i = 0; i < n; i++) {
-        const Timer &tm = i < P->ntimers ? P->timers[i] : P->total;
         float t = 0.f;
-        cudaEventSynchronize(tm.end);
-        cudaEventElapsedTime(&t, tm.beg, tm.end);
-        if (names) names[i] = i < P->ntimers ? tm.name : "matvec";
+        cudaEventSynchronize(all[i].first->end);
+        cudaEventElapsedTime(&t, all[i].first->beg, all[i].first->end);
+        if (names) names[i] = all[i].second;
         if (ms) ms[i] = t;
     }
     *count = total;

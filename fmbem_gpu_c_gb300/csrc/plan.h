@@ -86,6 +86,8 @@ struct Plan {
     cudaStream_t stream = nullptr;
     cudaStream_t side[NSIDE] = {};  // non-blocking side streams, forked from and joined to `stream`
     cudaEvent_t fork_ev = nullptr, join_ev[NSIDE] = {};
+    cudaGraphExec_t graph_exec = nullptr; // captured mixed translation passes for graph_nrhs columns
+    int graph_nrhs = 0, graph_seen = 0;
     size_t device_bytes = 0;
     char mixed_note[160] = "plan was created without build_mixed";
     double setup_seconds = 0.0;
@@ -93,7 +95,8 @@ struct Plan {
     int profiling = 0;
     Timer timers[MAX_TIMERS];
     Timer total;                  // whole matvec, recorded when profiling
-    int have_total = 0;
+    Timer phase;                  // the mixed translation passes as a whole (per-pass profiling)
+    int have_total = 0, have_phase = 0;
     int ntimers = 0, timers_created = 0;
     // GMRES workspace
     double2 *gm_V = nullptr, *gm_w = nullptr, *gm_r = nullptr, *gm_x = nullptr, *gm_b = nullptr, *gm_d = nullptr;
@@ -124,6 +127,7 @@ int build_lists(Plan *P);
 int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpose = 0, int nrhs = 1);
 int build_transpose(Plan *P);
 void launch_conj(Plan *P, const double2 *x, double2 *y, size_t n);
+void drop_graph(Plan *P);
 
 enum { PASS_M2M = 0, PASS_M2L = 1, PASS_L2L = 2 };
 int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st);

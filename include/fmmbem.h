@@ -162,9 +162,13 @@ int fmm_coax_matrices_noalloc(double k, const double *t, int n, int p, int sr, c
 /* Last error message of the calling thread (static storage). */
 const char *fmm_last_error(void);
 
-/* Per-kernel timing of the last matvec on the plan's stream (milliseconds), filled when
- * profiling is enabled with fmm_set_profiling(plan, 1).  names[i] are static strings; the
- * last entry, "matvec", spans the whole matvec (kernels, memsets and the gaps between them). */
+/* Timing of the last matvec on the plan's stream (milliseconds).  fmm_set_profiling(plan,
+ * mode): 0 off; 1 one entry per kernel or pass (the mixed translation passes then run as
+ * direct launches) plus the whole matvec; 2 the whole matvec only (the mixed translation
+ * passes keep running as a replayed CUDA graph).  names[i] are static strings; the last
+ * entry, "matvec", spans the whole matvec (kernels, memsets and the gaps between them); in
+ * mode 1 the mixed path adds "translations", the M2M/M2L/L2L phase as a whole (its M2L
+ * passes overlap on side streams, so their own timers overlap too). */
 int fmm_set_profiling(fmm_plan *plan, int on);
 int fmm_last_timings(const fmm_plan *plan, const char **names, double *ms, int *count);
 

@@ -122,6 +122,27 @@ def test_mixed_batched_columns_match_single_column(fm, sphere3, x3):
     plan.close()
 
 
+def test_graph_replay_and_profiling_modes(fm, sphere3, x3):
+    """The mixed translation passes replayed as a CUDA graph (profiling off or mode 2) give the
+    direct launches' result (mode 1, one timer per pass)."""
+    V, F = sphere3
+    plan = fm.Plan(V, F, k=K1, depth=3, p_levels={2: 8, 3: 8}, rule=1, a=0.5, b=0.0, c=-1.0)
+    plan.set_profiling(1)
+    direct = plan.matvec(x3, fm.FMM_MIXED)
+    names = [n for n, _ in plan.timings()]
+    assert names[0] == "p2m" and names[-2:] == ["translations", "matvec"]
+    assert {"m2m_l3", "m2l_l2", "m2l_l3", "l2l_l3", "l2p_near"} <= set(names)
+    plan.set_profiling(2)
+    for _ in range(3):  # first call direct, second captures, third replays
+        y = plan.matvec(x3, fm.FMM_MIXED)
+        assert rel(y, direct) < 1e-6
+    tm = plan.timings()
+    assert [n for n, _ in tm] == ["matvec"] and tm[0][1] > 0
+    plan.set_profiling(False)
+    assert rel(plan.matvec(x3, fm.FMM_MIXED), direct) < 1e-6
+    plan.close()
+
+
 def test_repeated_matvec_is_reproducible(fm, sphere3, x3):
     """FP64: owner-computes accumulation without atomics, identical bits run to run.
     Mixed: FP32 atomics in the batched translation tiles, equal to rounding."""
