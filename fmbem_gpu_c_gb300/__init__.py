@@ -74,6 +74,10 @@ def lib():
         L.fmm_far_field.argtypes = [c_vp, c_vp, c_dp, ctypes.c_int, c_vp]
         L.fmm_plane_wave_rhs.argtypes = [c_vp, c_dp, c_vp]
         L.fmm_mesh_icosphere.argtypes = [ctypes.c_int, ctypes.c_double, c_dp, c_ip, c_ip, c_ip]
+        L.fmm_mesh_geodesic.argtypes = [ctypes.c_int, ctypes.c_double, c_dp, c_ip, c_ip, c_ip]
+        L.fmm_mesh_ellipsoid.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_ulonglong, c_dp, c_ip, c_ip, c_ip]
+        L.fmm_mesh_box.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, c_dp, c_ip, c_ip, c_ip]
         L.fmm_last_error.restype = ctypes.c_char_p
         L.fmm_set_profiling.argtypes = [c_vp, ctypes.c_int]
         L.fmm_last_timings.argtypes = [c_vp, ctypes.POINTER(ctypes.c_char_p), c_dp, c_ip]
@@ -101,6 +105,30 @@ def icosphere(subdiv, radius):
     _check(lib().fmm_mesh_icosphere(subdiv, radius, V.ctypes.data_as(c_dp), ctypes.byref(nv), F.ctypes.data_as(c_ip),
                                     ctypes.byref(nf)))
     return V, F
+
+
+def _mesh(fn, *args):
+    nv, nf = ctypes.c_int(), ctypes.c_int()
+    _check(fn(*args, None, ctypes.byref(nv), None, ctypes.byref(nf)))
+    V = np.zeros((nv.value, 3))
+    F = np.zeros((nf.value, 3), dtype=np.int32)
+    _check(fn(*args, V.ctypes.data_as(c_dp), ctypes.byref(nv), F.ctypes.data_as(c_ip), ctypes.byref(nf)))
+    return V, F
+
+
+def geodesic_sphere(freq, radius):
+    """Geodesic sphere, 20 freq^2 triangles (``fmm_mesh_geodesic``)."""
+    return _mesh(lib().fmm_mesh_geodesic, freq, radius)
+
+
+def ellipsoid(freq, axes, lmax=-1, sigma=0.0, seed=0):
+    """Ellipsoid with seeded radial spherical-harmonic bumps (``fmm_mesh_ellipsoid``)."""
+    return _mesh(lib().fmm_mesh_ellipsoid, freq, float(axes[0]), float(axes[1]), float(axes[2]), lmax, sigma, seed)
+
+
+def box(n, edges):
+    """Box centred at the origin, 12 n^2 triangles (``fmm_mesh_box``)."""
+    return _mesh(lib().fmm_mesh_box, n, float(edges[0]), float(edges[1]), float(edges[2]))
 
 
 def _ptr(a):

@@ -136,6 +136,17 @@ int fmm_plane_wave_rhs(fmm_plan *plan, const double *dir, cuDoubleComplex *rhs);
  * nv/nf; with V or F NULL only the counts are returned.  Vertex coordinates are rounded to
  * 9 significant digits, the precision an OBJ writer of this library emits. */
 int fmm_mesh_icosphere(int subdiv, double radius, double *V, int *nv, int *F, int *nf);
+/* Geodesic sphere: every face of the icosahedron divided into freq^2 triangles (20 freq^2 in
+ * all, e.g. freq = 100 gives 200,000), vertices on the sphere of the given radius. */
+int fmm_mesh_geodesic(int freq, double radius, double *V, int *nv, int *F, int *nf);
+/* Ellipsoid with semi-axes (ax, ay, az) on the geodesic mesh of frequency freq, displaced
+ * radially by sum_{l <= lmax} c_lm Y_lm (real orthonormal spherical harmonics, c_lm ~
+ * N(0, sigma^2) from a SplitMix64/Box-Muller stream seeded by seed; lmax = -1: no bumps). */
+int fmm_mesh_ellipsoid(int freq, double ax, double ay, double az, int lmax, double sigma, unsigned long long seed,
+                       double *V, int *nv, int *F, int *nf);
+/* Box with edges (lx, ly, lz) centred at the origin, each face an n x n grid of squares cut
+ * into two triangles (12 n^2 triangles). */
+int fmm_mesh_box(int n, double lx, double ly, double lz, double *V, int *nv, int *F, int *nf);
 
 /* Coaxial translation matrices in FP64, without any device allocation.  This entry point has
  * no counterpart in the reference.  It is meant for callers that must not let a library
