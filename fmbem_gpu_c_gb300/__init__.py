@@ -70,6 +70,8 @@ def lib():
                                 c_ip, c_dp]
         L.fmm_solve_batched.argtypes = [c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, c_ip, c_dp]
+        L.fmm_solve_many.argtypes = [ctypes.POINTER(c_vp), ctypes.c_int, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp),
+                                     ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_ip, c_dp, c_ip]
         L.fmm_vjp.argtypes = [c_vp, c_vp, c_dp, c_dp, ctypes.c_int, c_vp, ctypes.c_double, ctypes.c_int, c_dp, c_vp]
         L.fmm_far_field.argtypes = [c_vp, c_vp, c_dp, ctypes.c_int, c_vp]
         L.fmm_plane_wave_rhs.argtypes = [c_vp, c_dp, c_vp]
@@ -136,6 +138,26 @@ def _ptr(a):
     if hasattr(a, "data_ptr"):
         return ctypes.c_void_p(a.data_ptr())
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def solve_many(plans, rhs, tol=1e-6, maxit=500, restart=50, precision=FMM_FP64, nthreads=8, x0=None):
+    """Solve plans[i] x_i = rhs[i] for all i concurrently (``fmm_solve_many``).
+    Returns (xs, iters, relres, status)."""
+    n = len(plans)
+    bs = [np.ascontiguousarray(b, dtype=np.complex128) for b in rhs]
+    xs = [np.zeros_like(b) if x0 is None else np.ascontiguousarray(x0[i], dtype=np.complex128).copy()
+          for i, b in enumerate(bs)]
+    ph = (c_vp * n)(*[p.h.value for p in plans])
+    bp = (c_vp * n)(*[b.ctypes.data for b in bs])
+    xp = (c_vp * n)(*[x.ctypes.data for x in xs])
+    it = np.zeros(n, dtype=np.int32)
+    rr = np.zeros(n)
+    stv = np.zeros(n, dtype=np.int32)
+    st = lib().fmm_solve_many(ph, n, bp, xp, tol, maxit, restart, precision, nthreads, it.ctypes.data_as(c_ip),
+                              rr.ctypes.data_as(c_dp), stv.ctypes.data_as(c_ip))
+    if st not in (0, 6):
+        _check(st)
+    return xs, it, rr, stv
 
 
 class Plan:

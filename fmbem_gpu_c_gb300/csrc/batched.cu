@@ -279,11 +279,8 @@ template <int TC, int CG, int R1, int R2, bool SHC>
 static int launch_tile(const RcrPass &ps, int n_items, size_t sm, cudaStream_t st)
 {
     static size_t attr = 0;
-    if (sm > attr) {
-        FMM_CUDA_TRY(cudaFuncSetAttribute(rcr_tile_kernel<TC, CG, R1, R2, SHC>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        attr = sm;
-    }
+    int e = raise_smem_limit((const void *)rcr_tile_kernel<TC, CG, R1, R2, SHC>, sm, &attr);
+    if (e) return e;
     rcr_tile_kernel<TC, CG, R1, R2, SHC><<<n_items, 256, sm, st>>>(ps);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;

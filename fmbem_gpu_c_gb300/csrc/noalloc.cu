@@ -88,9 +88,21 @@ __global__ void coax_noalloc_kernel(double k, const double *__restrict__ tvals, 
         }
     }
     __syncthreads();
+    // (R|R) entries with n' < n from the exact symmetry (R|R)_{n'n} = (-1)^{n+n'} (R|R)_{nn'}:
+    // the recurrence loses them to cancellation at small k t, as the plan builder's generator
+    // describes
     for (int m = 0; m < p; m++) {
         int sz = p - m, off = coax_off(p, m);
-        for (int i = threadIdx.x; i < sz * sz; i += blockDim.x) C[off + i] = EE(m, m + i % sz, m + i / sz);
+        for (int i = threadIdx.x; i < sz * sz; i += blockDim.x) {
+            int a = i % sz, b = i / sz;
+            if (!sr && a < b) {
+                double2 v = EE(m, m + b, m + a);
+                double sg = ((a + b) & 1) ? -1.0 : 1.0;
+                C[off + i] = make_double2(sg * v.x, sg * v.y);
+            } else {
+                C[off + i] = EE(m, m + a, m + b);
+            }
+        }
     }
 #undef EE
 }

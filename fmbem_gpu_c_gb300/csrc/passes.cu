@@ -269,14 +269,11 @@ template <typename T>
 static int set_smem_attrs(int pmax)
 {
     typedef typename Cx<T>::t C;
-    static size_t done[2] = {0, 0};
-    int slot = sizeof(T) == 8 ? 0 : 1;
+    static size_t m2m_set = 0, m2l_set = 0;
     size_t smax = 4 * (size_t)pmax * pmax * sizeof(C);
-    if (done[slot] >= smax) return FMM_OK;
-    FMM_CUDA_TRY(cudaFuncSetAttribute(m2m_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
-    FMM_CUDA_TRY(cudaFuncSetAttribute(m2l_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
-    done[slot] = smax;
-    return FMM_OK;
+    int st = raise_smem_limit((const void *)m2m_kernel<T>, smax, &m2m_set);
+    if (st) return st;
+    return raise_smem_limit((const void *)m2l_kernel<T>, smax, &m2l_set);
 }
 
 template <typename T>

@@ -9,6 +9,9 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <atomic>
+#include <mutex>
+#include <thread>
 
 namespace fmm {
 int set_dir_dist(const int *dd);
@@ -29,6 +32,24 @@ void fmm_set_error(const char *fmt, ...)
 extern "C" const char *fmm_last_error(void) { return g_err; }
 
 namespace fmm {
+// Kernels' dynamic shared-memory limits are process-wide while plans run on several host
+// threads (fmm_solve_many): raise a limit under one lock and never lower it, so that no
+// thread's launch sees a limit below what it set.
+static std::mutex g_smem_mutex;
+
+int raise_smem_limit(const void *func, size_t bytes, size_t *cache)
+{
+    std::lock_guard<std::mutex> lock(g_smem_mutex);
+    if (*cache >= bytes) return FMM_OK;
+    cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) {
+        fmm_set_error("raising a kernel's shared-memory limit to %zu bytes: %s", bytes, cudaGetErrorString(e));
+        return FMM_ERR_CUDA;
+    }
+    *cache = bytes;
+    return FMM_OK;
+}
+
 cudaError_t dev_alloc(Plan *P, void **ptr, size_t bytes)
 {
     cudaError_t e = cudaMalloc(ptr, bytes ? bytes : 1);
@@ -708,6 +729,53 @@ extern "C" int fmm_solve_batched(fmm_plan *plan, const cuDoubleComplex *B, cuDou
                                  int maxit, int restart, int precision, int *iters, double *relres)
 {
     return solve_entry((Plan *)plan, B, X, nrhs, tol, maxit, restart, precision, iters, relres);
+}
+
+extern "C" int fmm_solve_many(fmm_plan *const *plans, int n, const cuDoubleComplex *const *b, cuDoubleComplex *const *x,
+                              double tol, int maxit, int restart, int precision, int nthreads, int *iters, double *relres,
+                              int *status)
+{
+    if (!plans || n < 0 || !b || !x || nthreads < 1) { fmm_set_error("fmm_solve_many: invalid argument"); return FMM_ERR_ARG; }
+    for (int i = 0; i < n; i++)
+        if (!plans[i] || !b[i] || !x[i]) { fmm_set_error("fmm_solve_many: null plan or buffer %d", i); return FMM_ERR_ARG; }
+    // a plan is driven by one thread at a time (plans are not thread-safe)
+    for (int i = 0; i < n; i++)
+        for (int j = i + 1; j < n; j++)
+            if (plans[i] == plans[j]) { fmm_set_error("fmm_solve_many: plan %d appears twice", i); return FMM_ERR_ARG; }
+    std::atomic<int> next(0), worst(FMM_OK);
+    std::vector<std::string> errs(n);
+    auto work = [&]() {
+        int i;
+        while ((i = next.fetch_add(1)) < n) {
+            int it = 0;
+            double rr = 0.0;
+            // FMM_MIXED where the plan has mixed-precision tables, FP64 where plan creation
+            // could not build them
+            int prec = (precision == FMM_MIXED && !((Plan *)plans[i])->U32) ? FMM_FP64 : precision;
+            int st = fmm_gmres(plans[i], b[i], x[i], tol, maxit, restart, prec, &it, &rr);
+            if (iters) iters[i] = it;
+            if (relres) relres[i] = rr;
+            if (status) status[i] = st;
+            if (st != FMM_OK) {
+                errs[i] = fmm_last_error();
+                int w = worst.load();
+                // a hard error outranks non-convergence
+                while ((w == FMM_OK || (w == FMM_ERR_NOT_CONVERGED && st != FMM_ERR_NOT_CONVERGED)) &&
+                       !worst.compare_exchange_weak(w, st)) {
+                }
+            }
+        }
+    };
+    int nt = std::min(nthreads, std::max(n, 1));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; t++) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+    int w = worst.load();
+    if (w != FMM_OK)
+        for (int i = 0; i < n; i++)
+            if (!errs[i].empty()) { fmm_set_error("fmm_solve_many: plan %d: %s", i, errs[i].c_str()); break; }
+    return w;
 }
 
 extern "C" int fmm_far_field(fmm_plan *plan, const cuDoubleComplex *p, const double *pts, int npts, cuDoubleComplex *out)

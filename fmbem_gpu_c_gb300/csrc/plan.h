@@ -107,6 +107,9 @@ struct Plan {
 
 // allocation tracking
 cudaError_t dev_alloc(Plan *P, void **ptr, size_t bytes);
+// raise func's dynamic shared-memory limit to at least bytes (thread-safe, never lowers it);
+// *cache is the limit already set for func
+int raise_smem_limit(const void *func, size_t bytes, size_t *cache);
 
 // tables.cu
 int gen_rotation_tables(Plan *P);

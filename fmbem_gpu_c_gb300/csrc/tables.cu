@@ -2,6 +2,7 @@
 // P2M/L2P, the near-field matrix by quadrature, far-field evaluation.  All in FP64; the
 // mixed-precision path receives FP32 copies.
 #include "plan.h"
+#include <cstdio>
 #include <math.h>
 #include <vector>
 #include <algorithm>
@@ -324,29 +325,42 @@ __global__ void coax_kernel(double k, const double *tvals, int p, int sr, double
         }
     }
     __syncthreads();
+    // (R|R): the recurrence forms the entries with n' < n, which are tiny at small k t, by
+    // cancellation and loses them (absolute error ~1e-16 against values down to (kt)^(n-n'));
+    // an L2L multiplies them by the large high-degree local coefficients.  They are taken from
+    // the exact coaxial symmetry (R|R)_{n'n} = (-1)^{n+n'} (R|R)_{nn'}, whose n' > n side the
+    // recurrence forms to full relative accuracy.  (S|R) is accurate in both triangles.
     for (int m = 0; m < p; m++) {
         int sz = p - m, off = coax_off(p, m);
         for (int i = threadIdx.x; i < sz * sz; i += blockDim.x) {
             int a = i % sz, b = i / sz; // a = n'-m, b = n-m
-            C[off + i] = EE(m, m + a, m + b);
+            if (!sr && a < b) {
+                double2 v = EE(m, m + b, m + a);
+                double sg = ((a + b) & 1) ? -1.0 : 1.0;
+                C[off + i] = make_double2(sg * v.x, sg * v.y);
+            } else {
+                C[off + i] = EE(m, m + a, m + b);
+            }
         }
     }
 #undef EE
 }
 
 // The mixed-precision path stores the coaxial blocks in FP32.  At high order and small
-// k t the (S|R) entries grow like h_{2p-2}(k t) and can leave the float range; refuse to
-// build such a plan rather than carry inf through the matvec.
-static int check_fp32_range(const double2 *dev, size_t n, int l)
+// k t the (S|R) entries grow like h_{2p-2}(k t) and can leave the float range: then the plan
+// is built without the mixed-precision tables (FP64 only) rather than carry inf through the
+// matvec, and a mixed call says why.
+static int check_fp32_range(Plan *P, const double2 *dev, size_t n, int l)
 {
     std::vector<double2> h(n);
     FMM_CUDA_TRY(cudaMemcpy(h.data(), dev, sizeof(double2) * n, cudaMemcpyDeviceToHost));
     double mx = 0.0;
     for (size_t i = 0; i < n; i++) mx = std::max(mx, std::max(fabs(h[i].x), fabs(h[i].y)));
     if (!(mx < 1e37)) {
-        fmm_set_error("level %d coaxial entries reach %.3g, beyond FP32 range: lower p at this level or build "
-                      "without the mixed-precision tables", l, mx);
-        return FMM_ERR_ARG;
+        P->opt.build_mixed = 0;
+        snprintf(P->mixed_note, sizeof(P->mixed_note),
+                 "no mixed-precision tables: level %d coaxial entries reach %.3g, beyond FP32 range (lower p at "
+                 "that level or use FMM_FP64)", l, mx);
     }
     return FMM_OK;
 }
@@ -380,8 +394,10 @@ int gen_coax_tables(Plan *P)
         FMM_CUDA_TRY(cudaGetLastError());
         FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
         if (P->opt.build_mixed) {
-            int st = check_fp32_range(L.Csr64, (size_t)NDIST * coax_size(p), l);
+            int st = check_fp32_range(P, L.Csr64, (size_t)NDIST * coax_size(p), l);
             if (st != FMM_OK) return st;
+        }
+        if (P->opt.build_mixed) {
             FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Csr32, sizeof(float2) * NDIST * coax_size(p)));
             to_float((const double *)L.Csr64, (float *)L.Csr32, (size_t)2 * NDIST * coax_size(p), P->stream);
         }
@@ -639,7 +655,11 @@ int gen_element_tables(Plan *P)
     int pb = pl + 1;
     int warps = 4;
     size_t shm = (size_t)basis_per_warp(pb) * warps * sizeof(double);
-    if (shm > 48 * 1024) FMM_CUDA_TRY(cudaFuncSetAttribute(element_tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    static size_t shm_set = 48 * 1024;
+    if (shm > 48 * 1024) {
+        int e = raise_smem_limit((const void *)element_tables_kernel, shm, &shm_set);
+        if (e) return e;
+    }
     int blocks = std::min((P->nf + warps - 1) / warps, 152 * 32);
     double2 bco = make_double2(P->opt.b_re, P->opt.b_im), cco = make_double2(P->opt.c_re, P->opt.c_im);
     element_tables_kernel<<<blocks, 32 * warps, shm, P->stream>>>(P->V_dev, P->F_dev, P->elem_leaf, ctr_dev, P->nf, pl,

@@ -52,7 +52,9 @@ typedef struct {
     double eps;               /* truncNum accuracy parameter (reference: 0.05) */
     int rule;                 /* regular quadrature rule (fmm_rule) */
     double a_re, a_im, b_re, b_im, c_re, c_im; /* operator a I + b L + c M */
-    int build_mixed;          /* also build the FP32 tables for FMM_MIXED */
+    int build_mixed;          /* also build the FP32 tables for FMM_MIXED (skipped, with the reason in
+                                 fmm_last_error of a mixed call, where orders exceed 42 or coaxial
+                                 entries exceed the FP32 range) */
     int device;               /* CUDA device ordinal */
 } fmm_options;
 
@@ -112,6 +114,20 @@ int fmm_gmres(fmm_plan *plan, const cuDoubleComplex *b, cuDoubleComplex *x, doub
  * column misses tol.  No counterpart in the reference, which solves nothing. */
 int fmm_solve_batched(fmm_plan *plan, const cuDoubleComplex *B, cuDoubleComplex *X, int nrhs, double tol, int maxit,
                       int restart, int precision, int *iters, double *relres);
+
+/* Solve n independent systems, one per plan (bodies of a scene, each with its own mesh,
+ * wavenumber and right-hand side), concurrently: nthreads host threads take plans from a
+ * shared queue and run fmm_gmres on them.  Every plan has its own streams, so the GPU
+ * overlaps the kernels of different bodies, which matters for small bodies whose kernels
+ * leave most of the GPU idle.  b[i] and x[i] (initial guess in, solution out) have the
+ * plan's nf entries, host or device.  iters, relres and status (FMM status per plan) may be
+ * NULL.  FMM_MIXED runs each plan in mixed precision where it has the mixed tables and in
+ * FP64 where plan creation could not build them (fmm_info.m2l_columns all zero then).
+ * Returns the first hard error, else FMM_ERR_NOT_CONVERGED if a system missed tol, else
+ * FMM_OK.  A plan may appear only once.  No counterpart in the reference. */
+int fmm_solve_many(fmm_plan *const *plans, int n, const cuDoubleComplex *const *b, cuDoubleComplex *const *x,
+                   double tol, int maxit, int restart, int precision, int nthreads, int *iters, double *relres,
+                   int *status);
 
 /* Reverse-mode derivative of a far-field objective with respect to the vertex positions.
  * x solves A x = b, b the plane wave exp(i k dir.c) at the centroids (dir NULL: b does not

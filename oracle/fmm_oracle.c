@@ -275,10 +275,17 @@ void orc_coax(double k, double t, int p, int sr, double *Cout)
                 cplx e2 = (n - 1 >= m) ? EE(m, np, n - 1) : 0.0;
                 EE(m, np, n + 1) = t0 * e0 - t1 * EE(m, np + 1, n) + t2 * e2;
             }
+    /* (R|R): entries with n' < n come from the exact coaxial symmetry (R|R)_{n'n} =
+     * (-1)^{n+n'} (R|R)_{nn'}.  The recurrence above (translation.cu:678-771) forms them by
+     * cancellation and loses them at small k t (1e13 relative error at kt = 0.05, p = 14,
+     * against a 60-digit run), which breaks L2L; its n' >= n side is accurate to 1e-15.
+     * This is a deliberate deviation from the reference; (S|R) is accurate throughout. */
     for (int m = 0; m < p; m++) {
         int off = coax_off(p, m);
         for (int np = m; np < p; np++)
-            for (int n = m; n < p; n++) C[off + (np - m) + (n - m) * (p - m)] = EE(m, np, n);
+            for (int n = m; n < p; n++)
+                C[off + (np - m) + (n - m) * (p - m)] =
+                    (!sr && np < n) ? (((n + np) & 1) ? -1.0 : 1.0) * EE(m, n, np) : EE(m, np, n);
     }
 #undef EE
     free(E); free(jn); free(yn);

@@ -172,6 +172,75 @@ def test_rcr_translation_addition_theorem(oracle, p, off, k, box):
     assert abs(loc - direct) < 1e-9 * abs(direct) + (1e-6 if p == 12 else 0)
 
 
+def _coax_rr_mp(x, p, dps=60):
+    """The coaxial (R|R) recurrence (translation.cu:678-771) in 60-digit arithmetic, entry
+    (m, n', n) -> value; exact enough to judge the FP64 tables in both triangles."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = dps
+
+    def aC(n, m):
+        return mp.sqrt(mp.mpf(n + 1 + m) * (n + 1 - m) / ((2 * n + 1) * (2 * n + 3))) if n >= abs(m) else mp.mpf(0)
+
+    def bC(n, m):
+        if 0 <= m <= n:
+            return mp.sqrt(mp.mpf(n - m - 1) * (n - m) / ((2 * n - 1) * (2 * n + 1)))
+        if -n <= m < 0:
+            return -mp.sqrt(mp.mpf(n - m - 1) * (n - m) / ((2 * n - 1) * (2 * n + 1)))
+        return mp.mpf(0)
+
+    x = mp.mpf(x)
+    E = {}
+    for q in range(2 * p - 1):
+        E[0, q, 0] = (-1) ** q * mp.sqrt(2 * q + 1) * mp.sqrt(mp.pi / (2 * x)) * mp.besselj(q + mp.mpf(1) / 2, x)
+    for m in range(p - 1):
+        for q in range(m + 1, 2 * p - 2 - m):
+            E[m + 1, q, m + 1] = (bC(q, -m - 1) * E[m, q - 1, m] - bC(q + 1, m) * E[m, q + 1, m]) / bC(m + 1, -m - 1)
+    for m in range(p - 1):
+        for n in range(m, p - 1):
+            for q in range(m, 2 * p - 2 - n):
+                e0 = E[m, q - 1, n] if q - 1 >= m else 0
+                e2 = E[m, q, n - 1] if n - 1 >= m else 0
+                E[m, q, n + 1] = (aC(q - 1, m) * e0 - aC(q, m) * E[m, q + 1, n] + aC(n - 1, m) * e2) / aC(n, m)
+    return E
+
+
+@pytest.mark.parametrize("kt", [2.0, 0.05])
+def test_rr_coaxial_tables_accurate_in_both_triangles(oracle, kt):
+    """(R|R) at small k t: the entries below the diagonal come from the exact symmetry
+    (R|R)_{n'n} = (-1)^{n+n'} (R|R)_{nn'}; the plain recurrence loses them (1e13 relative
+    error at kt = 0.05), which broke L2L at low frequency."""
+    p = 12
+    E = _coax_rr_mp(kt, p)
+    C = oracle.coax(kt, 1.0, p, False)
+    worst = 0.0
+    for m in range(p):
+        off = m * (2 * m * m - (3 + 6 * p) * m + 1 + 6 * (p + p * p)) // 6
+        for q in range(m, p):
+            for n in range(m, p):
+                ex = float(E[m, q, n])
+                worst = max(worst, abs(C[off + (q - m) + (n - m) * (p - m)].real - ex) / abs(ex))
+    assert worst < 1e-13
+
+
+@pytest.mark.parametrize("k", [20.0, 1.0, 0.2])
+def test_m2l_then_l2l_accurate_at_low_frequency(oracle, k):
+    """A point source's multipole, (S|R) to a well-separated box, then (R|R) to a child box,
+    evaluated at a target: equals G to 1e-9 down to k t = 0.009 (p = 14)."""
+    p, box = 14, 0.02
+    rng = np.random.default_rng(3)
+    cs, cd = np.zeros(3), np.array([2.0, 1.0, 0.0]) * box
+    y0 = rng.uniform(-0.4, 0.4, 3) * box
+    x = cd + rng.uniform(-0.4, 0.4, 3) * box
+    R = oracle.basis(p, k, y0 - cs)
+    C = np.array([1j * k * R[n * n + n - m] for n in range(p) for m in range(-n, n + 1)])
+    D = oracle.rcr(k, cd - cs, p, True, C)
+    cc = cd + 0.25 * box * np.array([1, -1, 1])
+    D2 = oracle.rcr(k, cc - cd, p, False, D)
+    r = np.linalg.norm(x - y0)
+    direct = np.exp(1j * k * r) / (4 * np.pi * r)
+    assert abs(np.sum(D2 * oracle.basis(p, k, x - cc)) - direct) < 1e-9 * abs(direct)
+
+
 def test_fmm_oracle_converges_to_dense(oracle):
     """FMM oracle vs the dense direct-quadrature operator on the 1280-triangle sphere."""
     V, F = meshes.roundtrip(*meshes.icosphere(3, 0.1))
