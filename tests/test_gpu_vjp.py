@@ -19,9 +19,9 @@ def generic_sphere(fm, subdiv):
     return V @ q.T + np.array([0.0123, -0.0071, 0.0045]), F
 
 
-def pipeline(fm, V, F, pts, depth, p):
-    plan = fm.Plan(V, F, k=K1, depth=depth, p_levels={l: p for l in range(2, depth + 1)}, rule=fm.RULE_DUNAVANT7,
-                   a=0.5, b=0.0, c=-1.0, build_mixed=False)
+def pipeline(fm, V, F, pts, depth, p, b=0.0, k=K1):
+    plan = fm.Plan(V, F, k=k, depth=depth, p_levels={l: p for l in range(2, depth + 1)}, rule=fm.RULE_DUNAVANT7,
+                   a=0.5, b=b, c=-1.0, build_mixed=False)
     b = plan.plane_wave(DIR)
     x, it, rr, ok = plan.gmres(b, tol=1e-13, restart=80, maxit=2000, precision=fm.FMM_FP64)
     assert ok
@@ -82,3 +82,29 @@ def test_vjp_against_dense_oracle_differences(fm, oracle):
             Vm[v, a] -= h
             fd = (J_dense(Vp) - J_dense(Vm)) / (2 * h)
             assert abs(grad[v, a] - fd) <= 1e-4 * scale, (v, a, grad[v, a], fd)
+
+
+def test_vjp_with_admittance_boundary(fm):
+    """An admittance (Robin) boundary beta = 0.1 + 0.05i on a bumped ellipsoid at 3 kHz: the
+    operator gains the single layer, b = i k beta, so the gradient's single-layer branches
+    (singular self terms, near G, the far phi J term) enter; against central differences."""
+    k = 2 * np.pi * 3000 / 343.0
+    b = 1j * k * (0.1 + 0.05j)
+    V, F = fm.ellipsoid(6, (0.075, 0.09, 0.11), lmax=8, sigma=1.5e-3, seed=1)
+    V = V + np.array([0.0031, -0.0017, 0.0023])  # off the centred cube's symmetry planes
+    pts = fm.fibonacci_sphere(32, 1.0)
+    plan, x, pf, J = pipeline(fm, V, F, pts, 3, 16, b=b, k=k)
+    assert plan.info.num_m2l[2] > 0
+    grad, _ = plan.vjp(x, pts, pf, direction=DIR, tol=1e-13)
+    plan.close()
+    rng = np.random.default_rng(12)
+    h = 1e-6
+    scale = np.abs(grad).max()
+    for v in rng.choice(len(V), 12, replace=False):
+        e = rng.standard_normal(3)
+        e /= np.linalg.norm(e)
+        Vp, Vm = V.copy(), V.copy()
+        Vp[v] += h * e
+        Vm[v] -= h * e
+        fd = (pipeline(fm, Vp, F, pts, 3, 16, b=b, k=k)[3] - pipeline(fm, Vm, F, pts, 3, 16, b=b, k=k)[3]) / (2 * h)
+        assert abs(grad[v] @ e - fd) <= 1e-4 * scale, (v, grad[v] @ e, fd)
