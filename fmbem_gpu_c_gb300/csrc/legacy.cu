@@ -1059,3 +1059,286 @@ extern "C" cuFloatComplex triElemIntegral_pGp1n_sgl(const float k, const cartCoo
 {
     return split_sgl(k, nod, pt, wgt, 1);
 }
+
+// ------------------------------------------------- integral.h: regular-basis moments, dG/dn_y,
+// d2G/dn_x dn_y, derivative coefficients.  Host routines like the reference's; arithmetic in
+// FP64 from the FP32 arguments, results rounded to FP32 once.
+namespace {
+
+inline double2 z2(double re, double im) { return make_double2(re, im); }
+inline double2 zscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+inline cuFloatComplex to_f(double2 a) { return make_cuFloatComplex((float)a.x, (float)a.y); }
+
+// R_n^m(v) = j_n(k |v|) Q_n^{|m|}(cos theta) e^{i m phi}, n < P, index n^2 + n + m: the regular
+// basis of rglBasis (translation.cu:171-178) with the reference's spherical harmonics
+void regular_basis(int P, double k, const double v[3], std::vector<double2> &R)
+{
+    R.assign((size_t)P * P, z2(0.0, 0.0));
+    if (P <= 0) return;
+    double r = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (r == 0.0) {
+        R[0].x = 0.28209479177387814;
+        return;
+    }
+    std::vector<double> jn(P), Q((size_t)P * (P + 1) / 2);
+    sph_jn_array(P, k * r, jn.data());
+    legendre_Q(P, v[2] / r, Q.data());
+    double phi = atan2(v[1], v[0]);
+    for (int n = 0; n < P; n++)
+        for (int m = 0; m <= n; m++) {
+            double a = jn[n] * Q[n * (n + 1) / 2 + m], c = cos(m * phi), s = sin(m * phi);
+            R[nm_idx(n, m)] = z2(a * c, a * s);
+            R[nm_idx(n, -m)] = z2(a * c, -a * s);
+        }
+}
+
+inline double2 basis_at(const std::vector<double2> &R, int n, int m)
+{
+    if (n < 0 || m > n || -m > n) return z2(0.0, 0.0);
+    return R[nm_idx(n, m)];
+}
+
+// d R_n^m / dn from the basis of orders up to n+1 (G&D differentiation relations):
+//   k/2 (n_x - i n_y) [b_{n+1}^{-m-1} R_{n+1}^{m+1} - b_n^m R_{n-1}^{m+1}]
+// + k/2 (n_x + i n_y) [b_{n+1}^{m-1} R_{n+1}^{m-1} - b_n^{-m} R_{n-1}^{m-1}]
+// + k n_z [a_{n-1}^m R_{n-1}^m - a_n^m R_{n+1}^m]
+double2 dirdev(double k, int n, int m, const double nr[3], const std::vector<double2> &R)
+{
+    double2 t0 = csub(zscale(basis_at(R, n + 1, m + 1), coefB(n + 1, -m - 1)), zscale(basis_at(R, n - 1, m + 1), coefB(n, m)));
+    double2 t1 = csub(zscale(basis_at(R, n + 1, m - 1), coefB(n + 1, m - 1)), zscale(basis_at(R, n - 1, m - 1), coefB(n, -m)));
+    double2 t2 = csub(zscale(basis_at(R, n - 1, m), coefA(n - 1, m)), zscale(basis_at(R, n + 1, m), coefA(n, m)));
+    double2 r = cmul(z2(0.5 * k * nr[0], -0.5 * k * nr[1]), t0);
+    r = cadd(r, cmul(z2(0.5 * k * nr[0], 0.5 * k * nr[1]), t1));
+    return cadd(r, zscale(t2, k * nr[2]));
+}
+
+struct Tri {
+    double v[3][3];   // nodes
+    double nrml[3];   // (v0 - v2) x (v1 - v2)
+    double J, nh[3];  // |nrml| and the unit normal
+    explicit Tri(const cartCoord nod[3])
+    {
+        for (int i = 0; i < 3; i++) { v[i][0] = nod[i].x; v[i][1] = nod[i].y; v[i][2] = nod[i].z; }
+        init();
+    }
+    Tri(const double a[3], const double b[3], const double c[3])
+    {
+        for (int t = 0; t < 3; t++) { v[0][t] = a[t]; v[1][t] = b[t]; v[2][t] = c[t]; }
+        init();
+    }
+    void init()
+    {
+        double e0[3], e1[3];
+        for (int t = 0; t < 3; t++) { e0[t] = v[0][t] - v[2][t]; e1[t] = v[1][t] - v[2][t]; }
+        nrml[0] = e0[1] * e1[2] - e0[2] * e1[1];
+        nrml[1] = e0[2] * e1[0] - e0[0] * e1[2];
+        nrml[2] = e0[0] * e1[1] - e0[1] * e1[0];
+        J = sqrt(nrml[0] * nrml[0] + nrml[1] * nrml[1] + nrml[2] * nrml[2]);
+        for (int t = 0; t < 3; t++) nh[t] = nrml[t] / J;
+    }
+    void centroid(double c[3]) const
+    {
+        for (int t = 0; t < 3; t++) c[t] = v[0][t] + (2.0 / 3.0) * (0.5 * (v[1][t] + v[2][t]) - v[0][t]);
+    }
+};
+
+// The collapsed Gauss rule of integral.cu:80-109 over a triangle whose singular vertex (if any)
+// is v2: theta = (1 + pt_i)/2, rho = (1 + pt_j)/2, x = rho(1-theta) v0 + rho theta v1 + (1-rho) v2,
+// weight wgt_i wgt_j rho J / 4.  visit(x, w) is called for every point.
+template <class F> void collapsed_points(const Tri &T, const float *pt, const float *wgt, F visit)
+{
+    for (int i = 0; i < INTORDER; i++) {
+        double theta = 0.5 + 0.5 * (double)pt[i];
+        for (int j = 0; j < INTORDER; j++) {
+            double rho = 0.5 + 0.5 * (double)pt[j], w = 0.25 * (double)wgt[i] * (double)wgt[j] * rho * T.J;
+            double xi1 = rho * (1.0 - theta), xi2 = rho * theta, xi3 = 1.0 - rho, x[3];
+            for (int t = 0; t < 3; t++) x[t] = xi1 * T.v[0][t] + xi2 * T.v[1][t] + xi3 * T.v[2][t];
+            visit(x, w);
+        }
+    }
+}
+
+template <class K> double2 collapsed_d(const Tri &T, const float *pt, const float *wgt, K kern)
+{
+    double2 acc = z2(0.0, 0.0);
+    collapsed_points(T, pt, wgt, [&](const double *x, double w) { acc = cadd(acc, zscale(kern(x), w)); });
+    return acc;
+}
+
+// dG(x, y)/dn_y = G (ik - 1/r) (y - x).n / r   (pGp2n, integral.cu:400-413)
+double2 dgreen_dny(double k, const double x[3], const double y[3], const double n[3])
+{
+    double d[3] = {y[0] - x[0], y[1] - x[1], y[2] - x[2]};
+    double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    double s = 1.0 / (4.0 * FMM_PI * r), dn = (d[0] * n[0] + d[1] * n[1] + d[2] * n[2]) / r;
+    double2 g = z2(cos(k * r) * s, sin(k * r) * s);
+    return zscale(cmul(g, z2(-1.0 / r, k)), dn);
+}
+
+// d2G(x, y)/dn_x dn_y = e^{ikr}/(4 pi r^3) [(3 - 3ikr - k^2 r^2) ((x-y).n1/r) ((y-x).n2/r)
+//                                          + (1 - ikr) n1.n2]      (p2Gp1np2n, integral.cu:603-622)
+double2 d2green(double k, const double n1[3], const double n2[3], const double x[3], const double y[3])
+{
+    double d[3] = {x[0] - y[0], x[1] - y[1], x[2] - y[2]};
+    double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    double a1 = (d[0] * n1[0] + d[1] * n1[1] + d[2] * n1[2]) / r;
+    double a2 = -(d[0] * n2[0] + d[1] * n2[1] + d[2] * n2[2]) / r;
+    double n12 = n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2];
+    double s = 1.0 / (4.0 * FMM_PI * r * r * r), kr = k * r;
+    double2 e = z2(cos(kr) * s, sin(kr) * s);
+    double2 br = cadd(zscale(z2(3.0 - kr * kr, -3.0 * kr), a1 * a2), zscale(z2(1.0, -kr), n12));
+    return cmul(e, br);
+}
+
+// Distance from the centroid to the triangle's boundary along the in-plane direction at angle
+// theta (theta2rho, integral.cu:668-736).  The frame is the reference's: node 0 on the polar
+// axis, node 1 at the angle 0c1 (in [0, pi]), node 2 at 0c1 + 1c2, all from the side lengths;
+// below 0c1 the ray meets edge 01, below 0c1 + 1c2 edge 12, else edge 20.
+double centroid_ray(const Tri &T, double theta)
+{
+    double c[3], dc[3], de[3];
+    T.centroid(c);
+    auto dist = [](const double *a, const double *b) {
+        return sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
+    };
+    for (int i = 0; i < 3; i++) { dc[i] = dist(T.v[i], c); de[i] = dist(T.v[i], T.v[(i + 1) % 3]); }
+    double a01 = acos((dc[0] * dc[0] + dc[1] * dc[1] - de[0] * de[0]) / (2.0 * dc[0] * dc[1]));
+    double a02 = a01 + acos((dc[1] * dc[1] + dc[2] * dc[2] - de[1] * de[1]) / (2.0 * dc[1] * dc[2]));
+    double P[3][2] = {{dc[0], 0.0}, {dc[1] * cos(a01), dc[1] * sin(a01)}, {dc[2] * cos(a02), dc[2] * sin(a02)}};
+    int e = theta < a01 ? 0 : (theta < a02 ? 1 : 2);
+    const double *A = P[e], *B = P[(e + 1) % 3];
+    double u0 = cos(theta), u1 = sin(theta), v0 = B[0] - A[0], v1 = B[1] - A[1];
+    // the ray t u meets the edge A + s (B - A) at t = (A x (B - A)) / (u x (B - A))
+    return fabs((A[0] * v1 - A[1] * v0) / (u0 * v1 - u1 * v0));
+}
+
+} // namespace
+
+extern "C" cuFloatComplex triElemIntegral_R(const float wavNum, const cartCoord nod[3], const int n, const int m,
+                                             const cartCoord x_lp, const float *pt, const float *wgt)
+{
+    Tri T(nod);
+    const double c[3] = {x_lp.x, x_lp.y, x_lp.z};
+    std::vector<double2> R;
+    if (n < 0) return make_cuFloatComplex(0.0f, 0.0f);
+    return to_f(collapsed_d(T, pt, wgt, [&](const double *x) {
+        double v[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+        regular_basis(n + 1, wavNum, v, R);
+        return basis_at(R, n, m);
+    }));
+}
+
+extern "C" cuFloatComplex dirDev_R(const float wavNum, const int n, const int m, const cartCoord nrml, const cartCoord x)
+{
+    if (n < 0) return make_cuFloatComplex(0.0f, 0.0f);
+    const double v[3] = {x.x, x.y, x.z}, nr[3] = {nrml.x, nrml.y, nrml.z};
+    std::vector<double2> R;
+    regular_basis(n + 2, wavNum, v, R);
+    return to_f(dirdev(wavNum, n, m, nr, R));
+}
+
+extern "C" cuFloatComplex triElemIntegral_pRpn(const float wavNum, const cartCoord nod[3], const int n, const int m,
+                                                const cartCoord x_lp, const float *pt, const float *wgt)
+{
+    Tri T(nod);
+    const double c[3] = {x_lp.x, x_lp.y, x_lp.z};
+    std::vector<double2> R;
+    if (n < 0) return make_cuFloatComplex(0.0f, 0.0f);
+    return to_f(collapsed_d(T, pt, wgt, [&](const double *x) {
+        double v[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+        regular_basis(n + 2, wavNum, v, R);
+        return dirdev(wavNum, n, m, T.nh, R);
+    }));
+}
+
+extern "C" cuFloatComplex triElemIntegral_pGp2n_nsgl(const float wavNum, const cartCoord nod[3], const cartCoord nrml,
+                                                      const cartCoord y, const float *pt, const float *wgt)
+{
+    Tri T(nod);
+    const double yy[3] = {y.x, y.y, y.z}, nr[3] = {nrml.x, nrml.y, nrml.z};
+    return to_f(collapsed_d(T, pt, wgt, [&](const double *x) { return dgreen_dny(wavNum, x, yy, nr); }));
+}
+
+extern "C" cuFloatComplex triElemIntegral_pGp2n_sgl(const float wavNum, const cartCoord nod[3], const float *pt, const float *wgt)
+{
+    // centroid split (integral.cu:539-601): three sub-triangles with the centroid as the
+    // singular vertex, each integrated with its own unit normal at y = centroid
+    Tri T(nod);
+    double c[3];
+    T.centroid(c);
+    double2 acc = z2(0.0, 0.0);
+    for (int s = 0; s < 3; s++) {
+        Tri S(T.v[s], T.v[(s + 1) % 3], c);
+        acc = cadd(acc, collapsed_d(S, pt, wgt, [&](const double *x) { return dgreen_dny(wavNum, x, c, S.nh); }));
+    }
+    return to_f(acc);
+}
+
+extern "C" cuFloatComplex triElemIntegral_p2Gp1np2n_nsgl(const float wavNum, const cartCoord nod[3], const cartCoord nrml_y,
+                                                          const cartCoord y, const float *pt, const float *wgt)
+{
+    Tri T(nod);
+    const double yy[3] = {y.x, y.y, y.z}, nr[3] = {nrml_y.x, nrml_y.y, nrml_y.z};
+    return to_f(collapsed_d(T, pt, wgt, [&](const double *x) { return d2green(wavNum, T.nh, nr, x, yy); }));
+}
+
+extern "C" cuFloatComplex triElemIntegral_p2Gp1np2n_sgl(const float wavNum, const cartCoord nod[3], const float *pt, const float *wgt)
+{
+    // Hadamard finite part of int_T d2G/dn_x dn_y at the centroid of the flat element
+    // (integral.cu:738-751): the kernel is e^{ikr}(1 - ikr)/(4 pi r^3) = d/dr[-e^{ikr}/r]/(4 pi r),
+    // so in polar coordinates about the centroid
+    //   FP = -1/(4 pi) [ int_0^{2 pi} e^{ik rho(theta)}/rho(theta) dtheta - 2 pi i k ],
+    // the angle integral by the caller's Gauss rule mapped to theta = pi s + pi.
+    Tri T(nod);
+    double2 sum = z2(0.0, 0.0);
+    for (int i = 0; i < INTORDER; i++) {
+        double rho = centroid_ray(T, FMM_PI * (double)pt[i] + FMM_PI), w = (double)wgt[i] / rho;
+        sum = cadd(sum, z2(w * cos(wavNum * rho), w * sin(wavNum * rho)));
+    }
+    sum = csub(zscale(sum, FMM_PI), z2(0.0, 2.0 * FMM_PI * wavNum));
+    return to_f(zscale(sum, -1.0 / (4.0 * FMM_PI)));
+}
+
+extern "C" void cmptDiffCoeff(const float wavNum, const cuFloatComplex *coeff, const int p, const cartCoord nrml,
+                              cuFloatComplex *coeff_n)
+{
+    // coefficients of d/dn sum_{n<=p} c_n^m R_n^m on R_n^m, n < p: the relations of dirDev_R
+    // collected by output index (integral.cu:753-823, whose temporaries 3-5 are never
+    // assigned; this is the sum that code sets out to form).  coeff holds (p+1)^2 entries.
+    const double k = wavNum, nr[3] = {nrml.x, nrml.y, nrml.z};
+    auto c = [&](int n, int m) {
+        if (n < 0 || m > n || -m > n) return z2(0.0, 0.0);
+        cuFloatComplex v = coeff[nm_idx(n, m)];
+        return z2(cuCrealf(v), cuCimagf(v));
+    };
+    for (int n = 0; n < p; n++)
+        for (int m = -n; m <= n; m++) {
+            double2 t0 = csub(zscale(c(n - 1, m - 1), coefB(n, -m)), zscale(c(n + 1, m - 1), coefB(n + 1, m - 1)));
+            double2 t1 = csub(zscale(c(n - 1, m + 1), coefB(n, m)), zscale(c(n + 1, m + 1), coefB(n + 1, -m - 1)));
+            double2 t2 = csub(zscale(c(n + 1, m), coefA(n, m)), zscale(c(n - 1, m), coefA(n - 1, m)));
+            double2 r = cmul(z2(0.5 * k * nr[0], -0.5 * k * nr[1]), t0);
+            r = cadd(r, cmul(z2(0.5 * k * nr[0], 0.5 * k * nr[1]), t1));
+            coeff_n[nm_idx(n, m)] = to_f(cadd(r, zscale(t2, k * nr[2])));
+        }
+}
+
+extern "C" void bottomLevelCoeff_L(const float wavNum, const triElem elem, const cuFloatComplex q, const cartCoord *pt,
+                                   const cartCoord x_lp, const float *intPt, const float *intWgt, cuFloatComplex *coeff,
+                                   const int p)
+{
+    // multipole coefficients of the single layer of density q on one element about x_lp:
+    // coeff[n, m] = i k q int R_n^{-m}(x - x_lp) dS, n < p (integral.cu:825-840, whose inner
+    // loop tests n <= n; this is the loop over m = -n..n it stands for)
+    cartCoord nod[3] = {pt[elem.node[0]], pt[elem.node[1]], pt[elem.node[2]]};
+    Tri T(nod);
+    const double c[3] = {x_lp.x, x_lp.y, x_lp.z};
+    std::vector<double2> acc((size_t)p * p, z2(0.0, 0.0)), R;
+    collapsed_points(T, intPt, intWgt, [&](const double *x, double w) {
+        double v[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+        regular_basis(p, wavNum, v, R);
+        for (int n = 0; n < p; n++)
+            for (int m = -n; m <= n; m++) acc[nm_idx(n, m)] = cadd(acc[nm_idx(n, m)], zscale(R[nm_idx(n, -m)], w));
+    });
+    const double2 ikq = cmul(z2(0.0, (double)wavNum), z2(cuCrealf(q), cuCimagf(q)));
+    for (int i = 0; i < p * p; i++) coeff[i] = to_f(cmul(ikq, acc[i]));
+}

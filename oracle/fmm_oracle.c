@@ -537,6 +537,147 @@ void orc_elem_R(double k, const double *nod, const double *c, int p, int rule, i
     free(Rb);
 }
 
+/* directional derivative of R_n^m(x) along nrml (dirDev_R, integral.cu:284-331) */
+void orc_dirdev_R(double k, int n, int m, const double *nrml, const double *x, double *out)
+{
+    cplx *Rb = (cplx *)malloc(sizeof(cplx) * (n + 2) * (n + 2));
+    basis_generic(n + 2, k, x, Rb, 0);
+    cplx z = dirdev_R(k, n, m, nrml, Rb);
+    free(Rb);
+    out[0] = creal(z); out[1] = cimag(z);
+}
+
+/* dG(x, y)/dn_y (pGp2n, integral.cu:400-413): G (ik - 1/r) (y - x).n / r */
+static inline cplx dgreen_y(double k, const double *x, const double *y, const double *n)
+{
+    double d[3] = {y[0] - x[0], y[1] - x[1], y[2] - x[2]};
+    double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    cplx g = (cos(k * r) + I * sin(k * r)) / (4.0 * PI_D * r);
+    return g * (I * k - 1.0 / r) * (d[0] * n[0] + d[1] * n[1] + d[2] * n[2]) / r;
+}
+
+/* d2G(x, y)/dn_x dn_y (p2Gp1np2n, integral.cu:603-622):
+ * e^{ikr}/(4 pi r^3) [(3 - 3ikr - k^2 r^2) ((x-y).n1/r) ((y-x).n2/r) + (1 - ikr) n1.n2] */
+static inline cplx hyper_kernel(double k, const double *n1, const double *n2, const double *x, const double *y)
+{
+    double d[3] = {x[0] - y[0], x[1] - y[1], x[2] - y[2]};
+    double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    double a1 = (d[0] * n1[0] + d[1] * n1[1] + d[2] * n1[2]) / r;
+    double a2 = -(d[0] * n2[0] + d[1] * n2[1] + d[2] * n2[2]) / r;
+    double n12 = n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2];
+    cplx e = (cos(k * r) + I * sin(k * r)) / (4.0 * PI_D * r * r * r);
+    return e * ((3.0 - k * k * r * r - 3.0 * I * k * r) * a1 * a2 + (1.0 - I * k * r) * n12);
+}
+
+/* int_T dG/dn_y dS_x with the collapsed rule: regular (triElemIntegral_pGp2n_nsgl,
+ * integral.cu:509-537; the caller's normal at y) or self term (triElemIntegral_pGp2n_sgl,
+ * integral.cu:539-601: centroid split, each sub-triangle's own normal, y = centroid) */
+void orc_elem_dGdny(double k, const double *nod9, const double *nrml, const double *y, int sgl, double *out)
+{
+    double bary[64 * 3], w[64];
+    int nq = collapsed_rule(3, bary, w);
+    cplx acc = 0.0;
+    if (!sgl) {
+        double nn[3], J;
+        tri_normal(nod9, nn, &J);
+        for (int q = 0; q < nq; q++) {
+            double x[3];
+            tri_point(nod9, bary + 3 * q, x);
+            acc += w[q] * J * dgreen_y(k, x, y, nrml);
+        }
+    } else {
+        double c[3];
+        tri_centroid(nod9, c);
+        for (int s = 0; s < 3; s++) {
+            double sub[9], nn[3], J;
+            const double *a = nod9 + 3 * s, *b = nod9 + 3 * ((s + 1) % 3);
+            for (int t = 0; t < 3; t++) { sub[t] = a[t]; sub[3 + t] = b[t]; sub[6 + t] = c[t]; }
+            tri_normal(sub, nn, &J);
+            double nh[3] = {nn[0] / J, nn[1] / J, nn[2] / J};
+            for (int q = 0; q < nq; q++) {
+                double x[3];
+                tri_point(sub, bary + 3 * q, x);
+                acc += w[q] * J * dgreen_y(k, x, c, nh);
+            }
+        }
+    }
+    out[0] = creal(acc); out[1] = cimag(acc);
+}
+
+/* distance from the centroid to the boundary of the triangle along the in-plane direction at
+ * angle theta (theta2rho, integral.cu:668-736): node 1 on the polar axis, node 2 at the
+ * positive angle 1c2, node 3 at 1c2 + 2c3; the ray meets edge 12, 23 or 31 */
+static double centroid_ray(const double *nod9, double theta)
+{
+    double c[3], dc[3], de[3];
+    tri_centroid(nod9, c);
+    for (int i = 0; i < 3; i++) {
+        const double *a = nod9 + 3 * i, *b = nod9 + 3 * ((i + 1) % 3);
+        dc[i] = sqrt((a[0] - c[0]) * (a[0] - c[0]) + (a[1] - c[1]) * (a[1] - c[1]) + (a[2] - c[2]) * (a[2] - c[2]));
+        de[i] = sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
+    }
+    double th2 = acos((dc[0] * dc[0] + dc[1] * dc[1] - de[0] * de[0]) / (2.0 * dc[0] * dc[1]));
+    double th3 = th2 + acos((dc[1] * dc[1] + dc[2] * dc[2] - de[1] * de[1]) / (2.0 * dc[1] * dc[2]));
+    double P[3][2] = {{dc[0], 0.0}, {dc[1] * cos(th2), dc[1] * sin(th2)}, {dc[2] * cos(th3), dc[2] * sin(th3)}};
+    int e = theta < th2 ? 0 : (theta < th3 ? 1 : 2);
+    const double *A = P[e], *B = P[(e + 1) % 3];
+    double u[2] = {cos(theta), sin(theta)}, v[2] = {B[0] - A[0], B[1] - A[1]};
+    /* t u = A + s v  =>  t = (A x v) / (u x v) */
+    double t = (A[0] * v[1] - A[1] * v[0]) / (u[0] * v[1] - u[1] * v[0]);
+    return fabs(t);
+}
+
+/* int_T d2G/dn_x dn_y dS_x: regular (triElemIntegral_p2Gp1np2n_nsgl, integral.cu:624-660;
+ * n_x the element's unit normal, n_y the caller's) or the finite part at the centroid of the
+ * flat element (triElemIntegral_p2Gp1np2n_sgl, integral.cu:738-751):
+ *   -1/(4 pi) [ int_0^{2 pi} e^{ik rho(theta)} / rho(theta) dtheta - 2 pi i k ]
+ * with an nth-point Gauss rule in theta (the reference uses its 3-point rule). */
+void orc_elem_hyper(double k, const double *nod9, const double *nrml, const double *y, int sgl, int nth, double *out)
+{
+    cplx acc = 0.0;
+    if (!sgl) {
+        double bary[64 * 3], w[64], nn[3], J;
+        int nq = collapsed_rule(3, bary, w);
+        tri_normal(nod9, nn, &J);
+        double nh[3] = {nn[0] / J, nn[1] / J, nn[2] / J};
+        for (int q = 0; q < nq; q++) {
+            double x[3];
+            tri_point(nod9, bary + 3 * q, x);
+            acc += w[q] * J * hyper_kernel(k, nh, nrml, x, y);
+        }
+    } else {
+        double *s = (double *)malloc(sizeof(double) * 2 * nth), *ws = s + nth;
+        orc_gauss_legendre(nth, s, ws);
+        cplx sum = 0.0;
+        for (int i = 0; i < nth; i++) {
+            double rho = centroid_ray(nod9, PI_D * s[i] + PI_D);
+            sum += ws[i] * (cos(k * rho) + I * sin(k * rho)) / rho;
+        }
+        free(s);
+        acc = -(PI_D * sum - 2.0 * PI_D * I * k) / (4.0 * PI_D);
+    }
+    out[0] = creal(acc); out[1] = cimag(acc);
+}
+
+/* coefficients of the normal derivative of a regular expansion (cmptDiffCoeff,
+ * integral.cu:753-823): d/dn sum_{n<=p} c_n^m R_n^m = sum_{n<p} c'_n^m R_n^m + (orders >= p),
+ * from the G&D recurrences of dirDev_R collected by output index; coeff holds (p+1)^2
+ * entries (orders 0..p), coeff_n p^2. */
+void orc_diff_coeff(double k, const double *coeffp, int p, const double *nrml, double *outp)
+{
+    const cplx *c = (const cplx *)coeffp;
+    cplx *o = (cplx *)outp;
+#define CF(nn, mm) (((nn) < 0 || abs(mm) > (nn)) ? (cplx)0.0 : c[NM(nn, mm)])
+    for (int n = 0; n < p; n++)
+        for (int m = -n; m <= n; m++) {
+            cplx t0 = orc_bC(n, -m) * CF(n - 1, m - 1) - orc_bC(n + 1, m - 1) * CF(n + 1, m - 1);
+            cplx t1 = orc_bC(n, m) * CF(n - 1, m + 1) - orc_bC(n + 1, -m - 1) * CF(n + 1, m + 1);
+            cplx t2 = orc_aC(n, m) * CF(n + 1, m) - orc_aC(n - 1, m) * CF(n - 1, m);
+            o[NM(n, m)] = 0.5 * k * (nrml[0] - I * nrml[1]) * t0 + 0.5 * k * (nrml[0] + I * nrml[1]) * t1 + k * nrml[2] * t2;
+        }
+#undef CF
+}
+
 /* ------------------------------------------------------------------ FMM */
 typedef struct {
     int nb, p;

@@ -37,6 +37,10 @@ void orc_gauss_legendre(int n, double *x, double *w);
 void orc_elem_G(double k, const double *nod9, const double *y, int rule, int sgl, double *out);
 void orc_elem_dG(double k, const double *nod9, const double *y, int rule, int sgl, double *out);
 void orc_elem_R(double k, const double *nod9, const double *c, int p, int rule, int deriv, double *out);
+void orc_dirdev_R(double k, int n, int m, const double *nrml, const double *x, double *out);
+void orc_elem_dGdny(double k, const double *nod9, const double *nrml, const double *y, int sgl, double *out);
+void orc_elem_hyper(double k, const double *nod9, const double *nrml, const double *y, int sgl, int nth, double *out);
+void orc_diff_coeff(double k, const double *coeff, int p, const double *nrml, double *out);
 
 /* FMM operator  y = a x + b L x + c M x  on collocation points at triangle centroids */
 typedef struct orc_fmm orc_fmm;

@@ -52,6 +52,10 @@ def lib():
         L.orc_elem_G.argtypes = [ctypes.c_double, c_dp, c_dp, ctypes.c_int, ctypes.c_int, c_dp]
         L.orc_elem_dG.argtypes = [ctypes.c_double, c_dp, c_dp, ctypes.c_int, ctypes.c_int, c_dp]
         L.orc_elem_R.argtypes = [ctypes.c_double, c_dp, c_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_dp]
+        L.orc_dirdev_R.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int, c_dp, c_dp, c_dp]
+        L.orc_elem_dGdny.argtypes = [ctypes.c_double, c_dp, c_dp, c_dp, ctypes.c_int, c_dp]
+        L.orc_elem_hyper.argtypes = [ctypes.c_double, c_dp, c_dp, c_dp, ctypes.c_int, ctypes.c_int, c_dp]
+        L.orc_diff_coeff.argtypes = [ctypes.c_double, c_dp, ctypes.c_int, c_dp, c_dp]
         L.orc_rule.argtypes = [ctypes.c_int, c_dp, c_dp]
         L.orc_rule.restype = ctypes.c_int
         L.orc_rot_size.restype = ctypes.c_int
@@ -135,6 +139,47 @@ def elem_moments(k, nod, c, p, rule=0, deriv=False):
     c = np.ascontiguousarray(c, dtype=np.float64)
     out = np.zeros(p * p, dtype=np.complex128)
     lib().orc_elem_R(k, _d(nod), _d(c), p, rule, 1 if deriv else 0, _d(out.view(np.float64)))
+    return out
+
+
+def dirdev_R(k, n, m, nrml, x):
+    """Directional derivative of R_n^m at x along nrml (``dirDev_R``, integral.cu:284-331)."""
+    out = np.zeros(2)
+    lib().orc_dirdev_R(k, n, m, _d(np.ascontiguousarray(nrml, dtype=np.float64)),
+                       _d(np.ascontiguousarray(x, dtype=np.float64)), _d(out))
+    return complex(out[0], out[1])
+
+
+def elem_dGdny(k, nod, nrml=None, y=None, sgl=False):
+    """int_T dG/dn_y dS_x (``triElemIntegral_pGp2n_nsgl`` / ``_sgl``, integral.cu:509-601)."""
+    nod = np.ascontiguousarray(nod, dtype=np.float64).reshape(9)
+    nrml = np.zeros(3) if nrml is None else np.ascontiguousarray(nrml, dtype=np.float64)
+    y = np.zeros(3) if y is None else np.ascontiguousarray(y, dtype=np.float64)
+    out = np.zeros(2)
+    lib().orc_elem_dGdny(k, _d(nod), _d(nrml), _d(y), 1 if sgl else 0, _d(out))
+    return complex(out[0], out[1])
+
+
+def elem_hyper(k, nod, nrml=None, y=None, sgl=False, nth=3):
+    """int_T d2G/dn_x dn_y dS_x (``triElemIntegral_p2Gp1np2n_nsgl`` / ``_sgl``,
+    integral.cu:624-660, 738-751); the self term is the finite part with an nth-point rule
+    in the polar angle."""
+    nod = np.ascontiguousarray(nod, dtype=np.float64).reshape(9)
+    nrml = np.zeros(3) if nrml is None else np.ascontiguousarray(nrml, dtype=np.float64)
+    y = np.zeros(3) if y is None else np.ascontiguousarray(y, dtype=np.float64)
+    out = np.zeros(2)
+    lib().orc_elem_hyper(k, _d(nod), _d(nrml), _d(y), 1 if sgl else 0, nth, _d(out))
+    return complex(out[0], out[1])
+
+
+def diff_coeff(k, coeff, p, nrml):
+    """Coefficients of the normal derivative of sum_{n<=p} c_n^m R_n^m (``cmptDiffCoeff``,
+    integral.cu:753-823); coeff holds (p+1)^2 entries."""
+    c = np.ascontiguousarray(coeff, dtype=np.complex128)
+    assert c.size >= (p + 1) ** 2
+    out = np.zeros(p * p, dtype=np.complex128)
+    lib().orc_diff_coeff(k, _d(c.view(np.float64)), p, _d(np.ascontiguousarray(nrml, dtype=np.float64)),
+                         _d(out.view(np.float64)))
     return out
 
 

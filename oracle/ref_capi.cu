@@ -294,3 +294,31 @@ extern "C" void ref_elem_R(float k, const float *nod9, int n, int m, const float
     cuFloatComplex z = deriv ? triElemIntegral_pRpn(k, nod, n, m, c, pt, wgt) : triElemIntegral_R(k, nod, n, m, c, pt, wgt);
     out[0] = cuCrealf(z); out[1] = cuCimagf(z);
 }
+/* directional derivative of R_n^m along nrml at x (dirDev_R, integral.cu:284-331) */
+extern "C" void ref_dirdev_R(float k, int n, int m, const float *nrml3, const float *x3, float *out)
+{
+    cartCoord nr = {nrml3[0], nrml3[1], nrml3[2]}, x = {x3[0], x3[1], x3[2]};
+    cuFloatComplex z = dirDev_R(k, n, m, nr, x);
+    out[0] = cuCrealf(z); out[1] = cuCimagf(z);
+}
+/* element integrals of dG/dn_y (triElemIntegral_pGp2n_nsgl / _sgl, integral.cu:509-601) and of
+ * d2G/dn_x dn_y (triElemIntegral_p2Gp1np2n_nsgl / _sgl, integral.cu:624-660, 738-751) */
+extern "C" void ref_elem_dGdny(float k, const float *nod9, const float *nrml3, const float *y3, int sgl, float *out)
+{
+    float pt[INTORDER], wgt[INTORDER];
+    genGaussParams(INTORDER, pt, wgt);
+    cartCoord nod[3] = {{nod9[0], nod9[1], nod9[2]}, {nod9[3], nod9[4], nod9[5]}, {nod9[6], nod9[7], nod9[8]}};
+    cartCoord nr = {nrml3[0], nrml3[1], nrml3[2]}, y = {y3[0], y3[1], y3[2]};
+    cuFloatComplex z = sgl ? triElemIntegral_pGp2n_sgl(k, nod, pt, wgt) : triElemIntegral_pGp2n_nsgl(k, nod, nr, y, pt, wgt);
+    out[0] = cuCrealf(z); out[1] = cuCimagf(z);
+}
+extern "C" void ref_elem_hyper(float k, const float *nod9, const float *nrml3, const float *y3, int sgl, float *out)
+{
+    float pt[INTORDER], wgt[INTORDER];
+    genGaussParams(INTORDER, pt, wgt);
+    cartCoord nod[3] = {{nod9[0], nod9[1], nod9[2]}, {nod9[3], nod9[4], nod9[5]}, {nod9[6], nod9[7], nod9[8]}};
+    cartCoord nr = {nrml3[0], nrml3[1], nrml3[2]}, y = {y3[0], y3[1], y3[2]};
+    cuFloatComplex z = sgl ? triElemIntegral_p2Gp1np2n_sgl(k, nod, pt, wgt)
+                           : triElemIntegral_p2Gp1np2n_nsgl(k, nod, nr, y, pt, wgt);
+    out[0] = cuCrealf(z); out[1] = cuCimagf(z);
+}

@@ -13,6 +13,9 @@ fixtures here are its outputs on inputs this project generates:
 * quadrature fixtures: element integrals of G and dG/dn (regular and singular) and the
   P2M moments triElemIntegral_R / triElemIntegral_pRpn on fixed triangles.
 * truncNum values.
+* extended integral fixtures: dirDev_R at fixed points, the element integrals of dG/dn_y
+  (triElemIntegral_pGp2n_*) and of d2G/dn_x dn_y (triElemIntegral_p2Gp1np2n_*), regular and
+  singular.
 
 Usage:  python tests/golden/make_golden.py   (needs oracle/build_ref.sh to have run)
 """
@@ -63,6 +66,11 @@ def load_ref():
         getattr(L, f).argtypes = [ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     L.ref_elem_R.argtypes = [ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                              ctypes.c_void_p]
+    L.ref_dirdev_R.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                               ctypes.c_void_p]
+    for f in ("ref_elem_dGdny", "ref_elem_hyper"):
+        getattr(L, f).argtypes = [ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                  ctypes.c_void_p]
     return L
 
 
@@ -184,6 +192,40 @@ def quadrature(L):
     np.savez_compressed(os.path.join(HERE, "quadrature.npz"), **res)
 
 
+def integral_ext(L):
+    q = np.load(os.path.join(HERE, "quadrature.npz"))
+    tris = np.concatenate([q["tris"], np.array([[0.0, 0.0, 0.0, 0.2, 0.01, 0.03, 0.05, 0.13, -0.02]], np.float32)])
+    ys = np.concatenate([q["ys"], np.array([[0.1, 0.05, 0.3]], np.float32)])
+    nrmls = np.array([[0.3, -0.5, 0.8], [0.0, 0.0, 1.0], [-0.6, 0.0, 0.8], [0.48, 0.6, 0.64]], np.float64)
+    nrmls = (nrmls / np.linalg.norm(nrmls, axis=1)[:, None]).astype(np.float32)
+    ks = [9.3, 18.32, 146.55]
+    res = {"tris": tris, "ys": ys, "nrmls": nrmls, "ks": np.array(ks, np.float64)}
+    dGy = np.zeros((len(ks), len(tris), 2, 2), np.float32)    # k, tri, (nsgl, sgl), (re, im)
+    hyp = np.zeros_like(dGy)
+    for a, k in enumerate(ks):
+        for b, tri in enumerate(tris):
+            tri_c, y, nr = np.ascontiguousarray(tri), np.ascontiguousarray(ys[b]), np.ascontiguousarray(nrmls[b])
+            for sgl in (0, 1):
+                o = np.zeros(2, np.float32)
+                L.ref_elem_dGdny(k, ip(tri_c), ip(nr), ip(y), sgl, ip(o))
+                dGy[a, b, sgl] = o
+                L.ref_elem_hyper(k, ip(tri_c), ip(nr), ip(y), sgl, ip(o))
+                hyp[a, b, sgl] = o
+    res["dGdny"], res["hyper"] = dGy, hyp
+    # dirDev_R(k, n, m, nrml, x) for n < 6, |m| <= n at four points
+    xs = np.array([[0.05, -0.02, 0.03], [0.0, 0.0, 0.04], [-0.1, 0.07, -0.02], [0.01, 0.2, 0.0]], np.float32)
+    dd = np.zeros((len(xs), 36, 2), np.float32)
+    for i, x in enumerate(xs):
+        x_c, nr = np.ascontiguousarray(x), np.ascontiguousarray(nrmls[i])
+        for n in range(6):
+            for m in range(-n, n + 1):
+                o = np.zeros(2, np.float32)
+                L.ref_dirdev_R(18.32, n, m, ip(nr), ip(x_c), ip(o))
+                dd[i, n * n + n + m] = o
+    res["dirdev_x"], res["dirdev"], res["dirdev_k"] = xs, dd, np.float64(18.32)
+    np.savez_compressed(os.path.join(HERE, "integral_ext.npz"), **res)
+
+
 def main():
     L = load_ref()
     meta = {}
@@ -192,6 +234,7 @@ def main():
         print("octree", case[0], meta[case[0]]["nf"], flush=True)
     tables(L)
     quadrature(L)
+    integral_ext(L)
     with open(os.path.join(HERE, "octree_meta.json"), "w") as fh:
         json.dump(meta, fh, indent=1, sort_keys=True)
 

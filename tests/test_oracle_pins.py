@@ -3,6 +3,7 @@ identities.  CPU only."""
 import hashlib
 import json
 import os
+import warnings
 
 import numpy as np
 import pytest
@@ -90,6 +91,122 @@ def test_p2m_moments_vs_reference(oracle):
             mine = oracle.elem_moments(k, tris[b], ctr, 6, rule=0, deriv=bool(deriv))
             ref = mom[b, deriv, :, 0] + 1j * mom[b, deriv, :, 1]
             assert np.linalg.norm(mine - ref) <= 1e-5 * np.linalg.norm(ref), (b, deriv)
+
+
+def test_normal_y_and_hypersingular_integrals_vs_reference(oracle):
+    """int dG/dn_y and int d2G/dn_x dn_y (triElemIntegral_pGp2n_* / p2Gp1np2n_*, regular and
+    self term) and dirDev_R against the reference's FP32 outputs."""
+    g = np.load(os.path.join(GOLDEN, "integral_ext.npz"))
+    tris, ys, nr = g["tris"].astype(np.float64), g["ys"].astype(np.float64), g["nrmls"].astype(np.float64)
+    for a, k in enumerate(g["ks"]):
+        kf = float(np.float32(k))
+        for b in range(len(tris)):
+            kr = kf * np.linalg.norm(tris[b].reshape(3, 3) - ys[b], axis=1).max()
+            tol = 3e-7 * max(30.0, kr)
+            for sgl in (0, 1):
+                r = complex(*g["hyper"][a, b, sgl])
+                mine = oracle.elem_hyper(kf, tris[b], nr[b], ys[b], sgl=bool(sgl))
+                assert abs(mine - r) <= tol * abs(r), (a, b, sgl, mine, r)
+            r = complex(*g["dGdny"][a, b, 0])
+            assert abs(oracle.elem_dGdny(kf, tris[b], nr[b], ys[b]) - r) <= tol * abs(r)
+            # flat element: (y - x).n = 0 on every sub-triangle; the reference returns FP32 noise
+            assert abs(oracle.elem_dGdny(kf, tris[b], sgl=True)) < 1e-13 and abs(complex(*g["dGdny"][a, b, 1])) < 1e-5
+    kd = float(np.float32(g["dirdev_k"]))
+    for i, x in enumerate(g["dirdev_x"].astype(np.float64)):
+        ref = g["dirdev"][i, :, 0] + 1j * g["dirdev"][i, :, 1]
+        mine = np.array([oracle.dirdev_R(kd, n, m, nr[i], x) for n in range(6) for m in range(-n, n + 1)])
+        assert np.abs(mine - ref).max() <= 2e-6 * np.abs(ref).max()
+
+
+def test_normal_derivative_integrals_are_derivatives(oracle):
+    """The regular integrals of dG/dn_y and d2G/dn_x dn_y are the y-derivatives along n_y of the
+    integrals of G and dG/dn_x with the same rule; dirDev_R is the derivative of R_n^m."""
+    rng = np.random.default_rng(11)
+    tri = np.array([0.1, 0.0, 0.0, 0.0, 0.12, 0.0, 0.0, 0.0, 0.09])
+    y = np.array([0.3, 0.2, -0.1])
+    n = rng.standard_normal(3)
+    n /= np.linalg.norm(n)
+    k, h = 18.32, 1e-5
+    fd_G = (oracle.elem_integral("G", k, tri, y + h * n) - oracle.elem_integral("G", k, tri, y - h * n)) / (2 * h)
+    assert abs(oracle.elem_dGdny(k, tri, n, y) - fd_G) < 1e-7 * abs(fd_G)
+    fd_dG = (oracle.elem_integral("dG", k, tri, y + h * n) - oracle.elem_integral("dG", k, tri, y - h * n)) / (2 * h)
+    assert abs(oracle.elem_hyper(k, tri, n, y) - fd_dG) < 1e-7 * abs(fd_dG)
+    x = np.array([0.05, -0.02, 0.03])
+    for nn in range(5):
+        for m in range(-nn, nn + 1):
+            f = lambda v: oracle.basis(nn + 1, k, v)[nn * nn + nn + m]
+            fd = (f(x + h * n) - f(x - h * n)) / (2 * h)
+            assert abs(oracle.dirdev_R(k, nn, m, n, x) - fd) < 1e-7 * max(1.0, abs(fd)), (nn, m)
+
+
+def _hyper_finite_part(k, tri, off=0.0):
+    """int_T d2G/dn_x dn_y at the centroid c (off = 0: Hadamard finite part) or at c + off n
+    (n = n_y = n_x), by polar integration about c: adaptive in r, Gauss in theta between the
+    vertex angles.  Independent of the oracle's code."""
+    from scipy.integrate import quad
+
+    V = tri.reshape(3, 3)
+    nrm = np.cross(V[0] - V[2], V[1] - V[2])
+    nrm /= np.linalg.norm(nrm)
+    c = V.mean(axis=0)
+    e1 = (V[0] - c) / np.linalg.norm(V[0] - c)
+    e2 = np.cross(nrm, e1)
+    P = [(np.dot(v - c, e1), np.dot(v - c, e2)) for v in V]
+    ang = [np.arctan2(py, px) % (2 * np.pi) for px, py in P]
+    ang[0] = 0.0
+    cuts = sorted(ang) + [2 * np.pi]
+    t, w = np.polynomial.legendre.leggauss(48)
+
+    def rho(th):
+        u = np.array([np.cos(th), np.sin(th)])
+        best = np.inf
+        for i in range(3):
+            A, B = np.array(P[i]), np.array(P[(i + 1) % 3])
+            d = B - A
+            den = u[0] * d[1] - u[1] * d[0]
+            if abs(den) < 1e-300:
+                continue
+            tt = (A[0] * d[1] - A[1] * d[0]) / den
+            s = ((tt * u - A) @ d) / (d @ d)
+            if tt > 0 and -1e-12 <= s <= 1 + 1e-12:
+                best = min(best, tt)
+        return best
+
+    h = off
+
+    def radial(R):
+        if h == 0.0:
+            # finite part of int_0^R e^{ikr}(1 - ikr)/(4 pi r^2) dr = [-e^{ikr}/(4 pi r)]: drop the 1/r pole
+            return (-np.exp(1j * k * R) / R + 1j * k) / (4 * np.pi)
+        top = np.sqrt(R * R + h * h)
+
+        def f(r):
+            return np.exp(1j * k * r) / (4 * np.pi * r * r) * ((1 - 1j * k * r) - (3 - 3j * k * r - k * k * r * r) * h * h / (r * r))
+        with warnings.catch_warnings():
+            # quad reports roundoff when it reaches 1e-12; that is far below what the test needs
+            warnings.simplefilter("ignore")
+            re = quad(lambda r: f(r).real, h, top, limit=200, epsabs=0, epsrel=1e-12, points=[min(10 * h, top)])[0]
+            im = quad(lambda r: f(r).imag, h, top, limit=200, epsabs=0, epsrel=1e-12, points=[min(10 * h, top)])[0]
+        return re + 1j * im
+
+    total = 0.0
+    for lo, hi in zip(cuts[:-1], cuts[1:]):
+        th = 0.5 * (hi - lo) * t + 0.5 * (hi + lo)
+        total += 0.5 * (hi - lo) * sum(wi * radial(rho(x)) for wi, x in zip(w, th))
+    return total
+
+
+def test_hypersingular_self_term_is_the_finite_part(oracle):
+    """The self term of d2G/dn_x dn_y is the limit of the regular integral as y approaches the
+    centroid along the normal (the normal derivative of the double layer is continuous), and
+    the oracle's polar rule converges to it."""
+    pytest.importorskip("scipy")
+    tri = np.array([0.05, 0.02, 0.01, -0.03, 0.06, 0.02, 0.01, -0.04, 0.07])
+    for k in (9.3, 146.55):
+        fp = _hyper_finite_part(k, tri)
+        near = _hyper_finite_part(k, tri, off=1e-7)
+        assert abs(near - fp) < 1e-4 * abs(fp), (k, near, fp)
+        assert abs(oracle.elem_hyper(k, tri, sgl=True, nth=512) - fp) < 1e-4 * abs(fp)
 
 
 def test_truncnum_vs_reference(oracle):
