@@ -121,6 +121,7 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
     if (nf < 2 || nv < 3) { fmm_set_error("mesh too small (%d vertices, %d triangles)", nv, nf); return FMM_ERR_ARG; }
     if (!(opt->k > 0.0)) { fmm_set_error("wavenumber must be positive"); return FMM_ERR_ARG; }
     if (opt->rule != FMM_RULE_GAUSS3 && opt->rule != FMM_RULE_DUNAVANT7) { fmm_set_error("unknown rule %d", opt->rule); return FMM_ERR_ARG; }
+    if (!std::isfinite(opt->alpha_re) || !std::isfinite(opt->alpha_im)) { fmm_set_error("coupling alpha is not finite"); return FMM_ERR_ARG; }
     if (opt->depth < 0 || opt->depth > FMM_MAX_LEVEL) { fmm_set_error("depth %d out of range", opt->depth); return FMM_ERR_ARG; }
     for (int e = 0; e < nf; e++)
         for (int t = 0; t < 3; t++)

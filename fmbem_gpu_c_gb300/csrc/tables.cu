@@ -18,6 +18,9 @@ namespace fmm {
 __constant__ double c_rule_bary[2][16 * 3];
 __constant__ double c_rule_w[2][16];
 __constant__ int c_rule_n[2];
+// Gauss-Legendre rule on [-1, 1] for the edge integrals of the Burton-Miller terms
+#define LINE_PTS 8
+__constant__ double c_line_x[LINE_PTS], c_line_w[LINE_PTS];
 
 static void gauss_legendre(int n, double *x, double *w)
 {
@@ -82,6 +85,10 @@ static int upload_rules()
     FMM_CUDA_TRY(cudaMemcpyToSymbol(c_rule_bary, bary, sizeof(bary)));
     FMM_CUDA_TRY(cudaMemcpyToSymbol(c_rule_w, w, sizeof(w)));
     FMM_CUDA_TRY(cudaMemcpyToSymbol(c_rule_n, n, sizeof(n)));
+    double lx[LINE_PTS], lw[LINE_PTS];
+    gauss_legendre(LINE_PTS, lx, lw);
+    FMM_CUDA_TRY(cudaMemcpyToSymbol(c_line_x, lx, sizeof(lx)));
+    FMM_CUDA_TRY(cudaMemcpyToSymbol(c_line_w, lw, sizeof(lw)));
     return FMM_OK;
 }
 
@@ -515,6 +522,106 @@ __device__ double2 elem_integral_sgl(double k, const double *nod, int kern)
     return acc;
 }
 
+// ----------------------------------------------------------------------------- Burton-Miller terms
+// The combined operator adds alpha d/dn_y (b L + c M) at the collocation point y (unit normal
+// ny): alpha (b K' + c N).  K' integrates dG/dn_y (pGp2n, integral.cu:400-413); N integrates
+// d2G/dn_x dn_y (p2Gp1np2n, integral.cu:603-622), taken here in forms that stay accurate for
+// the near pairs: the regularised (Maue) form off the element and the polar finite part on it.
+
+// int_T dG(x, y)/dn_y dS_x = int_T G (ik - 1/r) (y - x).ny / r; zero on the flat element itself
+__device__ double2 elem_dGdny(double k, const double *nod, const double *y, const double *ny, int rule)
+{
+    double nh[3];
+    double J = tri_normal(nod, nh);
+    double2 acc = make_double2(0.0, 0.0);
+    int nq = c_rule_n[rule];
+    for (int q = 0; q < nq; q++) {
+        const double *b = &c_rule_bary[rule][3 * q];
+        double x[3];
+        for (int a = 0; a < 3; a++) x[a] = nod[a] * b[0] + nod[3 + a] * b[1] + nod[6 + a] * b[2];
+        double2 g = green_k(k, x, y, ny, 1);   // G (ik - 1/r) (x - y).ny / r
+        double wq = c_rule_w[rule][q] * J;
+        acc.x -= wq * g.x; acc.y -= wq * g.y;
+    }
+    return acc;
+}
+
+// number of equal segments of an edge of length len seen from distance dist: no longer than
+// dist, so that the 8-point rule converges like 4.2^-16 on the 1/r^2 and 1/r^3 integrands
+__device__ __forceinline__ int edge_segments(double len, double dist)
+{
+    double m = ceil(len / fmax(dist, 1e-12 * len));
+    return m > 64.0 ? 64 : (int)m;
+}
+
+// Hadamard finite part of int_T d2G/dn_x dn_y at the centroid c of the flat element T:
+//   -1/(4 pi) [ int_0^{2 pi} e^{ik rho(theta)}/rho(theta) dtheta - 2 pi i k ]
+// (integral.cu:738-751 with the angle integral taken accurately): along edge e, at distance
+// h_e from c and of length L_e, dtheta = h_e L_e / rho^3 ds for s in [0, 1].
+__device__ double2 elem_hyper_self(double k, const double *nod)
+{
+    double c[3];
+    tri_centroid(nod, c);
+    double sr = 0.0, si = 0.0;
+    for (int e = 0; e < 3; e++) {
+        const double *va = nod + 3 * e, *vb = nod + 3 * ((e + 1) % 3);
+        double t[3] = {vb[0] - va[0], vb[1] - va[1], vb[2] - va[2]}, u[3] = {va[0] - c[0], va[1] - c[1], va[2] - c[2]};
+        double c0 = u[1] * t[2] - u[2] * t[1], c1 = u[2] * t[0] - u[0] * t[2], c2 = u[0] * t[1] - u[1] * t[0];
+        double hL = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+        double len = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+        int nseg = edge_segments(len, hL / len);
+        for (int g = 0; g < nseg; g++)
+            for (int q = 0; q < LINE_PTS; q++) {
+                double s = (g + 0.5 + 0.5 * c_line_x[q]) / nseg, w = 0.5 * c_line_w[q] / nseg;
+                double d0 = u[0] + s * t[0], d1 = u[1] + s * t[1], d2 = u[2] + s * t[2];
+                double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+                double sn, cs;
+                sincos(k * r, &sn, &cs);
+                double f = w * hL / (r * r * r);
+                sr += f * cs; si += f * sn;
+            }
+    }
+    return make_double2(-sr / (4.0 * FMM_PI), (2.0 * FMM_PI * k - si) / (4.0 * FMM_PI));
+}
+
+// int_T d2G/dn_x dn_y dS_x at y off T (unit normal ny), regularised (Maue):
+//   k^2 (ny.nT) int_T G dS  -  oint_{dT} (ny x grad_y G) . dl,
+// the boundary traversed v0 -> v1 -> v2 (counter-clockwise about nT); grad_y G =
+// G (ik - 1/r) (y - x)/r.  The edge integrals are regular for y off the element.
+__device__ double2 elem_hyper_near(double k, const double *nod, const double *y, const double *ny, int rule)
+{
+    double nT[3];
+    tri_normal(nod, nT);
+    double2 S = elem_integral(k, nod, y, rule, 0);
+    double dn = ny[0] * nT[0] + ny[1] * nT[1] + ny[2] * nT[2];
+    double lr = 0.0, li = 0.0;
+    for (int e = 0; e < 3; e++) {
+        const double *va = nod + 3 * e, *vb = nod + 3 * ((e + 1) % 3);
+        double t[3] = {vb[0] - va[0], vb[1] - va[1], vb[2] - va[2]}, a[3] = {y[0] - va[0], y[1] - va[1], y[2] - va[2]};
+        double tt = t[0] * t[0] + t[1] * t[1] + t[2] * t[2], len = sqrt(tt);
+        double sc = fmin(fmax((a[0] * t[0] + a[1] * t[1] + a[2] * t[2]) / tt, 0.0), 1.0);
+        double e0 = a[0] - sc * t[0], e1 = a[1] - sc * t[1], e2 = a[2] - sc * t[2];
+        int nseg = edge_segments(len, sqrt(e0 * e0 + e1 * e1 + e2 * e2));
+        // (ny x d) . t = d . (t x ny), d = y - x
+        double tn0 = t[1] * ny[2] - t[2] * ny[1], tn1 = t[2] * ny[0] - t[0] * ny[2], tn2 = t[0] * ny[1] - t[1] * ny[0];
+        for (int g = 0; g < nseg; g++)
+            for (int q = 0; q < LINE_PTS; q++) {
+                double s = (g + 0.5 + 0.5 * c_line_x[q]) / nseg, w = 0.5 * c_line_w[q] / nseg;
+                double d0 = a[0] - s * t[0], d1 = a[1] - s * t[1], d2 = a[2] - s * t[2];
+                double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+                double sn, cs;
+                sincos(k * r, &sn, &cs);
+                double f = w * (d0 * tn0 + d1 * tn1 + d2 * tn2) / (4.0 * FMM_PI * r * r);
+                // G (ik - 1/r) = e^{ikr}/(4 pi r) (ik - 1/r); times f r = w (.)/(4 pi r)
+                double gr = cs, gi = sn, ar = -1.0 / r, ai = k;
+                lr += f * (gr * ar - gi * ai);
+                li += f * (gr * ai + gi * ar);
+            }
+    }
+    double kk = k * k * dn;
+    return make_double2(kk * S.x - lr, kk * S.y - li);
+}
+
 // ----------------------------------------------------------------------------- element tables
 // U_e[n,m] = b int R_n^{-m}(x - c) dS + c int dR_n^{-m}/dn dS   (integral.cu:251-365, the P2M
 // moments of bottomLevelCoeff_L with its loop corrected), Rv_e[n,m] = R_n^m(y_e - c) (L2P).
@@ -552,14 +659,28 @@ __device__ __forceinline__ void basis_prepare(const BasisSh &B, int pb, double k
     __syncwarp();
 }
 
+// nh . grad R_n^m from the staged basis of orders up to n+1 (integral.cu:284-331)
+__device__ __forceinline__ double2 basis_dirdev(const BasisSh &B, int pb, double k, int n, int mm, const double *nh)
+{
+    double2 t0 = csub(cscale(basis_R(B, pb, n + 1, mm + 1), coefB(n + 1, -(mm + 1))),
+                      cscale(basis_R(B, pb, n - 1, mm + 1), coefB(n, mm)));
+    double2 t1 = csub(cscale(basis_R(B, pb, n + 1, mm - 1), coefB(n + 1, mm - 1)),
+                      cscale(basis_R(B, pb, n - 1, mm - 1), coefB(n, -mm)));
+    double2 t2 = csub(cscale(basis_R(B, pb, n - 1, mm), coefA(n - 1, mm)),
+                      cscale(basis_R(B, pb, n + 1, mm), coefA(n, mm)));
+    double2 f0 = make_double2(0.5 * k * nh[0], -0.5 * k * nh[1]);
+    double2 f1 = make_double2(0.5 * k * nh[0], 0.5 * k * nh[1]);
+    return cadd(cadd(cmul(f0, t0), cmul(f1, t1)), cscale(t2, k * nh[2]));
+}
+
 // per-warp shared memory (in doubles) of the element-table kernel: j_n and Q, padded to an
 // even count so the double2 phases that follow stay 16-byte aligned, then 2pb+1 phases
 __host__ __device__ __forceinline__ int basis_ph_offset(int pb) { return (pb + pb * (pb + 1) / 2 + 1) & ~1; }
 __host__ __device__ __forceinline__ int basis_per_warp(int pb) { return basis_ph_offset(pb) + 2 * (2 * pb + 1); }
 
 __global__ void element_tables_kernel(const double *V, const int *F, const int *elem_leaf, const double *box_ctr,
-                                      int nf, int pl, double k, double2 bco, double2 cco, int rule,
-                                      double2 *U, double2 *Rv)
+                                      int nf, int pl, double k, double2 bco, double2 cco, double2 alpha,
+                                      int rule, double2 *U, double2 *Rv)
 {
     extern __shared__ double2 smem2[];
     double *smem = (double *)smem2;
@@ -600,16 +721,7 @@ __global__ void element_tables_kernel(const double *V, const int *F, const int *
                 }
                 if (cco.x != 0.0 || cco.y != 0.0) {
                     // directional derivative along nh (integral.cu:284-331)
-                    double2 t0 = csub(cscale(basis_R(B, pb, n + 1, mm + 1), coefB(n + 1, -(mm + 1))),
-                                      cscale(basis_R(B, pb, n - 1, mm + 1), coefB(n, mm)));
-                    double2 t1 = csub(cscale(basis_R(B, pb, n + 1, mm - 1), coefB(n + 1, mm - 1)),
-                                      cscale(basis_R(B, pb, n - 1, mm - 1), coefB(n, -mm)));
-                    double2 t2 = csub(cscale(basis_R(B, pb, n - 1, mm), coefA(n - 1, mm)),
-                                      cscale(basis_R(B, pb, n + 1, mm), coefA(n, mm)));
-                    double2 f0 = make_double2(0.5 * k * nh[0], -0.5 * k * nh[1]);
-                    double2 f1 = make_double2(0.5 * k * nh[0], 0.5 * k * nh[1]);
-                    double2 d = cadd(cadd(cmul(f0, t0), cmul(f1, t1)), cscale(t2, k * nh[2]));
-                    acc = cadd(acc, cmul(cco, d));
+                    acc = cadd(acc, cmul(cco, basis_dirdev(B, pb, k, n, mm, nh)));
                 }
                 Ue[i] = cadd(Ue[i], cscale(acc, wq));
             }
@@ -624,7 +736,11 @@ __global__ void element_tables_kernel(const double *V, const int *F, const int *
             while (n * n > i) n--;
             while ((n + 1) * (n + 1) <= i) n++;
             int m = i - n * n - n;
-            Re[i] = basis_R(B, pb, n, m);
+            // L2P vector of R + alpha dR/dn at the centroid (Burton-Miller: the target-side
+            // normal derivative of the far field)
+            double2 r = basis_R(B, pb, n, m);
+            if (alpha.x != 0.0 || alpha.y != 0.0) r = cadd(r, cmul(alpha, basis_dirdev(B, pb, k, n, m, nh)));
+            Re[i] = r;
         }
         __syncwarp();
     }
@@ -662,8 +778,10 @@ int gen_element_tables(Plan *P)
     }
     int blocks = std::min((P->nf + warps - 1) / warps, 152 * 32);
     double2 bco = make_double2(P->opt.b_re, P->opt.b_im), cco = make_double2(P->opt.c_re, P->opt.c_im);
+    double2 alpha = make_double2(P->opt.alpha_re, P->opt.alpha_im);
     element_tables_kernel<<<blocks, 32 * warps, shm, P->stream>>>(P->V_dev, P->F_dev, P->elem_leaf, ctr_dev, P->nf, pl,
-                                                                   P->opt.k, bco, cco, P->opt.rule, P->U64, P->Rv64);
+                                                                   P->opt.k, bco, cco, alpha, P->opt.rule, P->U64,
+                                                                   P->Rv64);
     FMM_CUDA_TRY(cudaGetLastError());
     FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
     if (P->opt.build_mixed) {
@@ -678,26 +796,37 @@ int gen_element_tables(Plan *P)
 }
 
 // ----------------------------------------------------------------------------- near field
-// A_ij = b int_{T_j} G(x, y_i) dS + c int_{T_j} dG/dn_x(x, y_i) dS for source elements j in
-// the leaf boxes adjacent to (or equal to) the leaf box of target i; the self term uses the
-// centroid split.  One warp per target element, one lane per source element.
+// A_ij = b int_{T_j} G(x, y_i) dS + c int_{T_j} dG/dn_x(x, y_i) dS
+//        + alpha (b int_{T_j} dG/dn_y dS + c int_{T_j} d2G/dn_x dn_y dS)
+// for source elements j in the leaf boxes adjacent to (or equal to) the leaf box of target i;
+// the self term uses the centroid split (and the polar finite part for the hypersingular
+// term).  One warp per target element, one lane per source element.
 __global__ void near_field_kernel(const double *V, const int *F, int nf, const int *near_beg, const int *near_col,
-                                  double k, double2 bco, double2 cco, int rule, double2 *out)
+                                  double k, double2 bco, double2 cco, double2 alpha, int rule, double2 *out)
 {
     int lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int nwt = (gridDim.x * blockDim.x) >> 5;
+    bool bm = alpha.x != 0.0 || alpha.y != 0.0;
     for (int i = warp; i < nf; i += nwt) {
-        double nodi[9], y[3];
+        double nodi[9], y[3], ny[3];
         load_tri(V, F, i, nodi);
         tri_centroid(nodi, y);
+        tri_normal(nodi, ny);
         for (int s = near_beg[i] + lane; s < near_beg[i + 1]; s += 32) {
             int j = near_col[s];
             double nod[9];
             load_tri(V, F, j, nod);
             double2 v = make_double2(0.0, 0.0);
             bool sgl = (i == j);
-            if (bco.x != 0.0 || bco.y != 0.0) v = cadd(v, cmul(bco, sgl ? elem_integral_sgl(k, nod, 0) : elem_integral(k, nod, y, rule, 0)));
-            if (cco.x != 0.0 || cco.y != 0.0) v = cadd(v, cmul(cco, sgl ? elem_integral_sgl(k, nod, 1) : elem_integral(k, nod, y, rule, 1)));
+            bool hb = bco.x != 0.0 || bco.y != 0.0, hc = cco.x != 0.0 || cco.y != 0.0;
+            if (hb) v = cadd(v, cmul(bco, sgl ? elem_integral_sgl(k, nod, 0) : elem_integral(k, nod, y, rule, 0)));
+            if (hc) v = cadd(v, cmul(cco, sgl ? elem_integral_sgl(k, nod, 1) : elem_integral(k, nod, y, rule, 1)));
+            if (bm) {
+                double2 w = make_double2(0.0, 0.0);
+                if (hb && !sgl) w = cadd(w, cmul(bco, elem_dGdny(k, nod, y, ny, rule)));
+                if (hc) w = cadd(w, cmul(cco, sgl ? elem_hyper_self(k, nod) : elem_hyper_near(k, nod, y, ny, rule)));
+                v = cadd(v, cmul(alpha, w));
+            }
             out[s] = v;
         }
     }
@@ -708,8 +837,9 @@ int gen_near_field(Plan *P)
     FMM_CUDA_TRY(dev_alloc(P, (void **)&P->near64, sizeof(double2) * (P->num_near + 1)));
     double2 bco = make_double2(P->opt.b_re, P->opt.b_im), cco = make_double2(P->opt.c_re, P->opt.c_im);
     int blocks = std::min((P->nf + 7) / 8, 152 * 16);
+    double2 alpha = make_double2(P->opt.alpha_re, P->opt.alpha_im);
     near_field_kernel<<<blocks, 256, 0, P->stream>>>(P->V_dev, P->F_dev, P->nf, P->near_beg, P->near_col, P->opt.k,
-                                                      bco, cco, P->opt.rule, P->near64);
+                                                      bco, cco, alpha, P->opt.rule, P->near64);
     FMM_CUDA_TRY(cudaGetLastError());
     FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
     if (P->opt.build_mixed) {
@@ -721,16 +851,22 @@ int gen_near_field(Plan *P)
 }
 
 // ----------------------------------------------------------------------------- far field
-__global__ void far_field_kernel(const double *V, const int *F, int nf, double k, int rule, const double2 *p,
-                                 const double *pts, double2 *out)
+// -(b L + c M) p at exterior points: the scattered pressure p_s = M p - L dp/dn of the exterior
+// problem written as c = -1, b = (dp/dn)/p (rigid body: b = 0, p_s = M p).  One block per point.
+__global__ void far_field_kernel(const double *V, const int *F, int nf, double k, double2 bco, double2 cco, int rule,
+                                 const double2 *p, const double *pts, double2 *out)
 {
     int t = blockIdx.x;
     double y[3] = {pts[3 * t], pts[3 * t + 1], pts[3 * t + 2]};
+    bool hb = bco.x != 0.0 || bco.y != 0.0, hc = cco.x != 0.0 || cco.y != 0.0;
     double2 acc = make_double2(0.0, 0.0);
     for (int j = threadIdx.x; j < nf; j += blockDim.x) {
         double nod[9];
         load_tri(V, F, j, nod);
-        acc = cadd(acc, cmul(p[j], elem_integral(k, nod, y, rule, 1)));
+        double2 v = make_double2(0.0, 0.0);
+        if (hb) v = cadd(v, cmul(bco, elem_integral(k, nod, y, rule, 0)));
+        if (hc) v = cadd(v, cmul(cco, elem_integral(k, nod, y, rule, 1)));
+        acc = csub(acc, cmul(p[j], v));
     }
     __shared__ double2 red[256];
     red[threadIdx.x] = acc;
@@ -745,13 +881,16 @@ __global__ void far_field_kernel(const double *V, const int *F, int nf, double k
 int launch_far_field(Plan *P, const double2 *p, const double *pts, int npts, double2 *out)
 {
     if (npts <= 0) return FMM_OK;
-    far_field_kernel<<<npts, 256, 0, P->stream>>>(P->V_dev, P->F_dev, P->nf, P->opt.k, P->opt.rule, p, pts, out);
+    double2 bco = make_double2(P->opt.b_re, P->opt.b_im), cco = make_double2(P->opt.c_re, P->opt.c_im);
+    far_field_kernel<<<npts, 256, 0, P->stream>>>(P->V_dev, P->F_dev, P->nf, P->opt.k, bco, cco, P->opt.rule, p, pts,
+                                                   out);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
 
+// p_inc + alpha dp_inc/dn = e^{ik d.y} (1 + alpha i k d.n) at the centroids (alpha = 0: p_inc)
 __global__ void plane_wave_kernel(const double *V, const int *F, int nf, double k, double dx, double dy, double dz,
-                                  double2 *rhs)
+                                  double2 alpha, double2 *rhs)
 {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nf; e += gridDim.x * blockDim.x) {
         double nod[9], y[3];
@@ -759,14 +898,22 @@ __global__ void plane_wave_kernel(const double *V, const int *F, int nf, double 
         tri_centroid(nod, y);
         double s, c;
         sincos(k * (dx * y[0] + dy * y[1] + dz * y[2]), &s, &c);
-        rhs[e] = make_double2(c, s);
+        double2 v = make_double2(c, s);
+        if (alpha.x != 0.0 || alpha.y != 0.0) {
+            double nh[3];
+            tri_normal(nod, nh);
+            double kd = k * (dx * nh[0] + dy * nh[1] + dz * nh[2]);
+            v = cmul(v, make_double2(1.0 - alpha.y * kd, alpha.x * kd));
+        }
+        rhs[e] = v;
     }
 }
 
 int launch_plane_wave(Plan *P, const double *dir, double2 *rhs)
 {
     plane_wave_kernel<<<(P->nf + 255) / 256, 256, 0, P->stream>>>(P->V_dev, P->F_dev, P->nf, P->opt.k, dir[0], dir[1],
-                                                                   dir[2], rhs);
+                                                                   dir[2], make_double2(P->opt.alpha_re, P->opt.alpha_im),
+                                                                   rhs);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

@@ -344,13 +344,24 @@ __device__ __forceinline__ void add_vertex_grad(double *grad, const int *F, int 
 }
 
 // ----------------------------------------------------------------------------- VJP kernels
-// right-hand side of the conjugated adjoint system: rhs_j = sum_k F_kj conj(pbar_k)
-__global__ void vjp_adjoint_rhs_kernel(const double *V, const int *F, int nf, double k, int rule, const double *pts,
-                                       int npts, const double2 *pbar, double2 *rhs);
+// the far-field operator F_kj = -int_{T_j} (b G + c dG/dn_x)(x, p_k) dS (fmm_far_field) with
+// dual-number vertex derivatives
+template <int N>
+__device__ __forceinline__ CDn<N> far_entry_d(double k, const Dn<N> *nod, const Dn<N> *y, int rule, double2 nb, double2 nc)
+{
+    CDn<N> f = cdzero<N>();
+    if (nb.x != 0.0 || nb.y != 0.0) cdmac(f, nb, elem_integral_d(k, nod, y, rule, 0));
+    if (nc.x != 0.0 || nc.y != 0.0) cdmac(f, nc, elem_integral_d(k, nod, y, rule, 1));
+    return f;
+}
 
-// 2 Re[ sum_k conj(pbar_k) x_j dF_kj/dV_j ] for the vertices of element j
-__global__ void vjp_farpts_kernel(const double *V, const int *F, int nf, double k, int rule, const double *pts, int npts,
-                                  const double2 *pbar, const double2 *x, double *grad)
+// right-hand side of the conjugated adjoint system: rhs_j = sum_k F_kj conj(pbar_k)
+__global__ void vjp_adjoint_rhs_kernel(const double *V, const int *F, int nf, double k, int rule, double2 nb, double2 nc,
+                                       const double *pts, int npts, const double2 *pbar, double2 *rhs);
+
+// 2 Re[ sum_k conj(pbar_k) x_j dF_kj/dV_j ] for the vertices of element j; nb = -b, nc = -c
+__global__ void vjp_farpts_kernel(const double *V, const int *F, int nf, double k, int rule, double2 nb, double2 nc,
+                                  const double *pts, int npts, const double2 *pbar, const double2 *x, double *grad)
 {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf; j += gridDim.x * blockDim.x) {
         double nd[9];
@@ -361,7 +372,7 @@ __global__ void vjp_farpts_kernel(const double *V, const int *F, int nf, double 
         double2 xj = x[j];
         for (int t = 0; t < npts; t++) {
             Dn<9> y[3] = {dconst<9>(pts[3 * t]), dconst<9>(pts[3 * t + 1]), dconst<9>(pts[3 * t + 2])};
-            CDn<9> f = elem_integral_d(k, nod, y, rule, 1);
+            CDn<9> f = far_entry_d(k, nod, y, rule, nb, nc);
             double2 pb = pbar[t];
             // w = conj(pbar) x_j
             double2 w = make_double2(pb.x * xj.x + pb.y * xj.y, pb.x * xj.y - pb.y * xj.x);
@@ -371,8 +382,8 @@ __global__ void vjp_farpts_kernel(const double *V, const int *F, int nf, double 
     }
 }
 
-__global__ void vjp_adjoint_rhs_kernel(const double *V, const int *F, int nf, double k, int rule, const double *pts,
-                                       int npts, const double2 *pbar, double2 *rhs)
+__global__ void vjp_adjoint_rhs_kernel(const double *V, const int *F, int nf, double k, int rule, double2 nb, double2 nc,
+                                       const double *pts, int npts, const double2 *pbar, double2 *rhs)
 {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf; j += gridDim.x * blockDim.x) {
         double nd[9];
@@ -382,7 +393,7 @@ __global__ void vjp_adjoint_rhs_kernel(const double *V, const int *F, int nf, do
         double2 acc = make_double2(0.0, 0.0);
         for (int t = 0; t < npts; t++) {
             Dn<1> y[3] = {dconst<1>(pts[3 * t]), dconst<1>(pts[3 * t + 1]), dconst<1>(pts[3 * t + 2])};
-            CDn<1> f = elem_integral_d(k, nod, y, rule, 1);
+            CDn<1> f = far_entry_d(k, nod, y, rule, nb, nc);
             double2 pb = pbar[t];
             acc.x += f.re.v * pb.x + f.im.v * pb.y; // F conj(pbar)
             acc.y += f.im.v * pb.x - f.re.v * pb.y;
@@ -603,6 +614,10 @@ extern "C" int fmm_vjp(fmm_plan *plan, const cuDoubleComplex *x, const double *d
     if (!P || !x || !pts || npts < 1 || !pbar || !grad || !(tol > 0)) { fmm_set_error("fmm_vjp: invalid argument"); return FMM_ERR_ARG; }
     if (precision != FMM_FP64 && precision != FMM_MIXED) { fmm_set_error("fmm_vjp: unknown precision"); return FMM_ERR_ARG; }
     if (P->pleaf + 1 > VJP_PMAX) { fmm_set_error("fmm_vjp: leaf order %d above %d", P->pleaf, VJP_PMAX - 1); return FMM_ERR_ARG; }
+    if (P->opt.alpha_re != 0.0 || P->opt.alpha_im != 0.0) {
+        fmm_set_error("fmm_vjp: the Burton-Miller operator (alpha != 0) has no vertex derivative here");
+        return FMM_ERR_ARG;
+    }
     int nf = P->nf, nv = P->nv, pl = P->pleaf, lmax = P->lmax;
     int nbl = P->lev[lmax].nb;
     cudaStream_t st = P->stream;
@@ -640,7 +655,8 @@ extern "C" int fmm_vjp(fmm_plan *plan, const cuDoubleComplex *x, const double *d
     {
         const int T = 128, B = std::min((nf + T - 1) / T, 152 * 8);
         // adjoint system A^T mu = F^T conj(pbar)
-        vjp_adjoint_rhs_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, P->opt.k, P->opt.rule, ptd, npts, pb, rhs);
+        double2 nb = make_double2(-P->opt.b_re, -P->opt.b_im), nc = make_double2(-P->opt.c_re, -P->opt.c_im);
+        vjp_adjoint_rhs_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, P->opt.k, P->opt.rule, nb, nc, ptd, npts, pb, rhs);
         VTRY(cudaGetLastError());
         int it = 0;
         double rr = 0.0;
@@ -659,7 +675,7 @@ extern "C" int fmm_vjp(fmm_plan *plan, const cuDoubleComplex *x, const double *d
         vjp_far_target_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, pl, P->opt.k, P->elem_leaf, ctr, D, mu, gd);
         vjp_near_kernel<<<std::min((nf + 7) / 8, 152 * 16), 256, 0, st>>>(P->V_dev, P->F_dev, nf, P->near_beg, P->near_col,
                                                                         P->opt.k, bco, cco, P->opt.rule, mu, xd, gd);
-        vjp_farpts_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, P->opt.k, P->opt.rule, ptd, npts, pb, xd, gd);
+        vjp_farpts_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, P->opt.k, P->opt.rule, nb, nc, ptd, npts, pb, xd, gd);
         if (dir)
             vjp_rhs_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, P->opt.k, dir[0], dir[1], dir[2], mu, gd);
         VTRY(cudaGetLastError());

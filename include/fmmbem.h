@@ -5,13 +5,20 @@
  * the element moment tables for P2M/L2P, the near-field matrix, and device buffers for
  * the FP64 and mixed-precision matvecs.  The operator is
  *
- *     y = a x + b L x + c M x,   (L x)_i = sum_j int_{T_j} G(x, y_i) x_j dS,
- *                                (M x)_i = sum_j int_{T_j} dG/dn_x(x, y_i) x_j dS,
+ *     y = a x + (1 + alpha d/dn_y) (b L + c M) x,
+ *         (L x)_i = sum_j int_{T_j} G(x, y_i) x_j dS,
+ *         (M x)_i = sum_j int_{T_j} dG/dn_x(x, y_i) x_j dS,
  *
- * with collocation at triangle centroids and one unknown per triangle (constant elements),
- * G = exp(ik r)/(4 pi r).  The reference's OprL (translation.cu:3412) computes the far part
- * of L only; fmm_matvec replaces it with the complete operator.  For a rigid (sound-hard)
- * body the exterior Neumann problem is a = 1/2, b = 0, c = -1 with right-hand side p_inc.
+ * with collocation at triangle centroids y_i and one unknown per triangle (constant
+ * elements), G = exp(ik r)/(4 pi r), d/dn_y the derivative along the unit normal at y_i.  The
+ * reference's OprL (translation.cu:3412) computes the far part of L only; fmm_matvec replaces
+ * it with the complete operator.  For a rigid (sound-hard) body the exterior Neumann problem
+ * is a = 1/2, b = 0, c = -1 with right-hand side p_inc; a locally reacting surface
+ * (dp/dn = i k beta p) has b = i k beta.  alpha != 0 is the Burton-Miller combination of that
+ * equation with its normal derivative (the hypersingular kernels of integral.cu:603-751),
+ * uniquely solvable at every wavenumber for Im(alpha) != 0 (alpha = i/k is usual); then
+ * a = (1 + alpha b)/2 and the right-hand side is p_inc + alpha dp_inc/dn
+ * (fmm_plane_wave_rhs adds the second term itself).
  *
  * Complex arrays are cuDoubleComplex (re, im interleaved doubles).  Every entry point
  * returns an fmm_status; FMM_OK is 0 (EXIT_SUCCESS).  Plans are not thread-safe: callers
@@ -56,6 +63,7 @@ typedef struct {
                                  fmm_last_error of a mixed call, where orders exceed 42 or coaxial
                                  entries exceed the FP32 range) */
     int device;               /* CUDA device ordinal */
+    double alpha_re, alpha_im;/* Burton-Miller coupling alpha (0: the conventional operator) */
 } fmm_options;
 
 typedef struct {
@@ -141,11 +149,13 @@ int fmm_solve_many(fmm_plan *const *plans, int n, const cuDoubleComplex *const *
 int fmm_vjp(fmm_plan *plan, const cuDoubleComplex *x, const double *dir, const double *pts, int npts,
             const cuDoubleComplex *pbar, double tol, int precision, double *grad, cuDoubleComplex *lambda);
 
-/* Scattered pressure of a rigid body at npts exterior points from the surface pressure p:
- * sum_j p_j int_{T_j} dG/dn_x(x, y) dS(x), regular rule of the plan. */
+/* Scattered pressure at npts exterior points y from the surface pressure p:
+ * -sum_j p_j int_{T_j} (b G + c dG/dn_x)(x, y) dS(x) with the plan's b and c and regular rule,
+ * i.e. M p - L dp/dn for the exterior problem (c = -1, b = (dp/dn)/p; rigid body: M p). */
 int fmm_far_field(fmm_plan *plan, const cuDoubleComplex *p, const double *pts, int npts, cuDoubleComplex *out);
 
-/* Right-hand side for a unit plane wave exp(i k d.x) at the element centroids. */
+/* Right-hand side for a unit plane wave exp(i k d.x) at the element centroids, plus
+ * alpha d/dn of it when the plan has a Burton-Miller coupling alpha. */
 int fmm_plane_wave_rhs(fmm_plan *plan, const double *dir, cuDoubleComplex *rhs);
 
 /* Mesh generators (front end for the synthetic configurations).  Return counts through

@@ -678,6 +678,136 @@ void orc_diff_coeff(double k, const double *coeffp, int p, const double *nrml, d
 #undef CF
 }
 
+/* int_T d2G/dn_x dn_y dS_y at the collocation point x with unit normal nx, T flat with unit
+ * normal nT, in the regularised (Maue) form
+ *     k^2 (nx.nT) int_T G dS_y  -  oint_{dT} (nx x grad_x G(x, y)) . dl_y,
+ * the boundary traversed v0 -> v1 -> v2 (counter-clockwise about nT).  With x the centroid of
+ * T itself (sgl) the finite part in polar form (elem_hyper_self). */
+#define MAUE_LINE_PTS 8
+/* distance from x to the segment [a, b] */
+static double seg_dist(const double *x, const double *a, const double *b)
+{
+    double t[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, d[3] = {x[0] - a[0], x[1] - a[1], x[2] - a[2]};
+    double tt = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+    double s = (d[0] * t[0] + d[1] * t[1] + d[2] * t[2]) / tt;
+    s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+    double e[3] = {d[0] - s * t[0], d[1] - s * t[1], d[2] - s * t[2]};
+    return sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+}
+
+/* Hadamard finite part of int_T d2G/dn_x dn_y at the centroid c of the flat element T,
+ *     -1/(4 pi) [ int_0^{2 pi} e^{ik rho(theta)} / rho(theta) dtheta - 2 pi i k ],
+ * the angle integral taken edge by edge: along edge e (length L_e, distance h_e from c)
+ * dtheta = h_e L_e / rho^3 ds, s in [0, 1], by Gauss on segments no longer than h_e. */
+static cplx elem_hyper_self(double k, const double *nod)
+{
+    double c[3], gx[MAUE_LINE_PTS], gw[MAUE_LINE_PTS];
+    tri_centroid(nod, c);
+    orc_gauss_legendre(MAUE_LINE_PTS, gx, gw);
+    cplx ang = 0.0;
+    for (int e = 0; e < 3; e++) {
+        const double *va = nod + 3 * e, *vb = nod + 3 * ((e + 1) % 3);
+        double t[3] = {vb[0] - va[0], vb[1] - va[1], vb[2] - va[2]}, u[3] = {va[0] - c[0], va[1] - c[1], va[2] - c[2]};
+        double cr[3] = {u[1] * t[2] - u[2] * t[1], u[2] * t[0] - u[0] * t[2], u[0] * t[1] - u[1] * t[0]};
+        double hL = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);  /* h_e L_e */
+        double len = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+        int nseg = (int)ceil(len / fmax(hL / len, 1e-12 * len));
+        if (nseg > 64) nseg = 64;
+        for (int g = 0; g < nseg; g++)
+            for (int q = 0; q < MAUE_LINE_PTS; q++) {
+                double s = (g + 0.5 + 0.5 * gx[q]) / nseg, w = 0.5 * gw[q] / nseg;
+                double d[3] = {u[0] + s * t[0], u[1] + s * t[1], u[2] + s * t[2]};
+                double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                ang += w * hL * (cos(k * r) + I * sin(k * r)) / (r * r * r);
+            }
+    }
+    return -(ang - 2.0 * PI_D * I * k) / (4.0 * PI_D);
+}
+
+static cplx elem_hyper_maue(double k, const double *nod, const double *x, const double *nx, int rule, int sgl)
+{
+    if (sgl) return elem_hyper_self(k, nod);
+    double nT[3], J;
+    tri_normal(nod, nT, &J);
+    nT[0] /= J; nT[1] /= J; nT[2] /= J;
+    double dotn = nx[0] * nT[0] + nx[1] * nT[1] + nx[2] * nT[2];
+    cplx S = sgl ? elem_integral_sgl(k, nod, 0) : elem_integral(k, nod, x, rule, 0);
+    double gx[MAUE_LINE_PTS], gw[MAUE_LINE_PTS];
+    orc_gauss_legendre(MAUE_LINE_PTS, gx, gw);
+    cplx line = 0.0;
+    for (int e = 0; e < 3; e++) {
+        const double *va = nod + 3 * e, *vb = nod + 3 * ((e + 1) % 3);
+        double t[3] = {vb[0] - va[0], vb[1] - va[1], vb[2] - va[2]};
+        double len = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+        /* segments no longer than the distance from x: Gauss converges like 4.2^(-2n) */
+        double dist = seg_dist(x, va, vb);
+        int nseg = (int)ceil(len / fmax(dist, 1e-12 * len));
+        if (nseg > 64) nseg = 64;
+        for (int g = 0; g < nseg; g++)
+            for (int q = 0; q < MAUE_LINE_PTS; q++) {
+                double s = (g + 0.5 + 0.5 * gx[q]) / nseg, w = 0.5 * gw[q] / nseg;
+                double d[3] = {x[0] - va[0] - s * t[0], x[1] - va[1] - s * t[1], x[2] - va[2] - s * t[2]};
+                double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                cplx gr = (cos(k * r) + I * sin(k * r)) / (4.0 * PI_D * r);
+                /* (nx x grad_x G) . t,  grad_x G = G (ik - 1/r) d / r */
+                double cr[3] = {nx[1] * d[2] - nx[2] * d[1], nx[2] * d[0] - nx[0] * d[2], nx[0] * d[1] - nx[1] * d[0]};
+                line += w * gr * (I * k - 1.0 / r) / r * (cr[0] * t[0] + cr[1] * t[1] + cr[2] * t[2]);
+            }
+    }
+    return k * k * dotn * S - line;
+}
+
+/* int_T dG/dn_x dS_y at the collocation point x with unit normal nx (the normal derivative of
+ * the single layer at x); zero on the flat element itself */
+static cplx elem_dGdnx(double k, const double *nod, const double *x, const double *nx, int rule, int sgl)
+{
+    if (sgl) return 0.0;
+    double bary[64 * 3], w[64], nn[3], J;
+    int nq = orc_rule(rule, bary, w);
+    tri_normal(nod, nn, &J);
+    cplx acc = 0.0;
+    for (int q = 0; q < nq; q++) {
+        double y[3];
+        tri_point(nod, bary + 3 * q, y);
+        acc += w[q] * J * dgreen_y(k, y, x, nx);
+    }
+    return acc;
+}
+
+/* Near-field coefficient of source element j at collocation element i (centroid yc, unit
+ * normal nh), without the diagonal a:
+ *     b L + c M + alpha (b K' + c N)
+ * L, M with the regular rule or the centroid split (self); K' the normal derivative of L at
+ * yc; N the normal derivative of M in the Maue form.  alpha = 0 is the conventional operator. */
+static cplx pair_value(double k, const double *nod, const double *yc, const double *nh, int sgl, int rule, cplx b, cplx c,
+                       cplx alpha)
+{
+    cplx v = 0.0;
+    if (b != 0.0) v += b * (sgl ? elem_integral_sgl(k, nod, 0) : elem_integral(k, nod, yc, rule, 0));
+    if (c != 0.0) v += c * (sgl ? elem_integral_sgl(k, nod, 1) : elem_integral(k, nod, yc, rule, 1));
+    if (alpha != 0.0) {
+        cplx w = 0.0;
+        if (b != 0.0) w += b * elem_dGdnx(k, nod, yc, nh, rule, sgl);
+        if (c != 0.0) w += c * elem_hyper_maue(k, nod, yc, nh, rule, sgl);
+        v += alpha * w;
+    }
+    return v;
+}
+
+/* the Maue-form element integral for the tests */
+void orc_elem_hyper_maue(double k, const double *nod9, const double *x, const double *nx, int rule, int sgl, double *out)
+{
+    cplx z = elem_hyper_maue(k, nod9, x, nx, rule, sgl);
+    out[0] = creal(z); out[1] = cimag(z);
+}
+
+static void unit_normal(const double *nod, double *nh)
+{
+    double J;
+    tri_normal(nod, nh, &J);
+    nh[0] /= J; nh[1] /= J; nh[2] /= J;
+}
+
 /* ------------------------------------------------------------------ FMM */
 typedef struct {
     int nb, p;
@@ -694,7 +824,7 @@ typedef struct {
 struct orc_fmm {
     int nv, nf, lmax, rule, nthreads, pmax;
     double k, d, pt_min[3];
-    cplx a, b, c;
+    cplx a, b, c, alpha;  /* y = a x + (1 + alpha d/dn_y)(b L + c M) x */
     double *Vc;
     int *F;
     orc_level lev[16];
@@ -755,14 +885,14 @@ static void rng_axis(int t, int top, int *lo, int *hi)
 
 orc_fmm *orc_fmm_create(int nv, const double *V, int nf, const int *F, double k,
                         double a_re, double a_im, double b_re, double b_im, double c_re, double c_im,
-                        int rule, int lmax, const int *nbox, const long long *boxes,
+                        double al_re, double al_im, int rule, int lmax, const int *nbox, const long long *boxes,
                         const int *elem_leaf, const int *p_level, double d, const double *pt_min,
                         int nthreads)
 {
     orc_fmm *f = (orc_fmm *)calloc(1, sizeof(orc_fmm));
     f->nv = nv; f->nf = nf; f->k = k; f->lmax = lmax; f->rule = rule; f->d = d;
     f->nthreads = nthreads > 0 ? nthreads : 1;
-    f->a = a_re + I * a_im; f->b = b_re + I * b_im; f->c = c_re + I * c_im;
+    f->a = a_re + I * a_im; f->b = b_re + I * b_im; f->c = c_re + I * c_im; f->alpha = al_re + I * al_im;
     memcpy(f->pt_min, pt_min, sizeof(double) * 3);
     f->Vc = (double *)malloc(sizeof(double) * 3 * nv);
     memcpy(f->Vc, V, sizeof(double) * 3 * nv);
@@ -926,7 +1056,19 @@ orc_fmm *orc_fmm_create(int nv, const double *V, int nf, const int *F, double k,
             }
             tri_centroid(nod, y);
             v[0] = y[0] - c[0]; v[1] = y[1] - c[1]; v[2] = y[2] - c[2];
-            basis_generic(pl, k, v, f->Rv + e * ppl, 0);
+            if (f->alpha == 0.0) {
+                basis_generic(pl, k, v, f->Rv + e * ppl, 0);
+            } else {
+                /* L2P vector of R + alpha dR/dn at the centroid along the element normal */
+                double nh[3];
+                unit_normal(nod, nh);
+                cplx *Rb = (cplx *)malloc(sizeof(cplx) * (pl + 1) * (pl + 1));
+                basis_generic(pl + 1, k, v, Rb, 0);
+                for (int n = 0; n < pl; n++)
+                    for (int m = -n; m <= n; m++)
+                        f->Rv[e * ppl + NM(n, m)] = Rb[NM(n, m)] + f->alpha * dirdev_R(k, n, m, nh, Rb);
+                free(Rb);
+            }
         }
         free(tmp);
     }
@@ -959,10 +1101,11 @@ orc_fmm *orc_fmm_create(int nv, const double *V, int nf, const int *F, double k,
 #pragma omp parallel for num_threads(f->nthreads) schedule(dynamic, 64)
         for (int e = 0; e < nf; e++) {
             int b = elem_leaf[e], pos = f->near_beg[e];
-            double nodi[9], y[3];
+            double nodi[9], y[3], nh[3];
             for (int t = 0; t < 3; t++)
                 for (int a = 0; a < 3; a++) nodi[3 * t + a] = V[3 * F[3 * e + t] + a];
             tri_centroid(nodi, y);
+            unit_normal(nodi, nh);
             for (int t = 0; t < nnb[b]; t++) {
                 int q = nbrs[27 * b + t];
                 for (int s = f->leaf_beg[q]; s < f->leaf_beg[q + 1]; s++) {
@@ -970,10 +1113,7 @@ orc_fmm *orc_fmm_create(int nv, const double *V, int nf, const int *F, double k,
                     double nod[9];
                     for (int u = 0; u < 3; u++)
                         for (int a = 0; a < 3; a++) nod[3 * u + a] = V[3 * F[3 * j + u] + a];
-                    cplx val = 0.0;
-                    int sgl = (j == e);
-                    if (f->b != 0.0) val += f->b * (sgl ? elem_integral_sgl(k, nod, 0) : elem_integral(k, nod, y, rule, 0));
-                    if (f->c != 0.0) val += f->c * (sgl ? elem_integral_sgl(k, nod, 1) : elem_integral(k, nod, y, rule, 1));
+                    cplx val = pair_value(k, nod, y, nh, j == e, rule, f->b, f->c, f->alpha);
                     f->near_col[pos] = j;
                     f->near_val[pos] = val;
                     pos++;
@@ -1131,28 +1271,25 @@ void orc_fmm_destroy(orc_fmm *f)
 
 void orc_dense_apply(int nv, const double *V, int nf, const int *F, double k,
                      double a_re, double a_im, double b_re, double b_im, double c_re, double c_im,
-                     int rule, const double *xin, double *yout, int nthreads)
+                     double al_re, double al_im, int rule, const double *xin, double *yout, int nthreads)
 {
     (void)nv;
     const cplx *x = (const cplx *)xin;
     cplx *y = (cplx *)yout;
-    cplx a = a_re + I * a_im, b = b_re + I * b_im, c = c_re + I * c_im;
+    cplx a = a_re + I * a_im, b = b_re + I * b_im, c = c_re + I * c_im, al = al_re + I * al_im;
 #pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) schedule(dynamic, 16)
     for (int i = 0; i < nf; i++) {
-        double nodi[9], yc[3];
+        double nodi[9], yc[3], nh[3];
         for (int t = 0; t < 3; t++)
             for (int q = 0; q < 3; q++) nodi[3 * t + q] = V[3 * F[3 * i + t] + q];
         tri_centroid(nodi, yc);
+        unit_normal(nodi, nh);
         cplx acc = a * x[i];
         for (int j = 0; j < nf; j++) {
             double nod[9];
             for (int t = 0; t < 3; t++)
                 for (int q = 0; q < 3; q++) nod[3 * t + q] = V[3 * F[3 * j + t] + q];
-            int sgl = (i == j);
-            cplx v = 0.0;
-            if (b != 0.0) v += b * (sgl ? elem_integral_sgl(k, nod, 0) : elem_integral(k, nod, yc, rule, 0));
-            if (c != 0.0) v += c * (sgl ? elem_integral_sgl(k, nod, 1) : elem_integral(k, nod, yc, rule, 1));
-            acc += v * x[j];
+            acc += pair_value(k, nod, yc, nh, i == j, rule, b, c, al) * x[j];
         }
         y[i] = acc;
     }
@@ -1163,36 +1300,35 @@ void orc_dense_apply(int nv, const double *V, int nf, const int *F, double k,
  * sums.  Used to check the transposed and adjoint operators on small meshes. */
 void orc_dense_matrix(int nv, const double *V, int nf, const int *F, double k,
                       double a_re, double a_im, double b_re, double b_im, double c_re, double c_im,
-                      int rule, double *out, int nthreads)
+                      double al_re, double al_im, int rule, double *out, int nthreads)
 {
     (void)nv;
     cplx *A = (cplx *)out;
-    cplx a = a_re + I * a_im, b = b_re + I * b_im, c = c_re + I * c_im;
+    cplx a = a_re + I * a_im, b = b_re + I * b_im, c = c_re + I * c_im, al = al_re + I * al_im;
 #pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) schedule(dynamic, 16)
     for (int i = 0; i < nf; i++) {
-        double nodi[9], yc[3];
+        double nodi[9], yc[3], nh[3];
         for (int t = 0; t < 3; t++)
             for (int q = 0; q < 3; q++) nodi[3 * t + q] = V[3 * F[3 * i + t] + q];
         tri_centroid(nodi, yc);
+        unit_normal(nodi, nh);
         for (int j = 0; j < nf; j++) {
             double nod[9];
             for (int t = 0; t < 3; t++)
                 for (int q = 0; q < 3; q++) nod[3 * t + q] = V[3 * F[3 * j + t] + q];
-            int sgl = (i == j);
-            cplx v = sgl ? a : 0.0;
-            if (b != 0.0) v += b * (sgl ? elem_integral_sgl(k, nod, 0) : elem_integral(k, nod, yc, rule, 0));
-            if (c != 0.0) v += c * (sgl ? elem_integral_sgl(k, nod, 1) : elem_integral(k, nod, yc, rule, 1));
+            cplx v = (i == j ? a : 0.0) + pair_value(k, nod, yc, nh, i == j, rule, b, c, al);
             A[(size_t)i * nf + j] = v;
         }
     }
 }
 
-void orc_far_field(int nv, const double *V, int nf, const int *F, double k, int rule,
-                   const double *pin, int npts, const double *pts, double *out, int nthreads)
+void orc_far_field(int nv, const double *V, int nf, const int *F, double k, double b_re, double b_im, double c_re,
+                   double c_im, int rule, const double *pin, int npts, const double *pts, double *out, int nthreads)
 {
     (void)nv;
     const cplx *p = (const cplx *)pin;
     cplx *o = (cplx *)out;
+    cplx b = b_re + I * b_im, c = c_re + I * c_im;
 #pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1)
     for (int t = 0; t < npts; t++) {
         cplx acc = 0.0;
@@ -1200,7 +1336,10 @@ void orc_far_field(int nv, const double *V, int nf, const int *F, double k, int 
             double nod[9];
             for (int u = 0; u < 3; u++)
                 for (int q = 0; q < 3; q++) nod[3 * u + q] = V[3 * F[3 * j + u] + q];
-            acc += p[j] * elem_integral(k, nod, pts + 3 * t, rule, 1);
+            cplx v = 0.0;
+            if (b != 0.0) v += b * elem_integral(k, nod, pts + 3 * t, rule, 0);
+            if (c != 0.0) v += c * elem_integral(k, nod, pts + 3 * t, rule, 1);
+            acc -= p[j] * v;
         }
         o[t] = acc;
     }
@@ -1231,6 +1370,43 @@ void orc_mie_rigid(double k, double a, int npts, const double *pts, double *out)
             cplx dhn = djn + I * dyn;
             cplx hr = jr[n] + I * yr[n];
             acc += -in * (2.0 * n + 1.0) * (djn / dhn) * hr * Pn;
+            in *= I;
+        }
+        o[t] = acc;
+    }
+    free(ja);
+}
+
+/* Mie series for a sphere of radius a with the locally reacting surface dp/dn = i k beta p
+ * (n the outward normal, e^{ikz} incident): p_s = sum_n (2n+1) i^n A_n h_n(kr) P_n(cos theta),
+ * A_n = -(j_n'(ka) - i beta j_n(ka)) / (h_n'(ka) - i beta h_n(ka)); beta = 0 is the rigid sphere. */
+void orc_mie_impedance(double k, double a, double beta_re, double beta_im, int npts, const double *pts, double *out)
+{
+    cplx *o = (cplx *)out;
+    cplx beta = beta_re + I * beta_im;
+    int N = (int)(k * a) + 30;
+    double *ja = (double *)malloc(sizeof(double) * (N + 2) * 4);
+    double *ya = ja + (N + 2), *jr = ya + (N + 2), *yr = jr + (N + 2);
+    double x = k * a;
+    orc_sph_jn(N + 2, x, ja);
+    orc_sph_yn(N + 2, x, ya);
+    for (int t = 0; t < npts; t++) {
+        const double *P = pts + 3 * t;
+        double r = sqrt(P[0] * P[0] + P[1] * P[1] + P[2] * P[2]);
+        double ct = P[2] / r;
+        orc_sph_jn(N + 2, k * r, jr);
+        orc_sph_yn(N + 2, k * r, yr);
+        cplx acc = 0.0, in = 1.0;
+        double Pnm2 = 0.0, Pnm1 = 0.0;
+        for (int n = 0; n <= N; n++) {
+            double Pn = (n == 0) ? 1.0 : (n == 1 ? ct : ((2.0 * n - 1.0) * ct * Pnm1 - (n - 1.0) * Pnm2) / n);
+            Pnm2 = Pnm1;
+            Pnm1 = Pn;
+            double djn = (n == 0) ? -ja[1] : ja[n - 1] - (n + 1.0) / x * ja[n];
+            double dyn = (n == 0) ? -ya[1] : ya[n - 1] - (n + 1.0) / x * ya[n];
+            cplx hn = ja[n] + I * ya[n], dhn = djn + I * dyn;
+            cplx An = -(djn - I * beta * ja[n]) / (dhn - I * beta * hn);
+            acc += in * (2.0 * n + 1.0) * An * (jr[n] + I * yr[n]) * Pn;
             in *= I;
         }
         o[t] = acc;

@@ -42,11 +42,14 @@ void orc_elem_dGdny(double k, const double *nod9, const double *nrml, const doub
 void orc_elem_hyper(double k, const double *nod9, const double *nrml, const double *y, int sgl, int nth, double *out);
 void orc_diff_coeff(double k, const double *coeff, int p, const double *nrml, double *out);
 
-/* FMM operator  y = a x + b L x + c M x  on collocation points at triangle centroids */
+void orc_elem_hyper_maue(double k, const double *nod9, const double *x, const double *nx, int rule, int sgl, double *out);
+
+/* FMM operator  y = a x + (1 + alpha d/dn_y)(b L + c M) x  on collocation points y at the
+ * triangle centroids (alpha: Burton-Miller coupling, 0 for the conventional operator) */
 typedef struct orc_fmm orc_fmm;
 orc_fmm *orc_fmm_create(int nv, const double *V, int nf, const int *F, double k,
                         double a_re, double a_im, double b_re, double b_im, double c_re, double c_im,
-                        int rule, int lmax, const int *nbox, const long long *boxes,
+                        double al_re, double al_im, int rule, int lmax, const int *nbox, const long long *boxes,
                         const int *elem_leaf, const int *p_level, double d, const double *pt_min,
                         int nthreads);
 void orc_fmm_apply(orc_fmm *f, const double *x, double *y);
@@ -56,22 +59,26 @@ void orc_fmm_destroy(orc_fmm *f);
 long long orc_fmm_num_sr(const orc_fmm *f, int l);
 long long orc_fmm_num_near(const orc_fmm *f);
 
-/* dense reference operator (all pairs by direct quadrature), same a, b, c */
+/* dense reference operator (all pairs by direct quadrature), same a, b, c, alpha */
 void orc_dense_apply(int nv, const double *V, int nf, const int *F, double k,
                      double a_re, double a_im, double b_re, double b_im, double c_re, double c_im,
-                     int rule, const double *x, double *y, int nthreads);
+                     double al_re, double al_im, int rule, const double *x, double *y, int nthreads);
 
 /* the same operator as an explicit row-major nf x nf matrix (entry (i, j): element j at
  * the centroid of element i) */
 void orc_dense_matrix(int nv, const double *V, int nf, const int *F, double k,
                       double a_re, double a_im, double b_re, double b_im, double c_re, double c_im,
-                      int rule, double *out, int nthreads);
+                      double al_re, double al_im, int rule, double *out, int nthreads);
 
-/* scattered field of a rigid body from surface pressure p: sum_e p_e int dG/dn_x(x, y) */
-void orc_far_field(int nv, const double *V, int nf, const int *F, double k, int rule,
+/* field of the operator's layer potentials at exterior points, -(b L + c M) p: the scattered
+ * pressure for the exterior problem (c = -1, b = dp/dn / p; rigid: b = 0) */
+void orc_far_field(int nv, const double *V, int nf, const int *F, double k, double b_re, double b_im, double c_re,
+                   double c_im, int rule,
                    const double *p, int npts, const double *pts, double *out, int nthreads);
 /* Mie series: scattered pressure of a rigid sphere (radius a) for exp(ikz) */
 void orc_mie_rigid(double k, double a, int npts, const double *pts, double *out);
+/* Mie series for the sphere with dp/dn = i k beta p (n outward) */
+void orc_mie_impedance(double k, double a, double beta_re, double beta_im, int npts, const double *pts, double *out);
 
 #ifdef __cplusplus
 }

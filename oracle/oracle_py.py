@@ -25,7 +25,7 @@ def lib():
         path = _build.build()
         L = ctypes.CDLL(path)
         L.orc_fmm_create.restype = ctypes.c_void_p
-        L.orc_fmm_create.argtypes = [ctypes.c_int, c_dp, ctypes.c_int, c_ip, ctypes.c_double] + [ctypes.c_double] * 6 + [
+        L.orc_fmm_create.argtypes = [ctypes.c_int, c_dp, ctypes.c_int, c_ip, ctypes.c_double] + [ctypes.c_double] * 8 + [
             ctypes.c_int, ctypes.c_int, c_ip, ctypes.POINTER(ctypes.c_longlong), c_ip, c_ip, ctypes.c_double, c_dp, ctypes.c_int]
         L.orc_fmm_apply.argtypes = [ctypes.c_void_p, c_dp, c_dp]
         L.orc_fmm_apply2.argtypes = [ctypes.c_void_p, c_dp, c_dp, ctypes.c_int]
@@ -34,12 +34,14 @@ def lib():
         L.orc_fmm_num_sr.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_fmm_num_near.restype = ctypes.c_longlong
         L.orc_fmm_num_near.argtypes = [ctypes.c_void_p]
-        L.orc_dense_apply.argtypes = [ctypes.c_int, c_dp, ctypes.c_int, c_ip, ctypes.c_double] + [ctypes.c_double] * 6 + [
+        L.orc_dense_apply.argtypes = [ctypes.c_int, c_dp, ctypes.c_int, c_ip, ctypes.c_double] + [ctypes.c_double] * 8 + [
             ctypes.c_int, c_dp, c_dp, ctypes.c_int]
-        L.orc_dense_matrix.argtypes = L.orc_dense_apply.argtypes[:12] + [c_dp, ctypes.c_int]
-        L.orc_far_field.argtypes = [ctypes.c_int, c_dp, ctypes.c_int, c_ip, ctypes.c_double, ctypes.c_int, c_dp,
-                                    ctypes.c_int, c_dp, c_dp, ctypes.c_int]
+        L.orc_dense_matrix.argtypes = L.orc_dense_apply.argtypes[:14] + [c_dp, ctypes.c_int]
+        L.orc_far_field.argtypes = [ctypes.c_int, c_dp, ctypes.c_int, c_ip, ctypes.c_double] + [ctypes.c_double] * 4 + [
+            ctypes.c_int, c_dp, ctypes.c_int, c_dp, c_dp, ctypes.c_int]
+        L.orc_elem_hyper_maue.argtypes = [ctypes.c_double, c_dp, c_dp, c_dp, ctypes.c_int, ctypes.c_int, c_dp]
         L.orc_mie_rigid.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, c_dp, c_dp]
+        L.orc_mie_impedance.argtypes = [ctypes.c_double] * 4 + [ctypes.c_int, c_dp, c_dp]
         for name in ("orc_rot_H", "orc_rot_H_recur"):
             getattr(L, name).argtypes = [ctypes.c_double, ctypes.c_int, c_dp]
         L.orc_coax.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, c_dp]
@@ -142,6 +144,16 @@ def elem_moments(k, nod, c, p, rule=0, deriv=False):
     return out
 
 
+def elem_hyper_maue(k, nod, x, nx, rule=0, sgl=False):
+    """int_T d2G/dn_x dn_y dS in the regularised (Maue) form: k^2 (nx.nT) int G - the line
+    integral of (nx x grad G) around T; the finite part when x is T's centroid (sgl)."""
+    out = np.zeros(2)
+    lib().orc_elem_hyper_maue(k, _d(np.ascontiguousarray(nod, dtype=np.float64).reshape(9)),
+                              _d(np.ascontiguousarray(x, dtype=np.float64)), _d(np.ascontiguousarray(nx, dtype=np.float64)),
+                              rule, 1 if sgl else 0, _d(out))
+    return complex(out[0], out[1])
+
+
 def dirdev_R(k, n, m, nrml, x):
     """Directional derivative of R_n^m at x along nrml (``dirDev_R``, integral.cu:284-331)."""
     out = np.zeros(2)
@@ -213,7 +225,7 @@ def tree_for_fmm(V, F, depth=None, s=5):
 class FMM:
     """FP64 CPU FMM operator  y = a x + b L x + c M x  (test oracle)."""
 
-    def __init__(self, V, F, k, tree, p_levels, a=0.0, b=0.0, c=0.0, rule=0, nthreads=None):
+    def __init__(self, V, F, k, tree, p_levels, a=0.0, b=0.0, c=0.0, rule=0, nthreads=None, alpha=0.0):
         L = lib()
         self.V = np.ascontiguousarray(V, dtype=np.float64)
         self.F = np.ascontiguousarray(F, dtype=np.int32)
@@ -226,9 +238,9 @@ class FMM:
         p = np.ascontiguousarray(p_levels, dtype=np.int32)
         pt_min = np.ascontiguousarray(tree["pt_min"], dtype=np.float64)
         nthreads = nthreads or os.cpu_count() or 1
-        a, b, c = complex(a), complex(b), complex(c)
+        a, b, c, al = complex(a), complex(b), complex(c), complex(alpha)
         self.h = L.orc_fmm_create(len(self.V), _d(self.V), self.nf, _i(self.F), k, a.real, a.imag, b.real, b.imag,
-                                  c.real, c.imag, rule, lmax, _i(nbox), boxes.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                  c.real, c.imag, al.real, al.imag, rule, lmax, _i(nbox), boxes.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
                                   _i(elem_leaf), _i(p), tree["d"], _d(pt_min), nthreads)
         self.lmax = lmax
 
@@ -251,35 +263,41 @@ class FMM:
             self.h = None
 
 
-def dense_apply(V, F, k, x, a=0.0, b=0.0, c=0.0, rule=0, nthreads=None):
+def dense_apply(V, F, k, x, a=0.0, b=0.0, c=0.0, rule=0, nthreads=None, alpha=0.0):
     V = np.ascontiguousarray(V, dtype=np.float64)
     F = np.ascontiguousarray(F, dtype=np.int32)
     x = np.ascontiguousarray(x, dtype=np.complex128)
     y = np.zeros(len(F), dtype=np.complex128)
-    a, b, c = complex(a), complex(b), complex(c)
-    lib().orc_dense_apply(len(V), _d(V), len(F), _i(F), k, a.real, a.imag, b.real, b.imag, c.real, c.imag, rule,
+    a, b, c, al = complex(a), complex(b), complex(c), complex(alpha)
+    lib().orc_dense_apply(len(V), _d(V), len(F), _i(F), k, a.real, a.imag, b.real, b.imag, c.real, c.imag, al.real,
+                          al.imag, rule,
                           _d(x.view(np.float64)), _d(y.view(np.float64)), nthreads or os.cpu_count() or 1)
     return y
 
 
-def dense_matrix(V, F, k, a=0.0, b=0.0, c=0.0, rule=0, nthreads=None):
+def dense_matrix(V, F, k, a=0.0, b=0.0, c=0.0, rule=0, nthreads=None, alpha=0.0):
     """The dense operator of dense_apply as an explicit complex nf x nf matrix (small meshes)."""
     V = np.ascontiguousarray(V, dtype=np.float64)
     F = np.ascontiguousarray(F, dtype=np.int32)
     A = np.zeros((len(F), len(F)), dtype=np.complex128)
-    a, b, c = complex(a), complex(b), complex(c)
-    lib().orc_dense_matrix(len(V), _d(V), len(F), _i(F), k, a.real, a.imag, b.real, b.imag, c.real, c.imag, rule,
+    a, b, c, al = complex(a), complex(b), complex(c), complex(alpha)
+    lib().orc_dense_matrix(len(V), _d(V), len(F), _i(F), k, a.real, a.imag, b.real, b.imag, c.real, c.imag, al.real,
+                           al.imag, rule,
                            _d(A.view(np.float64)), nthreads or os.cpu_count() or 1)
     return A
 
 
-def far_field(V, F, k, p_surf, pts, rule=0, nthreads=None):
+def far_field(V, F, k, p_surf, pts, rule=0, nthreads=None, b=0.0, c=-1.0):
+    """-(b L + c M) p at the points pts: the scattered pressure of the exterior problem
+    (c = -1, b = dp/dn / p on the surface; the rigid body b = 0)."""
     V = np.ascontiguousarray(V, dtype=np.float64)
     F = np.ascontiguousarray(F, dtype=np.int32)
     p_surf = np.ascontiguousarray(p_surf, dtype=np.complex128)
     pts = np.ascontiguousarray(pts, dtype=np.float64)
     out = np.zeros(len(pts), dtype=np.complex128)
-    lib().orc_far_field(len(V), _d(V), len(F), _i(F), k, rule, _d(p_surf.view(np.float64)), len(pts), _d(pts),
+    b, c = complex(b), complex(c)
+    lib().orc_far_field(len(V), _d(V), len(F), _i(F), k, b.real, b.imag, c.real, c.imag, rule,
+                        _d(p_surf.view(np.float64)), len(pts), _d(pts),
                         _d(out.view(np.float64)), nthreads or os.cpu_count() or 1)
     return out
 
@@ -288,4 +306,13 @@ def mie_rigid(k, a, pts):
     pts = np.ascontiguousarray(pts, dtype=np.float64)
     out = np.zeros(len(pts), dtype=np.complex128)
     lib().orc_mie_rigid(k, a, len(pts), _d(pts), _d(out.view(np.float64)))
+    return out
+
+
+def mie_impedance(k, a, beta, pts):
+    """Scattered pressure of a sphere with dp/dn = i k beta p (n outward) for exp(ikz)."""
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    out = np.zeros(len(pts), dtype=np.complex128)
+    beta = complex(beta)
+    lib().orc_mie_impedance(k, a, beta.real, beta.imag, len(pts), _d(pts), _d(out.view(np.float64)))
     return out
