@@ -25,6 +25,18 @@ struct RcrList {
     int tc = 8, shc = 0;          // columns per item; rotation/coaxial blocks staged in shared memory
 };
 
+// M2L of one level on the tensor cores (tc_m2l.cu): the level's 316 translation operators
+// stored densely, real-embedded and split into TF32 hi/lo parts in the layout the MMA reads.
+struct TcM2L {
+    int on = 0;                   // this level's mixed M2L runs on the tensor cores
+    int KC = 40, nch = 0, nhalf = 1, CH = 0, Nmma = 0;
+    float *B = nullptr;           // [dir][half][chunk][hi, lo][Nmma x KC core-matrix tile]
+    size_t B_bytes = 0;
+    int4 *items = nullptr;        // (direction, first column, count, 0), 128 columns each
+    size_t items_cap = 0;
+    int n_items = 0, items_nrhs = 0;
+};
+
 struct LevelDev {
     int nb = 0, p = 0;
     int *parent = nullptr;        // [nb], index in level l-1 (l > lmin)
@@ -44,6 +56,7 @@ struct LevelDev {
     // batched passes of the mixed path: M2L of this level, M2M (this level -> parents),
     // L2L (parents -> this level)
     RcrList m2l, m2m, l2l;
+    TcM2L tc;
 };
 
 struct Timer {
@@ -88,6 +101,7 @@ struct Plan {
     cudaEvent_t fork_ev = nullptr, join_ev[NSIDE] = {};
     cudaGraphExec_t graph_exec = nullptr; // captured mixed translation passes for graph_nrhs columns
     int graph_nrhs = 0, graph_seen = 0;
+    int *tc_err = nullptr;        // set by the tensor-core M2L when one of its waits gives up
     size_t device_bytes = 0;
     char mixed_note[160] = "plan was created without build_mixed";
     double setup_seconds = 0.0;
@@ -134,6 +148,12 @@ void drop_graph(Plan *P);
 
 enum { PASS_M2M = 0, PASS_M2L = 1, PASS_L2L = 2 };
 int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st);
+
+// tc_m2l.cu
+int gen_dense_m2l(Plan *P, int l, double2 *T);   // passes.cu
+int tune_tc_m2l(Plan *P);
+int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st);
+int check_tc_error(Plan *P);
 
 // batched.cu
 int build_rcr_lists(Plan *P);

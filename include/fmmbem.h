@@ -76,6 +76,10 @@ typedef struct {
     size_t device_bytes;
     double setup_seconds;
     int m2l_columns[FMM_MAX_LEVEL + 1];  /* mixed path: M2L translations per CTA tile (0 without mixed tables) */
+    int m2l_tensor[FMM_MAX_LEVEL + 1];   /* mixed path: 1 where the level's M2L runs on the tensor cores
+                                            (tcgen05, split TF32, dense per-direction operators; levels with
+                                            p <= 16 where plan-time timing found it faster, or all of them
+                                            with FMMBEM_TENSOR_M2L=1; none with FMMBEM_TENSOR_M2L=0) */
 } fmm_info;
 
 typedef struct fmm_plan fmm_plan;

@@ -1,0 +1,82 @@
+"""The tensor-core M2L (tcgen05, split TF32, dense per-direction operators) of the mixed path:
+forced on with FMMBEM_TENSOR_M2L=1, against the FP64 matvec, the SIMT tiles and the oracle,
+for even and odd orders, one and several right-hand sides, and the Burton-Miller operator."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+K1 = 2 * np.pi * 1000 / 343.0
+K2 = 2 * np.pi * 8000 / 343.0
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def make_plan(fm, mode, *args, **kw):
+    old = os.environ.get("FMMBEM_TENSOR_M2L")
+    os.environ["FMMBEM_TENSOR_M2L"] = mode
+    try:
+        return fm.Plan(*args, **kw)
+    finally:
+        if old is None:
+            del os.environ["FMMBEM_TENSOR_M2L"]
+        else:
+            os.environ["FMMBEM_TENSOR_M2L"] = old
+
+
+# (p = 16 at 1 kHz would leave the FP32 range in the coaxial tables: no mixed path there)
+@pytest.mark.parametrize("p,k", [(8, K1), (9, K1), (13, K1), (16, K2)])
+def test_tensor_m2l_matches_fp64_and_oracle(fm, oracle, p, k):
+    V, F = fm.icosphere(3, 0.1)
+    kw = dict(k=k, depth=3, p_levels={2: p, 3: p}, rule=1, a=0.5, b=0.0, c=-1.0)
+    plan = make_plan(fm, "1", V, F, **kw)
+    assert all(plan.info.m2l_tensor[l] == 1 for l in (2, 3))
+    simt = make_plan(fm, "0", V, F, **kw)
+    assert not any(simt.info.m2l_tensor[l] for l in range(13))
+    rng = np.random.default_rng(p)
+    x = rng.standard_normal(plan.nf) + 1j * rng.standard_normal(plan.nf)
+    y64 = plan.matvec(x, fm.FMM_FP64)
+    ym = plan.matvec(x, fm.FMM_MIXED)
+    assert rel(ym, y64) < 1e-5
+    assert rel(ym, simt.matvec(x, fm.FMM_MIXED)) < 1e-5
+    T = oracle.tree_for_fmm(V, F, depth=3)
+    assert rel(ym, oracle.FMM(V, F, k, T, [p, p], a=0.5, b=0.0, c=-1.0, rule=1).apply(x)) < 1e-5
+    # several right-hand sides in one pass, and the captured graph on the repeat
+    X = np.stack([x, 1j * x, rng.standard_normal(plan.nf) + 0j])
+    for _ in range(3):
+        Y = plan.matvec(X.reshape(-1), fm.FMM_MIXED).reshape(3, -1)
+        for r in range(3):
+            assert rel(Y[r], plan.matvec(X[r], fm.FMM_FP64)) < 1e-5
+    plan.close()
+    simt.close()
+
+
+def test_tensor_m2l_on_the_81920_triangle_workload(fm):
+    """cfg2 orders 40/30/20/14/10: the levels with p <= 16 (14 and 10) on the tensor cores."""
+    V, F = fm.icosphere(6, 0.3)
+    P2 = {2: 40, 3: 30, 4: 20, 5: 14, 6: 10}
+    plan = make_plan(fm, "1", V, F, k=K2, depth=6, p_levels=P2, rule=0, a=0.5, b=0.0, c=-1.0)
+    assert [plan.info.m2l_tensor[l] for l in range(2, 7)] == [0, 0, 0, 1, 1]
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(plan.nf) + 1j * rng.standard_normal(plan.nf)
+    y64 = plan.matvec(x, fm.FMM_FP64)
+    assert rel(plan.matvec(x, fm.FMM_MIXED), y64) < 1e-6
+    xs, it, rr, ok = plan.gmres(plan.plane_wave(), tol=1e-6, maxit=500, restart=60, precision=fm.FMM_MIXED)
+    assert ok
+    plan.close()
+
+
+def test_tensor_m2l_with_burton_miller(fm, oracle):
+    V, F = fm.icosphere(3, 0.1)
+    alpha = 1j / K1
+    kw = dict(k=K1, depth=3, p_levels={2: 10, 3: 10}, rule=1, a=0.5, b=0.0, c=-1.0, alpha=alpha)
+    plan = make_plan(fm, "1", V, F, **kw)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(plan.nf) + 1j * rng.standard_normal(plan.nf)
+    T = oracle.tree_for_fmm(V, F, depth=3)
+    yo = oracle.FMM(V, F, K1, T, [10, 10], a=0.5, b=0.0, c=-1.0, rule=1, alpha=alpha).apply(x)
+    assert rel(plan.matvec(x, fm.FMM_MIXED), yo) < 1e-5
+    plan.close()
