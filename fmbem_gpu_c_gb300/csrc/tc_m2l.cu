@@ -10,13 +10,19 @@
 // k and o running over interleaved (re, im) parts, so A is the expansion as it lies in memory.
 // Split TF32 (3 products hi*hi + hi*lo + lo*hi of 11-bit halves) gives FP32-level accuracy.
 //
-// One CTA per (128-translation tile, output half): 256 threads gather A and copy B, chunk by
-// chunk (KC of K), into two shared-memory stages in the no-swizzle K-major core-matrix layout;
-// one thread issues the MMAs into a TMEM accumulator (128 lanes x Nmma columns) and commits
-// them to the stage's mbarrier; at the end the 8 warps read the accumulator back
-// (tcgen05.ld), stage it in shared memory and add it into the destination local expansions
-// with coalesced FP32 atomics.  Every wait has a time limit; a wait that gives up sets the
-// plan's error flag and the CTA skips its output.
+// A persistent, warp-specialised kernel (one CTA per SM, 10 warps) runs over the tiles
+// (128 translations x one output half):
+//   warp 0     issues the MMAs (one thread) into one of two TMEM accumulators (2 x 256 columns)
+//              and commits each K chunk to its stage's "empty" barrier, each tile to its
+//              accumulator's "full" barrier;
+//   warp 1     copies the operator's K chunks (hi and lo tiles, contiguous) with cp.async.bulk;
+//   warps 2-5  gather the source expansions, one row (translation) per thread, split them into
+//              TF32 hi / lo and store them in the no-swizzle K-major core-matrix layout;
+//   warps 6-9  read a finished accumulator (tcgen05.ld, one TMEM lane quarter per warp), stage
+//              32 columns at a time in shared memory and add them into the destination local
+//              expansions with coalesced FP32 atomics, overlapping the next tile's MMAs.
+// Four shared-memory stages of KC = 16; every wait has a time limit, after which the thread sets
+// the plan's error flag and stops.
 #include "plan.h"
 #include <algorithm>
 #include <cstdlib>
@@ -25,29 +31,33 @@
 
 namespace fmm {
 
-constexpr int TC_M = 128;          // translations per tile (MMA M)
-constexpr int TC_THREADS = 256;
+constexpr int TC_M = 128;               // translations per tile (MMA M)
+constexpr int TC_KC = 16;               // K per stage (2 MMA K-steps of 8)
+constexpr int TC_STAGES = 4;
+constexpr int TC_THREADS = 320;         // 10 warps
 constexpr int TC_MAXP = 16;
+constexpr int TC_EPI_LD = 33;           // staging row stride (floats) of the epilogue
 constexpr size_t TC_SMEM_MAX = 232448;  // 227 KB of dynamic shared memory per CTA
-constexpr size_t TC_EXTRA = 16 + 16 + 2 * TC_M * sizeof(int);
 
 struct TcPass {
     const int4 *items;
     const int *g_src, *g_dst;
     int nrhs, nsrc, ndst;
-    int p, K, KC, nch, nhalf, CH, Nmma;
+    int p, K, nch, nhalf, CH, Nmma, ntiles;
     const float *B;
     const float2 *src;
     float2 *dst;
     int *err;
 };
 
-static size_t tc_stage_bytes(int KC, int Nmma) { return (size_t)8 * KC * (TC_M + Nmma); }
-static size_t tc_smem_bytes(int KC, int Nmma) { return 2 * tc_stage_bytes(KC, Nmma) + TC_EXTRA; }
+static size_t tc_stage_bytes(int Nmma) { return (size_t)8 * TC_KC * (TC_M + Nmma); }
+static size_t tc_smem_bytes(int Nmma)
+{
+    return TC_STAGES * tc_stage_bytes(Nmma) + 4 * 32 * TC_EPI_LD * sizeof(float) + (2 * TC_STAGES + 4) * 8 + 16;
+}
 
-// Output halves, MMA width and K chunk for order p: each half holds CH coefficients
-// (2 CH real outputs, Nmma = that rounded up to 16, <= 256); KC from {40, 32} with the
-// least padding of K = 2p^2 that fits two stages.
+// Output halves and MMA width for order p: each half holds CH coefficients (2 CH real outputs,
+// Nmma = that rounded up to 16, <= 256); K = 2p^2 in chunks of 16.
 static bool tc_geometry(int p, TcM2L &g)
 {
     if (p < 4 || p > TC_MAXP) return false;
@@ -57,15 +67,9 @@ static bool tc_geometry(int p, TcM2L &g)
         g.Nmma = (2 * g.CH + 15) / 16 * 16;
         if (g.Nmma <= 256) break;
     }
-    int best = 0;
-    for (int kc : {40, 32}) {
-        if (tc_smem_bytes(kc, g.Nmma) > TC_SMEM_MAX) continue;
-        int kp = (K + kc - 1) / kc * kc;
-        if (!best || kp < (K + best - 1) / best * best) best = kc;
-    }
-    if (!best) return false;
-    g.KC = best;
-    g.nch = (K + best - 1) / best;
+    if (tc_smem_bytes(g.Nmma) > TC_SMEM_MAX) return false;
+    g.KC = TC_KC;
+    g.nch = (K + TC_KC - 1) / TC_KC;
     return true;
 }
 
@@ -102,132 +106,221 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
     }
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// destination / source expansion of row r of tile (it): column e = translation t x nrhs + r
+__device__ __forceinline__ int tile_box(const TcPass &ps, int4 it, int r, bool source)
+{
+    if (r >= it.z) return -1;
+    int e = it.y + r, t = e / ps.nrhs, rr = e - t * ps.nrhs;
+    return source ? ps.g_src[t] + rr * ps.nsrc : ps.g_dst[t] + rr * ps.ndst;
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const int KC = ps.KC, Nmma = ps.Nmma, K = ps.K, P2 = ps.p * ps.p;
-    const uint32_t tA = (uint32_t)TC_M * KC * 4, tB = (uint32_t)Nmma * KC * 4, stage = 2 * tA + 2 * tB;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + 2 * stage);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
-    int *s_src = reinterpret_cast<int *>(tslot + 4), *s_dst = s_src + TC_M;
+    const int Nmma = ps.Nmma, K = ps.K, P2 = ps.p * ps.p, nch = ps.nch;
+    const uint32_t tA = (uint32_t)TC_M * TC_KC * 4, tB = (uint32_t)Nmma * TC_KC * 4, stage = 2 * tA + 2 * tB;
+    float *epi = reinterpret_cast<float *>(smem + TC_STAGES * stage);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(epi + 4 * 32 * TC_EPI_LD);
+    uint64_t *full = bars, *empty = bars + TC_STAGES, *accf = bars + 2 * TC_STAGES, *acce = accf + 2;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(acce + 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int item = blockIdx.x / ps.nhalf, h = blockIdx.x - item * ps.nhalf;
-    const int4 it = ps.items[item];
 
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(256));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(512));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar + 1)));
-    }
-    if (tid < TC_M) {
-        // column e = translation t x nrhs + right-hand side r, as in the batched tiles
-        bool v = tid < it.z;
-        int e = it.y + tid, t = e / ps.nrhs, r = e - t * ps.nrhs;
-        s_src[tid] = v ? ps.g_src[t] + r * ps.nsrc : -1;
-        s_dst[tid] = v ? ps.g_dst[t] + r * ps.ndst : -1;
+    if (tid == 32) {
+        for (int s = 0; s < TC_STAGES; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 5;" ::"r"(smem_u32(full + s)));   // 4 A warps + B copy
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)));  // MMA commit
+        }
+        for (int a = 0; a < 2; a++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(accf + a)));   // MMA commit
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(smem_u32(acce + a)));   // 4 epilogue warps
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = *tslot;
-    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Nmma >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
-    const uint32_t lbo = 128, sbo = 32 * KC;
-    const float *Bd = ps.B + (size_t)(it.x * ps.nhalf + h) * ps.nch * 2 * Nmma * KC;
-    const float *srcf = reinterpret_cast<const float *>(ps.src);
     bool ok = true;
 
-    for (int c = 0; c < ps.nch; c++) {
-        const int buf = c & 1;
-        unsigned char *Ahi = smem + buf * stage, *Alo = Ahi + tA, *Bst = Ahi + 2 * tA;
-        if (c >= 2) ok = mbar_wait(smem_u32(mbar + buf), ((c >> 1) - 1) & 1) && ok;
-        // A: 4 consecutive k of one row per task -> one 16-byte core row, split into hi / lo
-        const int kq = KC / 4;
-        for (int task = tid; task < TC_M * kq; task += TC_THREADS) {
-            int r = task / kq, kg = task - r * kq, k0 = c * KC + 4 * kg, s = s_src[r];
-            float x[4] = {0.f, 0.f, 0.f, 0.f};
-            if (s >= 0) {
-                const float *row = srcf + (size_t)s * K + k0;
-                if (k0 + 1 < K) {
-                    float2 v = __ldg(reinterpret_cast<const float2 *>(row));
-                    x[0] = v.x; x[1] = v.y;
+    if (warp == 0) {
+        // ---------------------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc =
+                (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Nmma >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+            const uint32_t lbo = 128, sbo = 32 * TC_KC;
+            int g = 0, i = 0;
+            for (int q = blockIdx.x; q < ps.ntiles && ok; q += gridDim.x, i++) {
+                const int a = i & 1;
+                ok = mbar_wait(smem_u32(acce + a), ((i >> 1) & 1) ^ 1);
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t d_tmem = tmem + (uint32_t)(a * 256);
+                for (int c = 0; c < nch && ok; c++, g++) {
+                    const int s = g % TC_STAGES;
+                    ok = mbar_wait(smem_u32(full + s), (g / TC_STAGES) & 1);
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t a_hi = smem_u32(smem + s * stage), a_lo = a_hi + tA, b_hi = a_hi + 2 * tA, b_lo = b_hi + tB;
+#pragma unroll
+                    for (int ks = 0; ks < TC_KC / 8; ks++)
+#pragma unroll
+                        for (int pass = 0; pass < 3; pass++) {
+                            uint64_t ad = smem_desc((pass == 2 ? a_lo : a_hi) + ks * 256, lbo, sbo);
+                            uint64_t bd = smem_desc((pass == 1 ? b_lo : b_hi) + ks * 256, lbo, sbo);
+                            uint32_t acc = (c > 0 || ks > 0 || pass > 0) ? 1u : 0u;
+                            asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t"
+                                         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, q;\n\t}" ::"r"(d_tmem),
+                                         "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                        }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_u32(empty + s))
+                                 : "memory");
                 }
-                if (k0 + 3 < K) {
-                    float2 v = __ldg(reinterpret_cast<const float2 *>(row + 2));
-                    x[2] = v.x; x[3] = v.y;
+                if (ok)
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_u32(accf + a))
+                                 : "memory");
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------------------- operator copies
+        if (lane == 0) {
+            const uint32_t bytes = 2 * tB;
+            int g = 0;
+            for (int q = blockIdx.x; q < ps.ntiles && ok; q += gridDim.x) {
+                const int item = q / ps.nhalf, h = q - item * ps.nhalf;
+                const int4 it = ps.items[item];
+                const float *Bd = ps.B + (size_t)(it.x * ps.nhalf + h) * nch * 2 * Nmma * TC_KC;
+                for (int c = 0; c < nch && ok; c++, g++) {
+                    const int s = g % TC_STAGES;
+                    ok = mbar_wait(smem_u32(empty + s), ((g / TC_STAGES) & 1) ^ 1);
+                    if (!ok) break;
+                    const uint32_t bar = smem_u32(full + s), dst = smem_u32(smem + s * stage + 2 * tA);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+                    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                                 "l"(Bd + (size_t)c * 2 * Nmma * TC_KC), "r"(bytes), "r"(bar)
+                                 : "memory");
                 }
             }
-            float4 hi, lo;
-            hi.x = tf32_trunc(x[0]); lo.x = tf32_trunc(x[0] - hi.x);
-            hi.y = tf32_trunc(x[1]); lo.y = tf32_trunc(x[1] - hi.y);
-            hi.z = tf32_trunc(x[2]); lo.z = tf32_trunc(x[2] - hi.z);
-            hi.w = tf32_trunc(x[3]); lo.w = tf32_trunc(x[3] - hi.w);
-            uint32_t o = core_off(r, 4 * kg, KC);
-            *reinterpret_cast<float4 *>(Ahi + o) = hi;
-            *reinterpret_cast<float4 *>(Alo + o) = lo;
         }
-        // B: the chunk's hi and lo tiles are stored contiguously in this layout
-        const float4 *bsrc = reinterpret_cast<const float4 *>(Bd + (size_t)c * 2 * Nmma * KC);
-        float4 *bdst = reinterpret_cast<float4 *>(Bst);
-        for (int i = tid; i < (int)(2 * tB / 16); i += TC_THREADS) bdst[i] = __ldg(bsrc + i);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t a_hi = smem_u32(Ahi), a_lo = a_hi + tA, b_hi = smem_u32(Bst), b_lo = b_hi + tB;
-            for (int ks = 0; ks < KC / 8; ks++)
-                for (int pass = 0; pass < 3; pass++) {
-                    uint64_t ad = smem_desc((pass == 2 ? a_lo : a_hi) + ks * 256, lbo, sbo);
-                    uint64_t bd = smem_desc((pass == 1 ? b_lo : b_hi) + ks * 256, lbo, sbo);
-                    uint32_t acc = (c > 0 || ks > 0 || pass > 0) ? 1u : 0u;
-                    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %4, 0;\n\t"
-                                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, q;\n\t}" ::"r"(tmem),
-                                 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-                }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(mbar + buf))
-                         : "memory");
-        }
-    }
-    {
-        const int last = ps.nch - 1;
-        ok = mbar_wait(smem_u32(mbar + (last & 1)), (last >> 1) & 1) && ok;
-    }
-    ok = __syncthreads_and(ok);
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    float *sD = reinterpret_cast<float *>(smem);
-    const int ld = Nmma + 1;
-    if (ok) {
-        // accumulator -> shared memory: warp w reads lanes 32 (w % 4)..+31 (its rows), warps
-        // 0-3 the first half of the columns, warps 4-7 the second
-        const int wq = warp & 3, row = wq * 32 + lane, half = Nmma / 2, c0 = (warp >> 2) * half;
-        for (int cc = c0; cc < c0 + half; cc += 8) {
-            uint32_t v[8];
-            uint32_t ta = tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)cc;
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
-                         : "r"(ta));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    } else if (warp < 6) {
+        // ---------------------------------------------------------------- source gather
+        // one row (translation) per thread; the loads of the next two chunks are in flight
+        // while a chunk waits for its stage and is split and stored
+        const int r = tid - 64;
+        const float *srcf = reinterpret_cast<const float *>(ps.src);
+        const bool vec4 = (K & 3) == 0;
+        int g = 0;
+        for (int q = blockIdx.x; q < ps.ntiles && ok; q += gridDim.x) {
+            const int item = q / ps.nhalf;
+            const int sb = tile_box(ps, ps.items[item], r, true);
+            const float *row = srcf + (size_t)(sb < 0 ? 0 : sb) * K;
+            auto load = [&](float(&x)[TC_KC], int c) {
+                const int k0 = c * TC_KC;
 #pragma unroll
-            for (int j = 0; j < 8; j++) sD[row * ld + cc + j] = __uint_as_float(v[j]);
+                for (int j = 0; j < TC_KC; j += 4) {
+                    const int k = k0 + j;
+                    if (sb >= 0 && vec4 && k + 3 < K) {
+                        float4 v = __ldg(reinterpret_cast<const float4 *>(row + k));
+                        x[j] = v.x; x[j + 1] = v.y; x[j + 2] = v.z; x[j + 3] = v.w;
+                    } else {
+                        float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
+                        if (sb >= 0 && k + 1 < K) v0 = __ldg(reinterpret_cast<const float2 *>(row + k));
+                        if (sb >= 0 && k + 3 < K) v1 = __ldg(reinterpret_cast<const float2 *>(row + k + 2));
+                        x[j] = v0.x; x[j + 1] = v0.y; x[j + 2] = v1.x; x[j + 3] = v1.y;
+                    }
+                }
+            };
+            auto store = [&](const float(&x)[TC_KC], int gg) -> bool {
+                const int s = gg % TC_STAGES;
+                if (!mbar_wait(smem_u32(empty + s), ((gg / TC_STAGES) & 1) ^ 1)) return false;
+                unsigned char *Ahi = smem + s * stage, *Alo = Ahi + tA;
+#pragma unroll
+                for (int j = 0; j < TC_KC; j += 4) {
+                    float4 hi, lo;
+                    hi.x = tf32_trunc(x[j]); lo.x = tf32_trunc(x[j] - hi.x);
+                    hi.y = tf32_trunc(x[j + 1]); lo.y = tf32_trunc(x[j + 1] - hi.y);
+                    hi.z = tf32_trunc(x[j + 2]); lo.z = tf32_trunc(x[j + 2] - hi.z);
+                    hi.w = tf32_trunc(x[j + 3]); lo.w = tf32_trunc(x[j + 3] - hi.w);
+                    const uint32_t o = core_off(r, j, TC_KC);
+                    *reinterpret_cast<float4 *>(Ahi + o) = hi;
+                    *reinterpret_cast<float4 *>(Alo + o) = lo;
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(full + s));
+                return true;
+            };
+            float xa[TC_KC], xb[TC_KC], xc[TC_KC];
+            load(xa, 0);
+            if (nch > 1) load(xb, 1);
+            for (int c = 0; c < nch && ok; c += 3) {
+                if (c + 2 < nch) load(xc, c + 2);
+                ok = store(xa, g + c);
+                if (!ok || c + 1 >= nch) break;
+                if (c + 3 < nch) load(xa, c + 3);
+                ok = store(xb, g + c + 1);
+                if (!ok || c + 2 >= nch) break;
+                if (c + 4 < nch) load(xb, c + 4);
+                ok = store(xc, g + c + 2);
+            }
+            g += nch;
         }
-    } else if (tid == 0) {
-        atomicExch(ps.err, 1);
+    } else {
+        // ---------------------------------------------------------------- epilogue
+        const int wq = warp & 3;  // TMEM lane quarter of this warp
+        float *st = epi + (warp - 6) * 32 * TC_EPI_LD;
+        int i = 0;
+        for (int q = blockIdx.x; q < ps.ntiles && ok; q += gridDim.x, i++) {
+            const int a = i & 1, item = q / ps.nhalf, h = q - item * ps.nhalf;
+            const int dbox = tile_box(ps, ps.items[item], wq * 32 + lane, false);
+            const int co0 = h * ps.CH, nco = min(ps.CH, P2 - co0);
+            ok = mbar_wait(smem_u32(accf + a), (i >> 1) & 1);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            for (int cb = 0; cb < Nmma; cb += 32) {
+                uint32_t v[32];
+                const uint32_t ta = tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(a * 256 + cb);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                               "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                               "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]),
+                               "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
+                               "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                             : "r"(ta));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int j = 0; j < 32; j++) st[lane * TC_EPI_LD + j] = __uint_as_float(v[j]);
+                __syncwarp();
+                // two rows per step, 16 coefficients (32 columns) per row
+                const int jc = lane & 15, c2 = cb + 2 * jc;
+#pragma unroll 4
+                for (int rp = 0; rp < 16; rp++) {
+                    const int rr = 2 * rp + (lane >> 4);
+                    const int d = __shfl_sync(0xffffffffu, dbox, rr);
+                    if (d >= 0 && c2 < 2 * nco)
+                        atomicAdd(ps.dst + (size_t)d * P2 + co0 + c2 / 2,
+                                  make_float2(st[rr * TC_EPI_LD + 2 * jc], st[rr * TC_EPI_LD + 2 * jc + 1]));
+                }
+                __syncwarp();
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(acce + a));
+        }
     }
+    if (!ok) atomicExch(ps.err, 1);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
-    if (!ok) return;
-    // coalesced adds into the destination locals: one row (translation) per warp at a time
-    const int co0 = h * ps.CH, nco = min(ps.CH, P2 - co0);
-    for (int r = warp; r < TC_M; r += TC_THREADS / 32) {
-        const int d = s_dst[r];
-        if (d < 0) continue;
-        float2 *out = ps.dst + (size_t)d * P2 + co0;
-        for (int j = lane; j < nco; j += 32) atomicAdd(out + j, make_float2(sD[r * ld + 2 * j], sD[r * ld + 2 * j + 1]));
-    }
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
 // The real-embedded operators of one level, split into TF32 hi/lo, in the tile layout:
@@ -321,20 +414,28 @@ int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st)
     ps.ndst = L.nb;
     ps.p = L.p;
     ps.K = 2 * L.p * L.p;
-    ps.KC = g.KC;
     ps.nch = g.nch;
     ps.nhalf = g.nhalf;
     ps.CH = g.CH;
     ps.Nmma = g.Nmma;
+    ps.ntiles = g.n_items * g.nhalf;
     ps.B = g.B;
     ps.src = L.Cm32;
     ps.dst = L.Dl32;
     ps.err = P->tc_err;
-    size_t sm = tc_smem_bytes(g.KC, g.Nmma);
+    size_t sm = tc_smem_bytes(g.Nmma);
     static size_t attr = 0;
     e = raise_smem_limit((const void *)m2l_tc_kernel, sm, &attr);
     if (e) return e;
-    m2l_tc_kernel<<<g.n_items * g.nhalf, TC_THREADS, sm, st>>>(ps);
+    // persistent: one CTA per SM (its shared memory and 512 TMEM columns take the SM)
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 152;
+    }
+    m2l_tc_kernel<<<std::min(ps.ntiles, nsm), TC_THREADS, sm, st>>>(ps);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
