@@ -151,8 +151,9 @@ def peaks():
 
 
 def ncu_traffic():
-    """DRAM bytes of the dominant kernel per matvec (all its launches) from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "rcr_tile_kernel_traffic_cfg2.md")
+    """DRAM bytes of the translation passes per matvec (all launches of rcr_tile_kernel and
+    m2l_tc_kernel) from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "translation_passes_traffic_cfg2.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -286,6 +287,31 @@ def gpu_arm(args, world, rank, local):
     rcr_ms = float(np.mean(kernel_ms["translations"]))  # the M2M/M2L/L2L phase as a whole
     bf16_peak, hbm_peak, peak_kind = peaks()
     achieved_tflops = rcr_flops / (rcr_ms / 1e3) / 1e12
+    # the M2L levels on the tensor cores (m2l_tc_kernel): split-TF32 GEMMs over dense operators,
+    # 3 MMAs of 128 x Nmma x 8 per 8 of K for every 128 translations and output half
+    tc_levels = [l for l in range(info.lmin, info.lmax + 1) if info.m2l_tensor[l]]
+    tc = None
+    if tc_levels:
+        ex = 0.0
+        for l in tc_levels:
+            p = info.p_level[l]
+            nhalf = 1
+            while True:
+                ch = -(-p * p // nhalf)
+                nmma = (2 * ch + 15) // 16 * 16
+                if nmma <= 256:
+                    break
+                nhalf += 1
+            nch = -(-2 * p * p // 16)
+            ex += info.num_m2l[l] * nhalf * nch * 16 * 6 * nmma
+        tc_ms = sum(float(np.mean(kernel_ms["m2l_l%d" % l])) for l in tc_levels)
+        tc_alg = sum(info.num_m2l[l] * f_rcr(info.p_level[l]) for l in tc_levels)
+        tc = {"kernel": "m2l_tc_kernel (tcgen05.mma kind::tf32, split TF32, TMEM accumulators)", "levels": tc_levels,
+              "ms_per_matvec": tc_ms, "executed_tf32_flops": ex, "executed_tflops": ex / (tc_ms / 1e3) / 1e12,
+              "tf32_peak_from_measured_bf16": bf16_peak / 2,
+              "executed_frac_of_tf32": ex / (tc_ms / 1e3) / 1e12 / (bf16_peak / 2),
+              "algorithmic_flops": tc_alg, "algorithmic_tflops": tc_alg / (tc_ms / 1e3) / 1e12,
+              "note": "per-pass times from direct launches with the other levels' passes running beside them"}
 
     # FP64 plain path and accuracy
     plan.matvec(x, fm.FMM_FP64, out=y)
@@ -375,12 +401,14 @@ def gpu_arm(args, world, rank, local):
                                    "wall_s_timed_region": wall}),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nf * 16, "d2h_bytes_per_step": nf * 16},
         "gpu_launches": launches_per_step * args.steps,
-        "roofline": {"bound": "tensor", "kernel": "rcr_tile_kernel (M2M, M2L, L2L, all levels)",
+        "roofline": {"bound": "tensor",
+                     "kernel": "translation passes: rcr_tile_kernel (M2M, L2L, M2L) + m2l_tc_kernel (M2L at levels %s)"
+                               % tc_levels,
                      "achieved": achieved_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
                      "frac": achieved_tflops / bf16_peak, "peak_source": peak_kind + " bf16 burst",
                      "fp32_simt_nominal_tflops": FP32_NOMINAL, "fp32_simt_frac": achieved_tflops / FP32_NOMINAL,
                      "traffic": ncu_traffic(), "algorithmic_flops_per_matvec": rcr_flops,
-                     "ms_per_matvec": rcr_ms},
+                     "ms_per_matvec": rcr_ms, "tensor_core_m2l": tc},
         "kernels_ms": {n: float(np.mean(v)) for n, v in kernel_ms.items()},
         "batched": batched,
         "fp64_plain": {"value": fp64_rate, "unit": UNIT, "mixed_speedup": value / world / fp64_rate,

@@ -642,7 +642,8 @@ static int solve_batch(Plan *P, int R, double tol, int maxit, int restart, int p
     int total = 0;
     // a zero initial guess needs no FP64 matvec for its residual: the FP64 matvec costs about
     // 20 mixed ones, so the first correction is solved to 0.5 tol (no lower than 5e-7, a few
-    // times the mixed operator's noise) and one FP64 residual normally confirms it
+    // times the mixed operator's noise: inner targets near that floor stall GMRES) and one or
+    // two FP64 residuals confirm it
     std::vector<double> xn;
     if ((st = bnorms(P, P->gm_x, R, xn))) return st;
     bool x_zero = true;

@@ -474,7 +474,7 @@ int tune_tc_m2l(Plan *P)
         rc = build_tc_level(P, l);
         if (rc || !L.tc.B) break;
         float ms[2] = {0.f, 0.f};
-        for (int on = 0; on < 2 && rc == FMM_OK; on++) {
+        for (int on = 0; on < 2 && rc == FMM_OK && mode != 1; on++) {
             L.tc.on = on;
             for (int rep = 0; rep < 4 && rc == FMM_OK; rep++) {
                 if (cudaEventRecord(a, P->stream) != cudaSuccess) rc = FMM_ERR_CUDA;
