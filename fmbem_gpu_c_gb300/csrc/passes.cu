@@ -354,15 +354,15 @@ static int translate32_direct(Plan *P, int nrhs)
     // every side stream waits on the fork, also one that gets no pass, so that all of them
     // join a graph capture
     FMM_CUDA_TRY(cudaEventRecord(P->fork_ev, st));
-    for (int i = 0; i < NSIDE; i++) FMM_CUDA_TRY(cudaStreamWaitEvent(P->side[i], P->fork_ev, 0));
+    for (int i = 0; i < P->nside; i++) FMM_CUDA_TRY(cudaStreamWaitEvent(P->side[i], P->fork_ev, 0));
     for (int l = lmin; l <= lmax; l++) {
-        cudaStream_t sl = P->side[(l - lmin) % NSIDE];
+        cudaStream_t sl = P->side[(l - lmin) % P->nside];
         timer_begin(P, m2l_names[l], sl);
         int e = launch_pass32(P, l, PASS_M2L, nrhs, sl);
         if (e) return e;
         timer_end(P, sl);
     }
-    for (int i = 0; i < NSIDE; i++) {
+    for (int i = 0; i < P->nside; i++) {
         FMM_CUDA_TRY(cudaEventRecord(P->join_ev[i], P->side[i]));
         FMM_CUDA_TRY(cudaStreamWaitEvent(st, P->join_ev[i], 0));
     }

@@ -151,6 +151,7 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
         CTRY(cudaEventCreateWithFlags(&P->join_ev[i], cudaEventDisableTiming));
     }
     CTRY(cudaEventCreateWithFlags(&P->fork_ev, cudaEventDisableTiming));
+    if (const char *ns = getenv("FMMBEM_M2L_STREAMS")) P->nside = std::max(1, std::min(NSIDE, atoi(ns)));
     if (build_tree(P->V, P->F, opt->s, opt->depth, P->tree) != 0 || P->tree.lmax > FMM_MAX_LEVEL) {
         fmm_set_error("octree build failed (lmax=%d)", P->tree.lmax);
         free_plan(P);

@@ -10,7 +10,7 @@ namespace fmm {
 constexpr int NDIR = 316;      // M2L offsets (dx,dy,dz) in [-3,3]^3 with max |d| >= 2
 constexpr int NDIST = 15;      // distinct squared lengths of those offsets
 constexpr int MAX_TIMERS = 64;
-constexpr int NSIDE = 3;      // side streams for the independent M2L passes
+constexpr int NSIDE = 8;      // side streams for the independent M2L passes (at most)
 
 // Work list of one batched translation pass: translations sorted by direction (src, dst,
 // key_beg per direction, key_w = coaxial block per direction) and the device items
@@ -99,6 +99,7 @@ struct Plan {
     cudaStream_t stream = nullptr;
     cudaStream_t side[NSIDE] = {};  // non-blocking side streams, forked from and joined to `stream`
     cudaEvent_t fork_ev = nullptr, join_ev[NSIDE] = {};
+    int nside = 3;                // side streams in use (FMMBEM_M2L_STREAMS, 1..NSIDE)
     cudaGraphExec_t graph_exec = nullptr; // captured mixed translation passes for graph_nrhs columns
     int graph_nrhs = 0, graph_seen = 0;
     int *tc_err = nullptr;        // set by the tensor-core M2L when one of its waits gives up

@@ -10,15 +10,16 @@
 // k and o running over interleaved (re, im) parts, so A is the expansion as it lies in memory.
 // Split TF32 (3 products hi*hi + hi*lo + lo*hi of 11-bit halves) gives FP32-level accuracy.
 //
-// A persistent, warp-specialised kernel (one CTA per SM, 10 warps) runs over the tiles
+// A persistent, warp-specialised kernel (one CTA per SM, 14 warps) runs over the tiles
 // (128 translations x one output half):
 //   warp 0     issues the MMAs (one thread) into one of two TMEM accumulators (2 x 256 columns)
 //              and commits each K chunk to its stage's "empty" barrier, each tile to its
 //              accumulator's "full" barrier;
 //   warp 1     copies the operator's K chunks (hi and lo tiles, contiguous) with cp.async.bulk;
-//   warps 2-5  gather the source expansions, one row (translation) per thread, split them into
-//              TF32 hi / lo and store them in the no-swizzle K-major core-matrix layout;
-//   warps 6-9  read a finished accumulator (tcgen05.ld, one TMEM lane quarter per warp), stage
+//   warps 2-9  gather the source expansions, two threads per row (translation), each half of
+//              every 16-wide K chunk, split them into TF32 hi / lo and store them in the
+//              no-swizzle K-major core-matrix layout;
+//   warps 10-13 read a finished accumulator (tcgen05.ld, one TMEM lane quarter per warp), stage
 //              32 columns at a time in shared memory and add them into the destination local
 //              expansions with coalesced FP32 atomics, overlapping the next tile's MMAs.
 // Four shared-memory stages of KC = 16; every wait has a time limit, after which the thread sets
@@ -34,7 +35,9 @@ namespace fmm {
 constexpr int TC_M = 128;               // translations per tile (MMA M)
 constexpr int TC_KC = 16;               // K per stage (2 MMA K-steps of 8)
 constexpr int TC_STAGES = 4;
-constexpr int TC_THREADS = 320;         // 10 warps
+constexpr int TC_THREADS = 448;         // 14 warps
+constexpr int TC_AWARPS = 8;            // source-gather warps (2..9)
+constexpr int TC_EPI0 = 2 + TC_AWARPS;  // first epilogue warp
 constexpr int TC_MAXP = 16;
 constexpr int TC_EPI_LD = 33;           // staging row stride (floats) of the epilogue
 constexpr size_t TC_SMEM_MAX = 232448;  // 227 KB of dynamic shared memory per CTA
@@ -136,7 +139,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
     }
     if (tid == 32) {
         for (int s = 0; s < TC_STAGES; s++) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 5;" ::"r"(smem_u32(full + s)));   // 4 A warps + B copy
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)), "r"(TC_AWARPS + 1));  // A warps + B copy
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)));  // MMA commit
         }
         for (int a = 0; a < 2; a++) {
@@ -210,11 +213,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                 }
             }
         }
-    } else if (warp < 6) {
+    } else if (warp < TC_EPI0) {
         // ---------------------------------------------------------------- source gather
-        // one row (translation) per thread; the loads of the next two chunks are in flight
-        // while a chunk waits for its stage and is split and stored
-        const int r = tid - 64;
+        // two threads per row (translation), each 8 of every 16-wide K chunk; the loads of the
+        // next two chunks are in flight while a chunk waits for its stage and is stored
+        constexpr int KH = TC_KC / 2;
+        const int at = tid - 64, r = at & (TC_M - 1), kh = (at >> 7) * KH;
         const float *srcf = reinterpret_cast<const float *>(ps.src);
         const bool vec4 = (K & 3) == 0;
         int g = 0;
@@ -222,10 +226,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
             const int item = q / ps.nhalf;
             const int sb = tile_box(ps, ps.items[item], r, true);
             const float *row = srcf + (size_t)(sb < 0 ? 0 : sb) * K;
-            auto load = [&](float(&x)[TC_KC], int c) {
-                const int k0 = c * TC_KC;
+            auto load = [&](float(&x)[KH], int c) {
+                const int k0 = c * TC_KC + kh;
 #pragma unroll
-                for (int j = 0; j < TC_KC; j += 4) {
+                for (int j = 0; j < KH; j += 4) {
                     const int k = k0 + j;
                     if (sb >= 0 && vec4 && k + 3 < K) {
                         float4 v = __ldg(reinterpret_cast<const float4 *>(row + k));
@@ -238,18 +242,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                     }
                 }
             };
-            auto store = [&](const float(&x)[TC_KC], int gg) -> bool {
+            auto store = [&](const float(&x)[KH], int gg) -> bool {
                 const int s = gg % TC_STAGES;
                 if (!mbar_wait(smem_u32(empty + s), ((gg / TC_STAGES) & 1) ^ 1)) return false;
                 unsigned char *Ahi = smem + s * stage, *Alo = Ahi + tA;
 #pragma unroll
-                for (int j = 0; j < TC_KC; j += 4) {
+                for (int j = 0; j < KH; j += 4) {
                     float4 hi, lo;
                     hi.x = tf32_trunc(x[j]); lo.x = tf32_trunc(x[j] - hi.x);
                     hi.y = tf32_trunc(x[j + 1]); lo.y = tf32_trunc(x[j + 1] - hi.y);
                     hi.z = tf32_trunc(x[j + 2]); lo.z = tf32_trunc(x[j + 2] - hi.z);
                     hi.w = tf32_trunc(x[j + 3]); lo.w = tf32_trunc(x[j + 3] - hi.w);
-                    const uint32_t o = core_off(r, j, TC_KC);
+                    const uint32_t o = core_off(r, kh + j, TC_KC);
                     *reinterpret_cast<float4 *>(Ahi + o) = hi;
                     *reinterpret_cast<float4 *>(Alo + o) = lo;
                 }
@@ -258,7 +262,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                 if (lane == 0) mbar_arrive(smem_u32(full + s));
                 return true;
             };
-            float xa[TC_KC], xb[TC_KC], xc[TC_KC];
+            float xa[KH], xb[KH], xc[KH];
             load(xa, 0);
             if (nch > 1) load(xb, 1);
             for (int c = 0; c < nch && ok; c += 3) {
@@ -276,7 +280,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
     } else {
         // ---------------------------------------------------------------- epilogue
         const int wq = warp & 3;  // TMEM lane quarter of this warp
-        float *st = epi + (warp - 6) * 32 * TC_EPI_LD;
+        float *st = epi + (warp - TC_EPI0) * 32 * TC_EPI_LD;
         int i = 0;
         for (int q = blockIdx.x; q < ps.ntiles && ok; q += gridDim.x, i++) {
             const int a = i & 1, item = q / ps.nhalf, h = q - item * ps.nhalf;
