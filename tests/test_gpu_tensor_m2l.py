@@ -80,3 +80,20 @@ def test_tensor_m2l_with_burton_miller(fm, oracle):
     yo = oracle.FMM(V, F, K1, T, [10, 10], a=0.5, b=0.0, c=-1.0, rule=1, alpha=alpha).apply(x)
     assert rel(plan.matvec(x, fm.FMM_MIXED), yo) < 1e-5
     plan.close()
+
+
+def test_tensor_m2l_in_the_transposed_operator(fm, oracle):
+    """The transposed matvec reuses the M2L lists and operators, so its mixed path runs on the
+    tensor cores too."""
+    V, F = fm.icosphere(3, 0.1)
+    kw = dict(k=K1, depth=3, p_levels={2: 10, 3: 10}, rule=0, a=0.3, b=0.7 + 0.2j, c=-1.0)
+    plan = make_plan(fm, "1", V, F, **kw)
+    rng = np.random.default_rng(9)
+    y = rng.standard_normal(plan.nf) + 1j * rng.standard_normal(plan.nf)
+    at64 = plan.matvec_adjoint(y, fm.FMM_FP64)
+    assert rel(plan.matvec_adjoint(y, fm.FMM_MIXED), at64) < 1e-5
+    assert rel(plan.matvec_adjoint(y, fm.FMM_MIXED, conjugate=True), plan.matvec_adjoint(y, fm.FMM_FP64, conjugate=True)) < 1e-5
+    T = oracle.tree_for_fmm(V, F, depth=3)
+    orc = oracle.FMM(V, F, K1, T, [10, 10], a=0.3, b=0.7 + 0.2j, c=-1.0, rule=0)
+    assert rel(at64, orc.apply(y, transpose=True)) < 1e-10
+    plan.close()
