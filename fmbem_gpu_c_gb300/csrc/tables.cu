@@ -642,19 +642,37 @@ __device__ __forceinline__ double2 basis_R(const BasisSh &B, int pb, int n, int 
     return make_double2(v * e.x, v * e.y);
 }
 
+// The basis of order pb at v, spread over the warp: lane 0 runs the spherical Bessel
+// recurrence, lane m (and m + 32) the Legendre column m (its diagonal entry as a product, then
+// the same three-term recurrence in n as legendre_Q), every lane a few phases.
 __device__ __forceinline__ void basis_prepare(const BasisSh &B, int pb, double k, const double *v, int lane)
 {
-    if (lane == 0) {
-        double r = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-        double ct = 1.0, phi = 0.0;
-        if (r > 0.0) { ct = v[2] / r; phi = atan2(v[1], v[0]); }
-        sph_jn_array(pb, k * r, B.jn);
-        legendre_Q(pb, ct, B.Q);
-        for (int m = -pb; m <= pb; m++) {
-            double s, c;
-            sincos(m * phi, &s, &c);
-            B.ph[m + pb] = make_double2(c, s);
+    double r = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    double ct = 1.0, phi = 0.0;
+    if (r > 0.0) { ct = v[2] / r; phi = atan2(v[1], v[0]); }
+    if (lane == 0) sph_jn_array(pb, k * r, B.jn);
+    const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+    for (int m = lane; m < pb; m += 32) {
+        double q = 0.28209479177387814; // 1/sqrt(4 pi)
+        for (int i = 1; i <= m; i++) q = sqrt((2.0 * i + 1.0) / (2.0 * i)) * st * q;
+        B.Q[m * (m + 1) / 2 + m] = q;
+        if (m + 1 < pb) {
+            double q1 = sqrt(2.0 * m + 3.0) * ct * q, q0 = q;
+            B.Q[(m + 1) * (m + 2) / 2 + m] = q1;
+            for (int n = m + 2; n < pb; n++) {
+                double a = sqrt((4.0 * n * n - 1.0) / ((double)n * n - (double)m * m));
+                double b = sqrt(((n - 1.0) * (n - 1.0) - (double)m * m) / (4.0 * (n - 1.0) * (n - 1.0) - 1.0));
+                double q2 = a * (ct * q1 - b * q0);
+                B.Q[n * (n + 1) / 2 + m] = q2;
+                q0 = q1;
+                q1 = q2;
+            }
         }
+    }
+    for (int m = lane - pb; m <= pb; m += 32) {
+        double s, c;
+        sincos(m * phi, &s, &c);
+        B.ph[m + pb] = make_double2(c, s);
     }
     __syncwarp();
 }
