@@ -129,6 +129,7 @@ int raise_smem_limit(const void *func, size_t bytes, size_t *cache);
 // tables.cu
 int gen_rotation_tables(Plan *P);
 void rule_tables(double bary[2][48], double w[2][16], int n[2]);
+void line_rule(int n, double *x, double *w);
 int gen_coax_tables(Plan *P);
 int gen_element_tables(Plan *P);
 int gen_near_field(Plan *P);

@@ -43,6 +43,9 @@ static void gauss_legendre(int n, double *x, double *w)
     }
 }
 
+// Gauss-Legendre nodes and weights on [-1, 1]
+void line_rule(int n, double *x, double *w) { gauss_legendre(n, x, w); }
+
 // The two regular rules as host tables (barycentric points, weights in units of J, counts).
 void rule_tables(double bary[2][48], double w[2][16], int n[2])
 {

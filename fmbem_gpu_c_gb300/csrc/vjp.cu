@@ -28,6 +28,9 @@ namespace fmm {
 __constant__ double v_rule_bary[2][16 * 3];
 __constant__ double v_rule_w[2][16];
 __constant__ int v_rule_n[2];
+// the 8-point Gauss rule on [-1, 1] of the Burton-Miller edge integrals (tables.cu)
+constexpr int V_LINE_PTS = 8;
+__constant__ double v_line_x[V_LINE_PTS], v_line_w[V_LINE_PTS];
 
 static int upload_vjp_rules()
 {
@@ -41,6 +44,10 @@ static int upload_vjp_rules()
     FMM_CUDA_TRY(cudaMemcpyToSymbol(v_rule_bary, bary, sizeof(bary)));
     FMM_CUDA_TRY(cudaMemcpyToSymbol(v_rule_w, w, sizeof(w)));
     FMM_CUDA_TRY(cudaMemcpyToSymbol(v_rule_n, n, sizeof(n)));
+    double lx[V_LINE_PTS], lw[V_LINE_PTS];
+    line_rule(V_LINE_PTS, lx, lw);
+    FMM_CUDA_TRY(cudaMemcpyToSymbol(v_line_x, lx, sizeof(lx)));
+    FMM_CUDA_TRY(cudaMemcpyToSymbol(v_line_w, lw, sizeof(lw)));
     dev_done = dev;
     return FMM_OK;
 }
@@ -253,6 +260,105 @@ __device__ CDn<N> elem_integral_sgl_d(double k, const Dn<N> *nod, int kern)
         acc.im = acc.im + part.im;
     }
     return acc;
+}
+
+// ---------------------------------------------------------------- Burton-Miller terms in duals
+// The same forms as tables.cu (elem_dGdny, elem_hyper_near, elem_hyper_self); the numbers of
+// edge segments follow from the values, as there, and are held fixed by the derivative.
+__device__ __forceinline__ int edge_segments_v(double len, double dist)
+{
+    double m = ceil(len / fmax(dist, 1e-12 * len));
+    return m > 64.0 ? 64 : (int)m;
+}
+
+// int_T dG(x, y)/dn_y dS_x, ny the unit normal at y
+template <int N>
+__device__ CDn<N> elem_dGdny_d(double k, const Dn<N> *nod, const Dn<N> *y, const Dn<N> *ny, int rule)
+{
+    Dn<N> nc[3], J;
+    tri_normal_d(nod, nc, J);
+    CDn<N> acc = cdzero<N>();
+    int nq = v_rule_n[rule];
+    for (int q = 0; q < nq; q++) {
+        const double *b = &v_rule_bary[rule][3 * q];
+        Dn<N> x[3];
+        for (int a = 0; a < 3; a++) x[a] = b[0] * nod[a] + b[1] * nod[3 + a] + b[2] * nod[6 + a];
+        CDn<N> g = green_d(k, x, y, ny, 1);   // G (ik - 1/r) (x - y).ny / r
+        Dn<N> wq = v_rule_w[rule][q] * J;
+        acc.re = acc.re - wq * g.re;
+        acc.im = acc.im - wq * g.im;
+    }
+    return acc;
+}
+
+// int_T d2G/dn_x dn_y dS_x at y off T: k^2 (ny.nT) int_T G - oint (ny x grad_y G) . dl
+template <int N>
+__device__ CDn<N> elem_hyper_near_d(double k, const Dn<N> *nod, const Dn<N> *y, const Dn<N> *ny, int rule)
+{
+    Dn<N> nc[3], J;
+    tri_normal_d(nod, nc, J);
+    CDn<N> S = elem_integral_d(k, nod, y, rule, 0);
+    Dn<N> dn = (ny[0] * nc[0] + ny[1] * nc[1] + ny[2] * nc[2]) / J;
+    CDn<N> line = cdzero<N>();
+    for (int e = 0; e < 3; e++) {
+        const Dn<N> *va = nod + 3 * e, *vb = nod + 3 * ((e + 1) % 3);
+        Dn<N> t[3] = {vb[0] - va[0], vb[1] - va[1], vb[2] - va[2]}, a[3] = {y[0] - va[0], y[1] - va[1], y[2] - va[2]};
+        double tt = t[0].v * t[0].v + t[1].v * t[1].v + t[2].v * t[2].v, len = sqrt(tt);
+        double sc = fmin(fmax((a[0].v * t[0].v + a[1].v * t[1].v + a[2].v * t[2].v) / tt, 0.0), 1.0);
+        double e0 = a[0].v - sc * t[0].v, e1 = a[1].v - sc * t[1].v, e2 = a[2].v - sc * t[2].v;
+        int nseg = edge_segments_v(len, sqrt(e0 * e0 + e1 * e1 + e2 * e2));
+        Dn<N> tn0 = t[1] * ny[2] - t[2] * ny[1], tn1 = t[2] * ny[0] - t[0] * ny[2], tn2 = t[0] * ny[1] - t[1] * ny[0];
+        for (int g = 0; g < nseg; g++)
+            for (int q = 0; q < V_LINE_PTS; q++) {
+                double s = (g + 0.5 + 0.5 * v_line_x[q]) / nseg, w = 0.5 * v_line_w[q] / nseg;
+                Dn<N> d0 = a[0] - s * t[0], d1 = a[1] - s * t[1], d2 = a[2] - s * t[2];
+                Dn<N> r2 = d0 * d0 + d1 * d1 + d2 * d2, r = dsqrt(r2);
+                Dn<N> sn, cs;
+                dsincos(k * r, sn, cs);
+                Dn<N> f = (w / (4.0 * FMM_PI)) * (d0 * tn0 + d1 * tn1 + d2 * tn2) / r2;
+                Dn<N> ar = -(dconst<N>(1.0) / r);
+                // e^{ikr} (ik - 1/r) f
+                line.re = line.re + f * (cs * ar - k * sn);
+                line.im = line.im + f * (k * cs + sn * ar);
+            }
+    }
+    Dn<N> kk = (k * k) * dn;
+    CDn<N> out;
+    out.re = kk * S.re - line.re;
+    out.im = kk * S.im - line.im;
+    return out;
+}
+
+// Hadamard finite part of int_T d2G/dn_x dn_y at the centroid of the flat element T
+template <int N>
+__device__ CDn<N> elem_hyper_self_d(double k, const Dn<N> *nod)
+{
+    Dn<N> c[3];
+    centroid_d(nod, c);
+    CDn<N> ang = cdzero<N>();
+    for (int e = 0; e < 3; e++) {
+        const Dn<N> *va = nod + 3 * e, *vb = nod + 3 * ((e + 1) % 3);
+        Dn<N> t[3] = {vb[0] - va[0], vb[1] - va[1], vb[2] - va[2]}, u[3] = {va[0] - c[0], va[1] - c[1], va[2] - c[2]};
+        Dn<N> c0 = u[1] * t[2] - u[2] * t[1], c1 = u[2] * t[0] - u[0] * t[2], c2 = u[0] * t[1] - u[1] * t[0];
+        Dn<N> hL = dsqrt(c0 * c0 + c1 * c1 + c2 * c2);
+        double len = sqrt(t[0].v * t[0].v + t[1].v * t[1].v + t[2].v * t[2].v);
+        int nseg = edge_segments_v(len, hL.v / len);
+        for (int g = 0; g < nseg; g++)
+            for (int q = 0; q < V_LINE_PTS; q++) {
+                double s = (g + 0.5 + 0.5 * v_line_x[q]) / nseg, w = 0.5 * v_line_w[q] / nseg;
+                Dn<N> d0 = u[0] + s * t[0], d1 = u[1] + s * t[1], d2 = u[2] + s * t[2];
+                Dn<N> r = dsqrt(d0 * d0 + d1 * d1 + d2 * d2);
+                Dn<N> sn, cs;
+                dsincos(k * r, sn, cs);
+                Dn<N> f = w * hL / (r * r * r);
+                ang.re = ang.re + f * cs;
+                ang.im = ang.im + f * sn;
+            }
+    }
+    CDn<N> out;
+    out.re = (-1.0 / (4.0 * FMM_PI)) * ang.re;
+    out.im = (-1.0 / (4.0 * FMM_PI)) * ang.im + dconst<N>(2.0 * FMM_PI * k / (4.0 * FMM_PI));
+    return out;
 }
 
 // spherical Bessel j_n(x), n < NB, Miller's backward recurrence normalised by j0 or j1, in duals
@@ -497,6 +603,125 @@ __global__ void vjp_far_target_kernel(const double *V, const int *F, int nf, int
     }
 }
 
+// Burton-Miller near pairs: -2 Re[ mu_i x_j d/dV alpha (b K'_ij + c N_ij) ], both elements'
+// vertices as dual slots (0..8 source j, 9..17 target i: its centroid and unit normal); the
+// self term N_ii (K'_ii = 0) in the element's own 9 slots
+__global__ void vjp_near_bm_kernel(const double *V, const int *F, int nf, const int *near_beg, const int *near_col,
+                                   double k, double2 bco, double2 cco, double2 alpha, int rule, const double2 *mu,
+                                   const double2 *x, double *grad)
+{
+    int lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int nwt = (gridDim.x * blockDim.x) >> 5;
+    const bool hb = bco.x != 0.0 || bco.y != 0.0, hc = cco.x != 0.0 || cco.y != 0.0;
+    for (int i = warp; i < nf; i += nwt) {
+        double ndi[9];
+        load_tri_d(V, F, i, ndi);
+        double2 mi = mu[i];
+        double gi[9] = {0};
+        for (int s = near_beg[i] + lane; s < near_beg[i + 1]; s += 32) {
+            int j = near_col[s];
+            double2 xj = x[j];
+            // w = -(mu_i x_j alpha)
+            double2 mx = make_double2(mi.x * xj.x - mi.y * xj.y, mi.x * xj.y + mi.y * xj.x);
+            double2 w = make_double2(-(mx.x * alpha.x - mx.y * alpha.y), -(mx.x * alpha.y + mx.y * alpha.x));
+            if (i == j) {
+                if (!hc) continue;
+                Dn<9> nod[9];
+                for (int q = 0; q < 9; q++) nod[q] = dvar<9>(ndi[q], q);
+                CDn<9> v = cdzero<9>();
+                cdmac(v, cco, elem_hyper_self_d(k, nod));
+                double g9[9];
+                for (int q = 0; q < 9; q++) g9[q] = 2.0 * re_wd(w, v, q);
+                add_vertex_grad(grad, F, j, g9);
+            } else {
+                double nd[9];
+                load_tri_d(V, F, j, nd);
+                Dn<18> nod[9], tgt[9], y[3], ncy[3], Jy;
+                for (int q = 0; q < 9; q++) {
+                    nod[q] = dvar<18>(nd[q], q);
+                    tgt[q] = dvar<18>(ndi[q], 9 + q);
+                }
+                centroid_d(tgt, y);
+                tri_normal_d(tgt, ncy, Jy);
+                Dn<18> ny[3] = {ncy[0] / Jy, ncy[1] / Jy, ncy[2] / Jy};
+                CDn<18> v = cdzero<18>();
+                if (hb) cdmac(v, bco, elem_dGdny_d(k, nod, y, ny, rule));
+                if (hc) cdmac(v, cco, elem_hyper_near_d(k, nod, y, ny, rule));
+                double g9[9];
+                for (int q = 0; q < 9; q++) g9[q] = 2.0 * re_wd(w, v, q);
+                add_vertex_grad(grad, F, j, g9);
+                for (int q = 0; q < 9; q++) gi[q] += 2.0 * re_wd(w, v, 9 + q);
+            }
+        }
+        add_vertex_grad(grad, F, i, gi);
+    }
+}
+
+// Burton-Miller far pairs, target side: -2 Re[ mu_i alpha d/dV (n_i . grad phi(c_i)) ] with
+// phi = sum_nm D_i[nm] R_n^m(. - C), grad phi from its derivative expansions (Dz, Dp, Dm)
+__global__ void vjp_far_target_bm_kernel(const double *V, const int *F, int nf, int pl, double k, double2 alpha,
+                                         const int *elem_leaf, const double *box_ctr, const double2 *Dz,
+                                         const double2 *Dp, const double2 *Dm, const double2 *mu, double *grad)
+{
+    const int po = pl + 1;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x) {
+        double nd[9];
+        load_tri_d(V, F, i, nd);
+        int b = elem_leaf[i];
+        Dn<9> nod[9], c[3], nc[3], J;
+        for (int q = 0; q < 9; q++) nod[q] = dvar<9>(nd[q], q);
+        centroid_d(nod, c);
+        tri_normal_d(nod, nc, J);
+        Dn<9> v[3];
+        for (int a = 0; a < 3; a++) v[a] = c[a] - dconst<9>(box_ctr[3 * b + a]);
+        const double2 *coef[3] = {Dz + (size_t)b * po * po, Dp + (size_t)b * po * po, Dm + (size_t)b * po * po};
+        CDn<9> e[3];
+        eval_expansions_d<9, 3>(po, k, v, coef, e);
+        CDn<9> gx, gy;
+        gx.re = 0.5 * (e[1].re + e[2].re);
+        gx.im = 0.5 * (e[1].im + e[2].im);
+        gy.re = 0.5 * (e[1].im - e[2].im);
+        gy.im = -0.5 * (e[1].re - e[2].re);
+        CDn<9> f;
+        f.re = (gx.re * nc[0] + gy.re * nc[1] + e[0].re * nc[2]) / J;
+        f.im = (gx.im * nc[0] + gy.im * nc[1] + e[0].im * nc[2]) / J;
+        double2 m = mu[i];
+        double2 w = make_double2(-(m.x * alpha.x - m.y * alpha.y), -(m.x * alpha.y + m.y * alpha.x));
+        double g9[9];
+        for (int q = 0; q < 9; q++) g9[q] = 2.0 * re_wd(w, f, q);
+        add_vertex_grad(grad, F, i, g9);
+    }
+}
+
+// 2 Re[ mu_i d/dV alpha i k (d.n_i) exp(i k d.c_i) ]: the Burton-Miller term of the plane-wave
+// right-hand side
+__global__ void vjp_rhs_bm_kernel(const double *V, const int *F, int nf, double k, double dx, double dy, double dz,
+                                  double2 alpha, const double2 *mu, double *grad)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x) {
+        double nd[9];
+        load_tri_d(V, F, i, nd);
+        Dn<9> nod[9], c[3], nc[3], J;
+        for (int q = 0; q < 9; q++) nod[q] = dvar<9>(nd[q], q);
+        centroid_d(nod, c);
+        tri_normal_d(nod, nc, J);
+        Dn<9> ph = k * (dx * c[0] + dy * c[1] + dz * c[2]);
+        Dn<9> kd = k * ((dx * nc[0] + dy * nc[1] + dz * nc[2]) / J);
+        Dn<9> sn, cs;
+        dsincos(ph, sn, cs);
+        // alpha i kd (cs + i sn) = alpha kd (-sn + i cs)
+        CDn<9> t;
+        t.re = -(kd * sn);
+        t.im = kd * cs;
+        CDn<9> f = cdzero<9>();
+        cdmac(f, alpha, t);
+        double2 m = mu[i];
+        double g9[9];
+        for (int q = 0; q < 9; q++) g9[q] = 2.0 * re_wd(m, f, q);
+        add_vertex_grad(grad, F, i, g9);
+    }
+}
+
 // Coefficients of the derivatives of a regular expansion sum Psi[nm] R_n^m of order pl as
 // expansions of order pl + 1 (from the G&D recurrences of dR/dz and (d/dx +- i d/dy) R):
 //   dz  : k [ a(n,m) Psi_{n+1}^m - a(n-1,m) Psi_{n-1}^m ]
@@ -614,10 +839,7 @@ extern "C" int fmm_vjp(fmm_plan *plan, const cuDoubleComplex *x, const double *d
     if (!P || !x || !pts || npts < 1 || !pbar || !grad || !(tol > 0)) { fmm_set_error("fmm_vjp: invalid argument"); return FMM_ERR_ARG; }
     if (precision != FMM_FP64 && precision != FMM_MIXED) { fmm_set_error("fmm_vjp: unknown precision"); return FMM_ERR_ARG; }
     if (P->pleaf + 1 > VJP_PMAX) { fmm_set_error("fmm_vjp: leaf order %d above %d", P->pleaf, VJP_PMAX - 1); return FMM_ERR_ARG; }
-    if (P->opt.alpha_re != 0.0 || P->opt.alpha_im != 0.0) {
-        fmm_set_error("fmm_vjp: the Burton-Miller operator (alpha != 0) has no vertex derivative here");
-        return FMM_ERR_ARG;
-    }
+
     int nf = P->nf, nv = P->nv, pl = P->pleaf, lmax = P->lmax;
     int nbl = P->lev[lmax].nb;
     cudaStream_t st = P->stream;
@@ -673,6 +895,20 @@ extern "C" int fmm_vjp(fmm_plan *plan, const cuDoubleComplex *x, const double *d
         vjp_far_source_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, pl, P->opt.k, P->opt.rule, bco, cco, P->elem_leaf,
                                                ctr, P->lev[lmax].Dl64, Dz, Dp, Dm, xd, gd);
         vjp_far_target_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, pl, P->opt.k, P->elem_leaf, ctr, D, mu, gd);
+        const double2 alpha = make_double2(P->opt.alpha_re, P->opt.alpha_im);
+        const bool bm = alpha.x != 0.0 || alpha.y != 0.0;
+        if (bm) {
+            // target-side normal derivative of the far field: the derivative expansions of D
+            // (Dz, Dp, Dm are free again once the source kernel above has run)
+            deriv_coef_kernel<<<(unsigned)std::min<size_t>((locd + 255) / 256, 152 * 8), 256, 0, st>>>(nbl, pl, P->opt.k,
+                                                                                                     D, Dz, Dp, Dm);
+            vjp_far_target_bm_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, pl, P->opt.k, alpha, P->elem_leaf, ctr, Dz,
+                                                      Dp, Dm, mu, gd);
+            vjp_near_bm_kernel<<<std::min((nf + 3) / 4, 152 * 16), 128, 0, st>>>(
+                P->V_dev, P->F_dev, nf, P->near_beg, P->near_col, P->opt.k, bco, cco, alpha, P->opt.rule, mu, xd, gd);
+            if (dir)
+                vjp_rhs_bm_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, P->opt.k, dir[0], dir[1], dir[2], alpha, mu, gd);
+        }
         vjp_near_kernel<<<std::min((nf + 7) / 8, 152 * 16), 256, 0, st>>>(P->V_dev, P->F_dev, nf, P->near_beg, P->near_col,
                                                                         P->opt.k, bco, cco, P->opt.rule, mu, xd, gd);
         vjp_farpts_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, P->opt.k, P->opt.rule, nb, nc, ptd, npts, pb, xd, gd);

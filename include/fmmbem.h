@@ -148,8 +148,10 @@ int fmm_solve_many(fmm_plan *const *plans, int n, const cuDoubleComplex *const *
  *     dJ/dV = 2 Re[ pbar^H (dF/dV) x + lambda^H (db/dV - (dA/dV) x) ],
  * lambda solving A^H lambda = F^H pbar by GMRES to tol at `precision`; lambda[nf] (may be
  * NULL) receives it.  dA/dV is the derivative of the operator fmm_matvec applies, with the
- * octree, truncation orders and box centres held fixed.  Host or device buffers.  Leaf
- * orders up to 23.  No counterpart in the reference. */
+ * octree, truncation orders and box centres held fixed (with the Burton-Miller coupling,
+ * also its hypersingular near terms, the target normal derivative of the far field and the
+ * alpha dp_inc/dn of the right-hand side).  Host or device buffers.  Leaf orders up to 23.
+ * No counterpart in the reference. */
 int fmm_vjp(fmm_plan *plan, const cuDoubleComplex *x, const double *dir, const double *pts, int npts,
             const cuDoubleComplex *pbar, double tol, int precision, double *grad, cuDoubleComplex *lambda);
 

@@ -95,13 +95,3 @@ def test_admittance_bm_solve_matches_impedance_mie(fm, oracle):
     pts = fib_points(60, 1.0)
     assert rel(plan.far_field(x, pts), oracle.mie_impedance(k, 0.1, beta, pts)) < 0.01
     plan.close()
-
-
-def test_vjp_rejects_bm(fm):
-    V, F = fm.icosphere(2, 0.1)
-    plan = fm.Plan(V, F, k=K1, depth=2, p_levels={2: 6}, a=0.5, b=0.0, c=-1.0, alpha=1j / K1)
-    x = np.ones(plan.nf, dtype=np.complex128)
-    pts = fib_points(4)
-    with pytest.raises(fm.FmmError, match="Burton-Miller"):
-        plan.vjp(x, pts, np.ones(4, dtype=np.complex128))
-    plan.close()

@@ -19,9 +19,9 @@ def generic_sphere(fm, subdiv):
     return V @ q.T + np.array([0.0123, -0.0071, 0.0045]), F
 
 
-def pipeline(fm, V, F, pts, depth, p, b=0.0, k=K1):
+def pipeline(fm, V, F, pts, depth, p, b=0.0, k=K1, alpha=0.0):
     plan = fm.Plan(V, F, k=k, depth=depth, p_levels={l: p for l in range(2, depth + 1)}, rule=fm.RULE_DUNAVANT7,
-                   a=0.5, b=b, c=-1.0, build_mixed=False)
+                   a=0.5 * (1 + alpha * b), b=b, c=-1.0, build_mixed=False, alpha=alpha)
     b = plan.plane_wave(DIR)
     x, it, rr, ok = plan.gmres(b, tol=1e-13, restart=80, maxit=2000, precision=fm.FMM_FP64)
     assert ok
@@ -108,3 +108,67 @@ def test_vjp_with_admittance_boundary(fm):
         Vm[v] -= h * e
         fd = (pipeline(fm, Vp, F, pts, 3, 16, b=b, k=k)[3] - pipeline(fm, Vm, F, pts, 3, 16, b=b, k=k)[3]) / (2 * h)
         assert abs(grad[v] @ e - fd) <= 1e-4 * scale, (v, grad[v] @ e, fd)
+
+
+@pytest.mark.parametrize("beta", [0.0, 0.1 + 0.05j])
+def test_vjp_with_burton_miller(fm, beta):
+    """The Burton-Miller operator (alpha = i/k): the gradient gains the hypersingular and
+    normal-derivative near terms (both elements' vertices), the target-side normal derivative
+    of the far field and the alpha dp_inc/dn term of the right-hand side; against central
+    differences of the GPU pipeline, rigid and with an admittance boundary."""
+    k = 2 * np.pi * 2000 / 343.0
+    b, alpha = 1j * k * beta, 1j / k
+    V, F = generic_sphere(fm, 2)
+    pts = fm.fibonacci_sphere(32, 1.0)
+    plan, x, pf, J = pipeline(fm, V, F, pts, 2, 16, b=b, k=k, alpha=alpha)
+    assert plan.info.num_m2l[2] > 0
+    grad, _ = plan.vjp(x, pts, pf, direction=DIR, tol=1e-13)
+    plan.close()
+    assert np.isfinite(grad).all()
+    rng = np.random.default_rng(21)
+    h = 1e-6
+    scale = np.abs(grad).max()
+    for v in rng.choice(len(V), 12, replace=False):
+        e = rng.standard_normal(3)
+        e /= np.linalg.norm(e)
+        Vp, Vm = V.copy(), V.copy()
+        Vp[v] += h * e
+        Vm[v] -= h * e
+        fd = (pipeline(fm, Vp, F, pts, 2, 16, b=b, k=k, alpha=alpha)[3]
+              - pipeline(fm, Vm, F, pts, 2, 16, b=b, k=k, alpha=alpha)[3]) / (2 * h)
+        assert abs(grad[v] @ e - fd) <= 1e-4 * scale, (v, grad[v] @ e, fd)
+
+
+def test_vjp_burton_miller_against_dense_oracle_differences(fm, oracle):
+    """The Burton-Miller gradient against central differences of J with the oracle's dense
+    combined operator and a dense FP64 solve."""
+    k = 2 * np.pi * 2000 / 343.0
+    alpha = 1j / k
+    V, F = generic_sphere(fm, 2)
+    pts = fm.fibonacci_sphere(32, 1.0)
+    plan, x, pf, J = pipeline(fm, V, F, pts, 2, 16, k=k, alpha=alpha)
+    grad, _ = plan.vjp(x, pts, pf, direction=DIR, tol=1e-13)
+    plan.close()
+    d = np.array(DIR)
+
+    def J_dense(Vx):
+        A = oracle.dense_matrix(Vx, F, k, a=0.5, b=0.0, c=-1.0, rule=1, alpha=alpha)
+        tri = Vx[F]
+        c = tri[:, 0] + (2.0 / 3.0) * (0.5 * (tri[:, 1] + tri[:, 2]) - tri[:, 0])
+        n = np.cross(tri[:, 0] - tri[:, 2], tri[:, 1] - tri[:, 2])
+        n /= np.linalg.norm(n, axis=1)[:, None]
+        rhs = np.exp(1j * k * (c @ d)) * (1 + alpha * 1j * k * (n @ d))
+        xs = np.linalg.solve(A, rhs)
+        return float(np.sum(np.abs(oracle.far_field(Vx, F, k, xs, pts, rule=1)) ** 2))
+
+    assert abs(J_dense(V) - J) < 1e-4 * J
+    rng = np.random.default_rng(4)
+    h = 1e-6
+    scale = np.abs(grad).max()
+    for v in rng.choice(len(V), 5, replace=False):
+        for a in range(3):
+            Vp, Vm = V.copy(), V.copy()
+            Vp[v, a] += h
+            Vm[v, a] -= h
+            fd = (J_dense(Vp) - J_dense(Vm)) / (2 * h)
+            assert abs(grad[v, a] - fd) <= 2e-4 * scale, (v, a, grad[v, a], fd)
