@@ -126,6 +126,21 @@ int build_tree(const std::vector<double> &V, const std::vector<int> &F, int s, i
     for (size_t e = 0; e < nf; e++)
         for (int a = 0; a < 3; a++) S[3 * e + a] = (C[3 * e + a] - T.pt_min[a]) / T.d;
     T.lmax = depth > 0 ? depth : deter_lmax(S, s);
+    if (depth < 0) {
+        // the reference's rule, capped where leaf boxes would get smaller than 1.5 times the
+        // longest element edge: an element filed under its centroid's box reaches outside it,
+        // and the expansions of boxes only one box apart lose their accuracy
+        double emax = 0.0;
+        for (size_t e = 0; e < nf; e++)
+            for (int a = 0; a < 3; a++) {
+                const double *p0 = &V[3 * F[3 * e + a]], *p1 = &V[3 * F[3 * e + (a + 1) % 3]];
+                double dx = p0[0] - p1[0], dy = p0[1] - p1[1], dz = p0[2] - p1[2];
+                emax = std::max(emax, sqrt(dx * dx + dy * dy + dz * dz));
+            }
+        int cap = T.lmin;
+        while (cap < 30 && T.d * ldexp(1.0, -(cap + 1)) >= 1.5 * emax) cap++;
+        T.lmax = std::max(T.lmin, std::min(T.lmax, cap));
+    }
     if (T.lmax < T.lmin) return -2;
     T.elem_key.resize(nf);
     for (size_t e = 0; e < nf; e++) T.elem_key[e] = morton_key(&S[3 * e], T.lmax);

@@ -124,7 +124,7 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
     if (!(opt->k > 0.0)) { fmm_set_error("wavenumber must be positive"); return FMM_ERR_ARG; }
     if (opt->rule != FMM_RULE_GAUSS3 && opt->rule != FMM_RULE_DUNAVANT7) { fmm_set_error("unknown rule %d", opt->rule); return FMM_ERR_ARG; }
     if (!std::isfinite(opt->alpha_re) || !std::isfinite(opt->alpha_im)) { fmm_set_error("coupling alpha is not finite"); return FMM_ERR_ARG; }
-    if (opt->depth < 0 || opt->depth > FMM_MAX_LEVEL) { fmm_set_error("depth %d out of range", opt->depth); return FMM_ERR_ARG; }
+    if (opt->depth < -1 || opt->depth > FMM_MAX_LEVEL) { fmm_set_error("depth %d out of range", opt->depth); return FMM_ERR_ARG; }
     for (int e = 0; e < nf; e++)
         for (int t = 0; t < 3; t++)
             if (F[3 * e + t] < 0 || F[3 * e + t] >= nv) { fmm_set_error("element %d has vertex index %d out of range", e, F[3 * e + t]); return FMM_ERR_MESH; }
@@ -143,8 +143,9 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
 #define TRY(x) do { int s_ = (x); if (s_ != FMM_OK) { free_plan(P); return s_; } } while (0)
 #define CTRY(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { fmm_set_error("%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_)); free_plan(P); return FMM_ERR_CUDA; } } while (0)
     CTRY(cudaSetDevice(opt->device));
-    // a blocking stream: setup code mixes kernels on this stream with default-stream
-    // cudaMemcpy read-backs (list counts), which must wait for those kernels
+    // a blocking stream during setup: setup code mixes kernels on this stream with
+    // default-stream cudaMemcpy read-backs (list counts), which must wait for those kernels;
+    // replaced by a non-blocking stream once the plan is built
     CTRY(cudaStreamCreate(&P->stream));
     for (int i = 0; i < NSIDE; i++) {
         CTRY(cudaStreamCreateWithFlags(&P->side[i], cudaStreamNonBlocking));
@@ -156,6 +157,21 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
         fmm_set_error("octree build failed (lmax=%d)", P->tree.lmax);
         free_plan(P);
         return FMM_ERR_MESH;
+    }
+    if (opt->depth < 0 && opt->p_level[P->tree.lmax] <= 0) {
+        // the element-size cap gives way where the leaf order would exceed 40 (meshes coarse
+        // against the wavelength): one level deeper at a time, no deeper than the plain rule
+        HostTree plain;
+        int lref = build_tree(P->V, P->F, opt->s, 0, plain) == 0 ? plain.lmax : P->tree.lmax;
+        while (P->tree.lmax < std::min(lref, FMM_MAX_LEVEL) &&
+               trunc_num(opt->k, opt->eps > 0 ? opt->eps : 0.05, 1.5, ldexp(P->tree.d, -P->tree.lmax)) > 40) {
+            int next = P->tree.lmax + 1;
+            if (build_tree(P->V, P->F, opt->s, next, P->tree) != 0) {
+                fmm_set_error("octree build failed (lmax=%d)", next);
+                free_plan(P);
+                return FMM_ERR_MESH;
+            }
+        }
     }
     P->lmin = P->tree.lmin;
     P->lmax = P->tree.lmax;
@@ -215,6 +231,15 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
     CTRY(cudaEventCreate(&P->phase.end));
     P->timers_created = 1;
     CTRY(cudaStreamSynchronize(P->stream));
+    // From here on the plan's work (matvecs, solves, graph captures) runs on a non-blocking
+    // stream: the legacy default stream, which other threads may use (another plan's setup,
+    // cudaMemcpy), must never come to depend on a stream that is capturing a graph.
+    {
+        cudaStream_t s2 = nullptr;
+        CTRY(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+        CTRY(cudaStreamDestroy(P->stream));
+        P->stream = s2;
+    }
     P->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     *out = (fmm_plan *)P;
 #undef TRY
@@ -321,7 +346,7 @@ static int apply_operator(Plan *P, const cuDoubleComplex *x, cuDoubleComplex *y,
     FMM_CUDA_TRY(cudaGetLastError());
     if (!yd) FMM_CUDA_TRY(cudaMemcpyAsync(y, P->ybuf, sizeof(double2) * n, cudaMemcpyDeviceToHost, P->stream));
     FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
-    return FMM_OK;
+    return precision == FMM_MIXED ? check_tc_error(P) : FMM_OK;
 }
 
 extern "C" int fmm_matvec(fmm_plan *plan, const cuDoubleComplex *x, cuDoubleComplex *y, int nrhs, int precision)
@@ -710,6 +735,7 @@ static int solve_entry(Plan *P, const cuDoubleComplex *b, cuDoubleComplex *x, in
     if ((st = solve_batch(P, R, tol, maxit, restart, precision, it, rr))) return st;
     FMM_CUDA_TRY(cudaMemcpyAsync(x, P->gm_x, sizeof(double2) * n, xd ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, P->stream));
     FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    if (precision == FMM_MIXED && (st = check_tc_error(P))) return st;
     bool ok = true;
     for (int r = 0; r < R; r++) {
         if (iters) iters[r] = it[r];

@@ -53,7 +53,10 @@ typedef enum { FMM_RULE_GAUSS3 = 0, FMM_RULE_DUNAVANT7 = 1 } fmm_rule;
 
 typedef struct {
     double k;                 /* wavenumber */
-    int depth;                /* leaf level; 0 = choose from s like deterLmax */
+    int depth;                /* leaf level; 0 = choose from s like deterLmax (octree.c:635-679);
+                                 -1 = the same, capped so that leaf boxes stay at least 1.5 times
+                                 the longest element edge (meshes whose elements are coarse against
+                                 the centroid spacing, e.g. flat faces) */
     int s;                    /* leaf occupancy for the depth rule (reference: 5) */
     int p_level[FMM_MAX_LEVEL + 1]; /* truncation order per level l (index l); 0 = truncNum */
     double eps;               /* truncNum accuracy parameter (reference: 0.05) */
