@@ -120,12 +120,12 @@ __global__ void __launch_bounds__(256, 2) rcr_tile_kernel(RcrPass ps)
     const float *H = SHC ? sH : Hg;
     const float2 *Cc = SHC ? sC : Cg;
     if (threadIdx.x < TC) {
-        // column e = translation t x nrhs + right-hand side r; each right-hand side has its own
-        // copy of the source and destination levels
+        // column e = translation t x nrhs + right-hand side r; the expansions hold the columns
+        // of a box next to each other ([box][rhs][p^2]), so a tile's sources are contiguous runs
         bool v = (int)threadIdx.x < cnt;
         int e = it.y + threadIdx.x, t = e / ps.nrhs, r = e - t * ps.nrhs;
-        s_src[threadIdx.x] = v ? ps.g_src[t] + r * ps.nsrc : -1;
-        s_dst[threadIdx.x] = v ? ps.g_dst[t] + r * ps.ndst : -1;
+        s_src[threadIdx.x] = v ? ps.g_src[t] * ps.nrhs + r : -1;
+        s_dst[threadIdx.x] = v ? ps.g_dst[t] * ps.nrhs + r : -1;
     }
     if (SHC) {
         const int rs = rot_size(p), cs = coax_size(p);

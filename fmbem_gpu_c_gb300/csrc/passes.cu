@@ -118,7 +118,7 @@ __global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *
     typedef typename Cx<T>::t C;
     int b = blockIdx.x, ppl = pl * pl;
     x += (size_t)blockIdx.y * nf; // right-hand side blockIdx.y
-    Cm += (size_t)blockIdx.y * nb * ppl;
+    typename Cx<T>::t *out = Cm + ((size_t)b * gridDim.y + blockIdx.y) * ppl; // [box][rhs][p^2]
     int s0 = leaf_beg[b], s1 = leaf_beg[b + 1];
     for (int i = threadIdx.x; i < ppl; i += blockDim.x) {
         int q = i;
@@ -136,7 +136,7 @@ __global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *
             ar += xr * u.x - xi * u.y;
             ai += xr * u.y + xi * u.x;
         }
-        Cm[(size_t)b * ppl + i] = mk2(ar, ai);
+        out[i] = mk2(ar, ai);
     }
 }
 
@@ -215,7 +215,6 @@ __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_lea
     int ppl = pl * pl;
     x += (size_t)blockIdx.y * nf; // right-hand side blockIdx.y
     y += (size_t)blockIdx.y * nf;
-    Dl += (size_t)blockIdx.y * nb * ppl;
     T ar = 0, ai = 0;
     for (int s = near_beg[e] + lane; s < near_beg[e + 1]; s += 32) {
         C v = nearv[s];
@@ -224,7 +223,7 @@ __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_lea
         ar += v.x * xr - v.y * xi;
         ai += v.x * xi + v.y * xr;
     }
-    const C *D = Dl + (size_t)elem_leaf[e] * ppl;
+    const C *D = Dl + ((size_t)elem_leaf[e] * gridDim.y + blockIdx.y) * ppl; // [box][rhs][p^2]
     const C *R = Rv + (size_t)e * ppl;
     for (int i = lane; i < ppl; i += 32) {
         int q = i;
@@ -529,7 +528,7 @@ int set_dir_dist(const int *dd)
     return FMM_OK;
 }
 
-// The FP32 expansions hold rhs_cap32 right-hand sides, level by level ([rhs][box][p^2]).
+// The FP32 expansions hold rhs_cap32 right-hand sides, level by level ([box][rhs][p^2]).
 static int ensure_rhs32(Plan *P, int nrhs)
 {
     if (nrhs <= P->rhs_cap32) return FMM_OK;

@@ -114,12 +114,13 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// destination / source expansion of row r of tile (it): column e = translation t x nrhs + r
+// destination / source expansion of row r of tile (it): column e = translation t x nrhs + r,
+// expansions stored [box][rhs][p^2]
 __device__ __forceinline__ int tile_box(const TcPass &ps, int4 it, int r, bool source)
 {
     if (r >= it.z) return -1;
     int e = it.y + r, t = e / ps.nrhs, rr = e - t * ps.nrhs;
-    return source ? ps.g_src[t] + rr * ps.nsrc : ps.g_dst[t] + rr * ps.ndst;
+    return (source ? ps.g_src[t] : ps.g_dst[t]) * ps.nrhs + rr;
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
