@@ -44,7 +44,8 @@ class Info(ctypes.Structure):
                 ("d", ctypes.c_double), ("pt_min", ctypes.c_double * 3), ("p_level", ctypes.c_int * (MAX_LEVEL + 1)),
                 ("num_box", ctypes.c_int * (MAX_LEVEL + 1)), ("num_m2l", ctypes.c_longlong * (MAX_LEVEL + 1)),
                 ("num_near", ctypes.c_longlong), ("device_bytes", ctypes.c_size_t), ("setup_seconds", ctypes.c_double),
-                ("m2l_columns", ctypes.c_int * (MAX_LEVEL + 1)), ("m2l_tensor", ctypes.c_int * (MAX_LEVEL + 1))]
+                ("m2l_columns", ctypes.c_int * (MAX_LEVEL + 1)), ("m2l_tensor", ctypes.c_int * (MAX_LEVEL + 1)),
+                ("expansions_scaled", ctypes.c_int)]
 
 
 _lib = None

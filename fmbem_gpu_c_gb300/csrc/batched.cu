@@ -360,17 +360,20 @@ int launch_rcr_pass(RcrList &Lst, int p, int pin, int pout, int atomic, const fl
 // Shared memory that keeps two CTAs on an SM: 228 KB per SM, 1 KB reserved and the static
 // arrays per CTA.
 static const size_t TWO_CTA_SMEM = (228 * 1024) / 2 - 1024 - 1024;
+// and the most one CTA may take (227 KB less the static column indices)
+const size_t MAX_TILE_SMEM = 227 * 1024 - 1024;
 
 // Columns per CTA: the largest of 64, 32, 16 whose tiles (and, where they also fit, the
-// staged rotation and coaxial blocks) keep two CTAs per SM, else 8 (one CTA per SM, p <= 42).
-// With 16-column groups that gives every thread of the CTA a unit of work down to p = 10.
+// staged rotation and coaxial blocks) keep two CTAs per SM, else 8 (one CTA per SM, p <= 42),
+// else 4 (p <= 60).  With 16-column groups that gives every thread of the CTA a unit of work
+// down to p = 10.
 static void pick_tile(int p, int &tc, int &shc)
 {
     for (tc = 64; tc >= 16; tc /= 2) {
         if (rcr_tile_smem(p, tc, 1) <= TWO_CTA_SMEM) { shc = 1; return; }
         if (rcr_tile_smem(p, tc, 0) <= TWO_CTA_SMEM) { shc = 0; return; }
     }
-    tc = 8;
+    tc = rcr_tile_smem(p, 8, 0) <= MAX_TILE_SMEM ? 8 : 4;
     shc = 0;
 }
 

@@ -317,8 +317,8 @@ int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st)
     if (which == PASS_M2M)
         return launch_rcr_pass(L.m2m, PL.p, L.p, PL.p, 1, P->Hss32, rs, P->PHss32, w, pmax - 1, L.Crr32, L.Cm32, PL.Cm32,
                                nrhs, L.nb, PL.nb, st);
-    return launch_rcr_pass(L.l2l, PL.p, PL.p, L.p, 0, P->Hrr32, rs, P->PHrr32, w, pmax - 1, L.Crr32, PL.Dl32, L.Dl32, nrhs,
-                           PL.nb, L.nb, st);
+    return launch_rcr_pass(L.l2l, PL.p, PL.p, L.p, 0, P->Hrr32, rs, P->PHrr32, w, pmax - 1, L.Crr32L ? L.Crr32L : L.Crr32,
+                           PL.Dl32, L.Dl32, nrhs, PL.nb, L.nb, st);
 }
 
 // The mixed path's translation passes for nrhs columns: zero the expansions, M2M up, the

@@ -87,7 +87,7 @@ static void free_plan(Plan *P)
     for (int l = 0; l <= FMM_MAX_LEVEL + 1; l++) {
         LevelDev &L = P->lev[l];
         F(L.parent); F(L.octant); F(L.child_beg); F(L.child_list); F(L.sr_beg); F(L.sr_src); F(L.sr_dir);
-        F(L.Cm64); F(L.Dl64); F(L.Cm32); F(L.Dl32); F(L.Csr64); F(L.Csr32); F(L.Crr64); F(L.Crr32);
+        F(L.Cm64); F(L.Dl64); F(L.Cm32); F(L.Dl32); F(L.Csr64); F(L.Csr32); F(L.Crr64); F(L.Crr32); F(L.Crr32L);
         for (RcrList *R : {&L.m2l, &L.m2m, &L.l2l}) { F(R->items); F(R->src); F(R->dst); }
         F(L.tc.B); F(L.tc.items);
     }
@@ -184,11 +184,11 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
         P->pmax = std::max(P->pmax, p);
     }
     P->pleaf = P->lev[P->lmax].p;
-    if (P->opt.build_mixed && rcr_tile_smem(P->pmax, 8, 0) > 227 * 1024) {
-        // the batched FP32 translations keep two p^2 x 8 complex tiles in shared memory
+    if (P->opt.build_mixed && rcr_tile_smem(P->pmax, 4, 0) > MAX_TILE_SMEM) {
+        // the batched FP32 translations keep two p^2 x 4 complex tiles in shared memory at least
         P->opt.build_mixed = 0;
         snprintf(P->mixed_note, sizeof(P->mixed_note),
-                 "mixed precision needs truncation orders <= 42 (this plan has %d); use FMM_FP64", P->pmax);
+                 "mixed precision needs truncation orders <= 60 (this plan has %d); use FMM_FP64", P->pmax);
     }
     if (P->pleaf > 40) { fmm_set_error("leaf truncation order %d above 40", P->pleaf); free_plan(P); return FMM_ERR_ARG; }
     CTRY(dev_alloc(P, (void **)&P->V_dev, sizeof(double) * P->V.size()));
@@ -287,6 +287,7 @@ extern "C" int fmm_plan_info(const fmm_plan *plan, fmm_info *info)
         info->m2l_columns[l] = P->opt.build_mixed ? (P->lev[l].tc.on ? 128 : P->lev[l].m2l.tc) : 0;
         info->m2l_tensor[l] = P->opt.build_mixed && P->lev[l].tc.on ? 1 : 0;
     }
+    info->expansions_scaled = P->opt.build_mixed && P->scaled ? 1 : 0;
     info->num_near = P->num_near;
     info->device_bytes = P->device_bytes;
     info->setup_seconds = P->setup_seconds;

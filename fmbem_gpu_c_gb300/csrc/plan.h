@@ -52,7 +52,8 @@ struct LevelDev {
     double2 *Csr64 = nullptr;     // NDIST coaxial (S|R) blocks at order p
     float2 *Csr32 = nullptr;
     double2 *Crr64 = nullptr;     // coaxial (R|R) at order p_{l-1} for M2M into / L2L out of level l-1
-    float2 *Crr32 = nullptr;
+    float2 *Crr32 = nullptr;      // FP32 (R|R) of the M2M (and of the L2L when not scaled)
+    float2 *Crr32L = nullptr;     // FP32 (R|R) of the L2L in plans with scaled expansions
     // batched passes of the mixed path: M2L of this level, M2M (this level -> parents),
     // L2L (parents -> this level)
     RcrList m2l, m2m, l2l;
@@ -105,6 +106,9 @@ struct Plan {
     int *tc_err = nullptr;        // set by the tensor-core M2L when one of its waits gives up
     size_t device_bytes = 0;
     char mixed_note[160] = "plan was created without build_mixed";
+    // FP32 expansions scaled by degree (low k t): multipole d_n M_n, local L_n / d_n per level
+    int scaled = 0;
+    std::vector<double> dsc[FMM_MAX_LEVEL + 2];
     double setup_seconds = 0.0;
     // profiling
     int profiling = 0;
@@ -161,6 +165,7 @@ int check_tc_error(Plan *P);
 int build_rcr_lists(Plan *P);
 int tune_rcr_tiles(Plan *P);
 size_t rcr_tile_smem(int p, int tc, int shc);
+extern const size_t MAX_TILE_SMEM;
 int launch_rcr_pass(RcrList &Lst, int p, int pin, int pout, int atomic, const float *H, int hstride,
                     const float2 *PH, int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst,
                     int nrhs, int nsrc, int ndst, cudaStream_t st);

@@ -166,6 +166,19 @@ __global__ void to_float_kernel(const double *in, float *out, size_t n)
         out[i] = (float)in[i];
 }
 
+// FP32 copy of an [rows][p^2] table with entry (n, m) times d[n]
+__global__ void to_float_degree_kernel(const double2 *in, float2 *out, size_t n, int p, const double *d)
+{
+    const int pp = p * p;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        int nm = (int)(i % pp), q = (int)sqrtf((float)nm);
+        while (q * q > nm) q--;
+        while ((q + 1) * (q + 1) <= nm) q++;
+        double2 v = in[i];
+        out[i] = make_float2((float)(v.x * d[q]), (float)(v.y * d[q]));
+    }
+}
+
 static void to_float(const double *in, float *out, size_t n, cudaStream_t s)
 {
     int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
@@ -356,23 +369,51 @@ __global__ void coax_kernel(double k, const double *tvals, int p, int sr, double
 #undef EE
 }
 
-// The mixed-precision path stores the coaxial blocks in FP32.  At high order and small
-// k t the (S|R) entries grow like h_{2p-2}(k t) and can leave the float range: then the plan
-// is built without the mixed-precision tables (FP64 only) rather than carry inf through the
-// matvec, and a mixed call says why.
-static int check_fp32_range(Plan *P, const double2 *dev, size_t n, int l)
+// The mixed-precision path stores the coaxial blocks in FP32.  At high order and small k t
+// the (S|R) entries grow like h_{2p-2}(k t) (and the multipole coefficients fall like
+// (k r)^n / (2n+1)!!) beyond the float range.  Such plans keep their FP32 expansions scaled
+// by degree: multipoles of level l as d_n M_n, locals as L_n / d_n, with d_n the square root
+// of the largest diagonal (S|R) entry of degree n at that level.  The scaling commutes with
+// the rotations (block-diagonal in n), so only the coaxial blocks (scaled (S|R):
+// C / (d_n' d_n); M2M: d^{l-1}_n' C / d^l_n; L2L: d^{l-1}_n C / d^l_n') and the element
+// tables (both times d^{lmax}_n) change; the kernels do not.  The scaled blocks are near
+// one in size, the expansions of order one.  Plans whose largest unscaled entry stays below
+// 1e20 keep the plain tables.
+static const double SCALE_ABOVE = 1e20;
+
+static double max_abs(const std::vector<double2> &h)
 {
-    std::vector<double2> h(n);
-    FMM_CUDA_TRY(cudaMemcpy(h.data(), dev, sizeof(double2) * n, cudaMemcpyDeviceToHost));
     double mx = 0.0;
-    for (size_t i = 0; i < n; i++) mx = std::max(mx, std::max(fabs(h[i].x), fabs(h[i].y)));
-    if (!(mx < 1e37)) {
-        P->opt.build_mixed = 0;
-        snprintf(P->mixed_note, sizeof(P->mixed_note),
-                 "no mixed-precision tables: level %d coaxial entries reach %.3g, beyond FP32 range (lower p at "
-                 "that level or use FMM_FP64)", l, mx);
+    for (const double2 &v : h) {
+        double a = std::max(fabs(v.x), fabs(v.y));
+        if (!(a <= mx)) mx = a; // NaN propagates
     }
-    return FMM_OK;
+    return mx;
+}
+
+// FP32 copy of coaxial blocks of order p for nmat matrices: entry (n', n) of block m times
+// row[n'] * col[n]
+static std::vector<float2> scaled_coax(const std::vector<double2> &in, int p, int nmat, const std::vector<double> &row,
+                                       const std::vector<double> &col, double *maxout)
+{
+    std::vector<float2> out(in.size());
+    double mx = 0.0;
+    const int cs = coax_size(p);
+    for (int q = 0; q < nmat; q++)
+        for (int m = 0; m < p; m++) {
+            int sz = p - m, off = q * cs + coax_off(p, m);
+            for (int i = 0; i < sz * sz; i++) {
+                int a = i % sz, b = i / sz; // a = n' - m, b = n - m
+                double f = row[m + a] * col[m + b];
+                double2 v = in[off + i];
+                double x = v.x * f, y = v.y * f;
+                double av = std::max(fabs(x), fabs(y));
+                if (!(av <= mx)) mx = av;
+                out[off + i] = make_float2((float)x, (float)y);
+            }
+        }
+    *maxout = mx;
+    return out;
 }
 
 int gen_coax_tables(Plan *P)
@@ -392,6 +433,10 @@ int gen_coax_tables(Plan *P)
     double *tdev = nullptr;
     FMM_CUDA_TRY(cudaMalloc(&scratch, sizeof(double2) * maxScratch));
     FMM_CUDA_TRY(cudaMalloc(&tdev, sizeof(double) * NDIST));
+    // FP64 blocks of every level (host copies kept for the FP32 conversion)
+    std::vector<double2> hsr[FMM_MAX_LEVEL + 2], hrr[FMM_MAX_LEVEL + 2];
+    double unscaled_max = 0.0;
+    int worst_level = P->lmin;
     for (int l = P->lmin; l <= P->lmax; l++) {
         LevelDev &L = P->lev[l];
         int p = L.p;
@@ -404,12 +449,10 @@ int gen_coax_tables(Plan *P)
         FMM_CUDA_TRY(cudaGetLastError());
         FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
         if (P->opt.build_mixed) {
-            int st = check_fp32_range(P, L.Csr64, (size_t)NDIST * coax_size(p), l);
-            if (st != FMM_OK) return st;
-        }
-        if (P->opt.build_mixed) {
-            FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Csr32, sizeof(float2) * NDIST * coax_size(p)));
-            to_float((const double *)L.Csr64, (float *)L.Csr32, (size_t)2 * NDIST * coax_size(p), P->stream);
+            hsr[l].resize((size_t)NDIST * coax_size(p));
+            FMM_CUDA_TRY(cudaMemcpy(hsr[l].data(), L.Csr64, sizeof(double2) * hsr[l].size(), cudaMemcpyDeviceToHost));
+            double mx = max_abs(hsr[l]);
+            if (!(mx <= unscaled_max)) { unscaled_max = mx; worst_level = l; }
         }
         if (l > P->lmin) {
             int pp = P->lev[l - 1].p;
@@ -420,14 +463,78 @@ int gen_coax_tables(Plan *P)
             FMM_CUDA_TRY(cudaGetLastError());
             FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
             if (P->opt.build_mixed) {
-                FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Crr32, sizeof(float2) * coax_size(pp)));
-                to_float((const double *)L.Crr64, (float *)L.Crr32, (size_t)2 * coax_size(pp), P->stream);
+                hrr[l].resize(coax_size(pp));
+                FMM_CUDA_TRY(cudaMemcpy(hrr[l].data(), L.Crr64, sizeof(double2) * hrr[l].size(), cudaMemcpyDeviceToHost));
+                double mx = max_abs(hrr[l]);
+                if (!(mx <= unscaled_max)) { unscaled_max = mx; worst_level = l; }
             }
         }
     }
-    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
     cudaFree(scratch);
     cudaFree(tdev);
+    if (!P->opt.build_mixed) return FMM_OK;
+    if (!std::isfinite(unscaled_max)) {
+        P->opt.build_mixed = 0;
+        snprintf(P->mixed_note, sizeof(P->mixed_note), "no mixed-precision tables: level %d coaxial entries are not finite",
+                 worst_level);
+        return FMM_OK;
+    }
+    P->scaled = unscaled_max >= SCALE_ABOVE;
+    int pall = 0;
+    for (int l = P->lmin; l <= P->lmax; l++) pall = std::max(pall, P->lev[l].p);
+    // d^l_n for n < p_l (1 elsewhere, and for unscaled plans)
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        int p = P->lev[l].p, cs = coax_size(p);
+        P->dsc[l].assign(pall, 1.0);
+        if (!P->scaled) continue;
+        for (int n = 0; n < p; n++) {
+            double mx = 0.0;
+            for (int q = 0; q < NDIST; q++)
+                for (int m = 0; m <= n; m++) {
+                    int sz = p - m;
+                    double2 v = hsr[l][(size_t)q * cs + coax_off(p, m) + (size_t)(n - m) * sz + (n - m)];
+                    mx = std::max(mx, hypot(v.x, v.y));
+                }
+            P->dsc[l][n] = mx > 0.0 && std::isfinite(mx) ? sqrt(mx) : 1.0;
+        }
+    }
+    double scaled_max = 0.0;
+    std::vector<double> ones(pall, 1.0);
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        LevelDev &L = P->lev[l];
+        int p = L.p;
+        std::vector<double> inv(pall, 1.0);
+        for (int n = 0; n < pall; n++) inv[n] = 1.0 / P->dsc[l][n];
+        double mx;
+        std::vector<float2> f = scaled_coax(hsr[l], p, NDIST, inv, inv, &mx);
+        scaled_max = std::max(scaled_max, mx);
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Csr32, sizeof(float2) * f.size()));
+        FMM_CUDA_TRY(cudaMemcpy(L.Csr32, f.data(), sizeof(float2) * f.size(), cudaMemcpyHostToDevice));
+        if (l > P->lmin) {
+            int pp = P->lev[l - 1].p;
+            // M2M: rows are parent degrees (times d^{l-1}), columns child degrees (over d^l; zero
+            // beyond the child's order, whose sources are zero padding); L2L the other way round
+            // (rows beyond the child's order are never read).  Unscaled plans share one plain table.
+            std::vector<double> up_col(pall, P->scaled ? 0.0 : 1.0), down_row(pall, 0.0);
+            for (int n = 0; n < p && n < pall; n++) up_col[n] = down_row[n] = inv[n];
+            f = scaled_coax(hrr[l], pp, 1, P->dsc[l - 1], up_col, &mx);
+            scaled_max = std::max(scaled_max, mx);
+            FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Crr32, sizeof(float2) * f.size()));
+            FMM_CUDA_TRY(cudaMemcpy(L.Crr32, f.data(), sizeof(float2) * f.size(), cudaMemcpyHostToDevice));
+            if (P->scaled) {
+                f = scaled_coax(hrr[l], pp, 1, down_row, P->dsc[l - 1], &mx);
+                scaled_max = std::max(scaled_max, mx);
+                FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Crr32L, sizeof(float2) * f.size()));
+                FMM_CUDA_TRY(cudaMemcpy(L.Crr32L, f.data(), sizeof(float2) * f.size(), cudaMemcpyHostToDevice));
+            }
+        }
+    }
+    if (!(scaled_max < 1e37)) {
+        P->opt.build_mixed = 0;
+        snprintf(P->mixed_note, sizeof(P->mixed_note),
+                 "no mixed-precision tables: coaxial entries reach %.3g%s, beyond FP32 range (lower p or use FMM_FP64)",
+                 scaled_max, P->scaled ? " after scaling" : "");
+    }
     return FMM_OK;
 }
 
@@ -808,8 +915,21 @@ int gen_element_tables(Plan *P)
     if (P->opt.build_mixed) {
         FMM_CUDA_TRY(dev_alloc(P, (void **)&P->U32, sizeof(float2) * tbl));
         FMM_CUDA_TRY(dev_alloc(P, (void **)&P->Rv32, sizeof(float2) * tbl));
-        to_float((const double *)P->U64, (float *)P->U32, 2 * tbl, P->stream);
-        to_float((const double *)P->Rv64, (float *)P->Rv32, 2 * tbl, P->stream);
+        if (P->scaled) {
+            // multipole and local of the leaf level scaled by d_n (see gen_coax_tables)
+            double *dd = nullptr;
+            FMM_CUDA_TRY(cudaMalloc(&dd, sizeof(double) * pl));
+            FMM_CUDA_TRY(cudaMemcpy(dd, P->dsc[P->lmax].data(), sizeof(double) * pl, cudaMemcpyHostToDevice));
+            int blocks = (int)std::min<size_t>((tbl + 255) / 256, 152 * 16);
+            to_float_degree_kernel<<<blocks, 256, 0, P->stream>>>(P->U64, P->U32, tbl, pl, dd);
+            to_float_degree_kernel<<<blocks, 256, 0, P->stream>>>(P->Rv64, P->Rv32, tbl, pl, dd);
+            FMM_CUDA_TRY(cudaGetLastError());
+            FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+            cudaFree(dd);
+        } else {
+            to_float((const double *)P->U64, (float *)P->U32, 2 * tbl, P->stream);
+            to_float((const double *)P->Rv64, (float *)P->Rv32, 2 * tbl, P->stream);
+        }
         FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
     }
     cudaFree(ctr_dev);

@@ -331,8 +331,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
 // The real-embedded operators of one level, split into TF32 hi/lo, in the tile layout:
 // element (o, k) of half h, chunk c holds  Re T (o, k even-even / odd-odd), -Im T (o even, k
 // odd) or Im T (o odd, k even) of coefficient (h CH + o/2, (c KC + k)/2).
+// dinv (plans with scaled FP32 expansions, else null): 1/d_n per degree; the operator maps
+// scaled multipoles to scaled locals, T_ij / (d_n(i) d_n(j)).
 __global__ void tc_split_kernel(const double2 *__restrict__ T, int p, int KC, int nch, int nhalf, int CH, int Nmma,
-                                float *__restrict__ B, size_t total)
+                                const double *__restrict__ dinv, float *__restrict__ B, size_t total)
 {
     const int P2 = p * p, K = 2 * P2;
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
@@ -349,6 +351,7 @@ __global__ void tc_split_kernel(const double2 *__restrict__ T, int p, int KC, in
             double2 t = T[((size_t)d * P2 + h * CH + nr / 2) * P2 + k / 2];
             int po = nr & 1, pi = k & 1;
             v = po == 0 ? (pi == 0 ? t.x : -t.y) : (pi == 0 ? t.y : t.x);
+            if (dinv) v *= dinv[(int)sqrtf((float)(h * CH + nr / 2) + 0.5f)] * dinv[(int)sqrtf((float)(k / 2) + 0.5f)];
         }
         float hi = tf32_trunc((float)v);
         float lo = tf32_trunc((float)(v - (double)hi));
@@ -371,10 +374,19 @@ static int build_tc_level(Plan *P, int l)
     cudaError_t e = dev_alloc(P, (void **)&g.B, sizeof(float) * total);
     if (e != cudaSuccess) { cudaFree(T); fmm_set_error("tensor-core M2L tables: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
     g.B_bytes = sizeof(float) * total;
-    tc_split_kernel<<<152 * 16, 256, 0, P->stream>>>(T, L.p, g.KC, g.nch, g.nhalf, g.CH, g.Nmma, g.B, total);
+    double *dinv = nullptr;
+    if (P->scaled) {
+        std::vector<double> h(L.p);
+        for (int n = 0; n < L.p; n++) h[n] = 1.0 / P->dsc[l][n];
+        e = cudaMalloc(&dinv, sizeof(double) * L.p);
+        if (e == cudaSuccess) e = cudaMemcpy(dinv, h.data(), sizeof(double) * L.p, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { cudaFree(T); cudaFree(dinv); fmm_set_error("tensor-core M2L tables: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
+    }
+    tc_split_kernel<<<152 * 16, 256, 0, P->stream>>>(T, L.p, g.KC, g.nch, g.nhalf, g.CH, g.Nmma, dinv, g.B, total);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
     cudaFree(T);
+    cudaFree(dinv);
     if (e != cudaSuccess) { fmm_set_error("tensor-core M2L tables: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
     return FMM_OK;
 }

@@ -63,8 +63,8 @@ typedef struct {
     int rule;                 /* regular quadrature rule (fmm_rule) */
     double a_re, a_im, b_re, b_im, c_re, c_im; /* operator a I + b L + c M */
     int build_mixed;          /* also build the FP32 tables for FMM_MIXED (skipped, with the reason in
-                                 fmm_last_error of a mixed call, where orders exceed 42 or coaxial
-                                 entries exceed the FP32 range) */
+                                 fmm_last_error of a mixed call, where orders exceed 60 or even the
+                                 degree-scaled coaxial entries exceed the FP32 range) */
     int device;               /* CUDA device ordinal */
     double alpha_re, alpha_im;/* Burton-Miller coupling alpha (0: the conventional operator) */
 } fmm_options;
@@ -83,6 +83,9 @@ typedef struct {
                                             (tcgen05, split TF32, dense per-direction operators; levels with
                                             p <= 16 where plan-time timing found it faster, or all of them
                                             with FMMBEM_TENSOR_M2L=1; none with FMMBEM_TENSOR_M2L=0) */
+    int expansions_scaled;               /* mixed path: 1 where the FP32 expansions are kept scaled by degree
+                                            (low k t, where the plain coaxial entries would leave the FP32
+                                            range): multipoles d_n M_n, locals L_n / d_n per level */
 } fmm_info;
 
 typedef struct fmm_plan fmm_plan;
