@@ -74,6 +74,13 @@ def lib():
                                         ctypes.c_int, c_ip, c_dp]
         L.fmm_solve_many.argtypes = [ctypes.POINTER(c_vp), ctypes.c_int, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp),
                                      ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_ip, c_dp, c_ip]
+        L.fmm_scene_create.argtypes = [ctypes.POINTER(c_vp), ctypes.c_int, ctypes.POINTER(c_vp)]
+        L.fmm_scene_destroy.argtypes = [c_vp]
+        L.fmm_scene_unknowns.argtypes = [c_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
+        L.fmm_scene_matvec.argtypes = [c_vp, c_vp, c_vp, ctypes.c_int]
+        L.fmm_scene_solve.argtypes = [c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      c_ip, c_dp]
+        L.fmm_scene_timings.argtypes = [c_vp, c_dp, c_dp, c_ip, c_dp, c_ip]
         L.fmm_vjp.argtypes = [c_vp, c_vp, c_dp, c_dp, ctypes.c_int, c_vp, ctypes.c_double, ctypes.c_int, c_dp, c_vp]
         L.fmm_far_field.argtypes = [c_vp, c_vp, c_dp, ctypes.c_int, c_vp]
         L.fmm_plane_wave_rhs.argtypes = [c_vp, c_dp, c_vp]
@@ -160,6 +167,79 @@ def solve_many(plans, rhs, tol=1e-6, maxit=500, restart=50, precision=FMM_FP64, 
     if st not in (0, 6):
         _check(st)
     return xs, it, rr, stv
+
+
+class Scene:
+    """Plans solved in lockstep (``fmm_scene_create``): their unknowns form one vector, plan i
+    at ``offsets[i]``; a mixed matvec applies all operators with one set of launches.  The
+    plans must outlive the scene."""
+
+    def __init__(self, plans):
+        self.plans = list(plans)
+        n = len(self.plans)
+        ph = (c_vp * n)(*[p.h.value for p in self.plans])
+        h = c_vp()
+        _check(lib().fmm_scene_create(ph, n, ctypes.byref(h)))
+        self.h = h
+        tot = ctypes.c_longlong()
+        offs = (ctypes.c_longlong * (n + 1))()
+        _check(lib().fmm_scene_unknowns(self.h, ctypes.byref(tot), offs))
+        self.n = int(tot.value)
+        self.offsets = np.array(offs[:], dtype=np.int64)
+
+    def split(self, v):
+        """Per-plan views of a scene vector."""
+        return [v[self.offsets[i]:self.offsets[i + 1]] for i in range(len(self.plans))]
+
+    def join(self, vs):
+        """One scene vector from per-plan vectors."""
+        return np.concatenate([np.asarray(v, dtype=np.complex128) for v in vs])
+
+    def matvec(self, x, precision=FMM_MIXED, out=None):
+        if out is None:
+            if hasattr(x, "data_ptr"):
+                import torch
+                out = torch.empty_like(x)
+            else:
+                x = np.ascontiguousarray(x, dtype=np.complex128)
+                out = np.empty_like(x)
+        _check(lib().fmm_scene_matvec(self.h, _ptr(x), _ptr(out), precision))
+        return out
+
+    def solve(self, b, tol=1e-6, maxit=500, restart=50, precision=FMM_MIXED, x0=None):
+        """Lockstep GMRES over all plans (``fmm_scene_solve``); b is a scene vector or a list of
+        per-plan vectors.  Returns (x, iters, relres, converged) with x a scene vector."""
+        if isinstance(b, (list, tuple)):
+            b = self.join(b)
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.zeros_like(b) if x0 is None else np.ascontiguousarray(x0, dtype=np.complex128).copy()
+        it = np.zeros(len(self.plans), dtype=np.int32)
+        rr = np.zeros(len(self.plans))
+        st = lib().fmm_scene_solve(self.h, _ptr(b), _ptr(x), tol, maxit, restart, precision, it.ctypes.data_as(c_ip),
+                                   rr.ctypes.data_as(c_dp))
+        if st not in (0, 6):
+            _check(st)
+        return x, it, rr, st == 0
+
+    def timings(self):
+        """The last solve: wall seconds, device ms and count of its mixed and FP64 matvecs."""
+        s, mm, fm_ = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        mc, fc = ctypes.c_int(), ctypes.c_int()
+        _check(lib().fmm_scene_timings(self.h, ctypes.byref(s), ctypes.byref(mm), ctypes.byref(mc), ctypes.byref(fm_),
+                                       ctypes.byref(fc)))
+        return {"solve_s": s.value, "mixed_ms": mm.value, "mixed_calls": mc.value, "fp64_ms": fm_.value,
+                "fp64_calls": fc.value}
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            lib().fmm_scene_destroy(self.h)
+            self.h = c_vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Plan:

@@ -25,19 +25,6 @@
 
 namespace fmm {
 
-struct RcrPass {
-    int p, pin, pout, atomic;        // RCR order, source order, destination order
-    int nrhs, nsrc, ndst;            // right-hand sides; boxes per right-hand side in src and dst
-    int hstride, phstride, phoff;    // per-direction strides of H and the phases; phase index m + phoff
-    const float *H;
-    const float2 *PH;
-    const float2 *Cc;                // coaxial blocks, item.w selects one (stride coax_size(p))
-    const float2 *src;               // [boxes][pin^2]
-    float2 *dst;                     // [boxes][pout^2]
-    const int4 *items;               // (direction, first, count, coaxial block) over columns e = t nrhs + r
-    const int *g_src, *g_dst;
-};
-
 static __device__ __forceinline__ void nm_of(int i, int &n, int &m)
 {
     int q = (int)sqrtf((float)i);
@@ -100,19 +87,17 @@ static __device__ __forceinline__ void cmac(float2 &acc, float2 c, float ar, flo
     acc.y = fmaf(c.y, ar, acc.y);
 }
 
-// SHC also stages the direction's rotation block and coaxial block in shared memory, after
-// the two tiles.
+// One tile: item it = (direction, first column, count, coaxial block) of pass ps, with the
+// CTA's dynamic shared memory smem4 and its column indices s_src / s_dst.  SHC also stages
+// the direction's rotation block and coaxial block in shared memory, after the two tiles.
 template <int TC, int CG, int R1, int R2, bool SHC>
-__global__ void __launch_bounds__(256, 2) rcr_tile_kernel(RcrPass ps)
+static __device__ __forceinline__ void rcr_tile(const RcrPass &ps, const int4 it, float4 *smem4, int *s_src, int *s_dst)
 {
-    extern __shared__ float4 smem4[];
     const int p = ps.p, pp = p * p;
     float2 *X = reinterpret_cast<float2 *>(smem4);
     float2 *W = X + (size_t)pp * TC;
     float2 *sC = W + (size_t)pp * TC;
     float *sH = reinterpret_cast<float *>(sC + coax_size(p));
-    __shared__ int s_src[TC], s_dst[TC];
-    const int4 it = ps.items[blockIdx.x];
     const int cnt = it.z;
     const float *Hg = ps.H + (size_t)it.x * ps.hstride;
     const float2 *ph = ps.PH + (size_t)it.x * ps.phstride + ps.phoff;
@@ -268,6 +253,39 @@ __global__ void __launch_bounds__(256, 2) rcr_tile_kernel(RcrPass ps)
     }
 }
 
+template <int TC, int CG, int R1, int R2, bool SHC>
+__global__ void __launch_bounds__(256, 2) rcr_tile_kernel(RcrPass ps)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ int s_src[TC], s_dst[TC];
+    rcr_tile<TC, CG, R1, R2, SHC>(ps, ps.items[blockIdx.x], smem4, s_src, s_dst);
+}
+
+// Persistent form for many passes at once (the translation passes of many plans, one phase
+// of a lockstep matvec): a grid of resident CTAs takes work items (pass, tile) from a device
+// queue, in the order given (longest first), until it is empty.  The queue head is an
+// atomic counter, zeroed before the launch; no CTA waits on another.
+template <int TC, int CG, int R1, int R2, bool SHC>
+__global__ void __launch_bounds__(256, 2) rcr_queue_kernel(const RcrPass *__restrict__ passes, const int *__restrict__ work_pass,
+                                                           const int4 *__restrict__ work_item, int nwork, int *head,
+                                                           const int *__restrict__ pass_owner, const int *__restrict__ active)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ int s_src[TC], s_dst[TC];
+    __shared__ int s_w;
+    for (;;) {
+        if (threadIdx.x == 0) s_w = atomicAdd(head, 1);
+        __syncthreads();
+        const int w = s_w;
+        if (w >= nwork) break;
+        const int pi = work_pass[w];
+        // items of passes whose owner is switched off (a converged body) are skipped
+        if (!active || active[pass_owner[pi]])
+            rcr_tile<TC, CG, R1, R2, SHC>(passes[pi], work_item[w], smem4, s_src, s_dst);
+        __syncthreads();
+    }
+}
+
 size_t rcr_tile_smem(int p, int tc, int shc)
 {
     size_t s = 2 * (size_t)p * p * tc * sizeof(float2);
@@ -284,6 +302,85 @@ static int launch_tile(const RcrPass &ps, int n_items, size_t sm, cudaStream_t s
     rcr_tile_kernel<TC, CG, R1, R2, SHC><<<n_items, 256, sm, st>>>(ps);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
+}
+
+template <int TC, int CG, int R1, int R2, bool SHC>
+static const void *queue_fn()
+{
+    return (const void *)rcr_queue_kernel<TC, CG, R1, R2, SHC>;
+}
+
+template <int TC, int CG, int R1, int R2, bool SHC>
+static int queue_prep(size_t sm, int nwork, int *grid)
+{
+    static size_t attr = 0;
+    const void *fn = queue_fn<TC, CG, R1, R2, SHC>();
+    int e = raise_smem_limit(fn, sm, &attr);
+    if (e) return e;
+    int dev = 0, nsm = 0, per_sm = 0;
+    FMM_CUDA_TRY(cudaGetDevice(&dev));
+    FMM_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    FMM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, sm));
+    *grid = std::max(1, std::min(nwork, nsm * std::max(per_sm, 1)));
+    return FMM_OK;
+}
+
+// Raise the queue kernel's shared-memory limit and size its grid: every CTA resident at once
+// (SMs x CTAs per SM at this shared memory), no more than the items.
+int rcr_queue_prepare(int tc, int shc, size_t sm, int nwork, int *grid)
+{
+    if (shc) {
+        switch (tc) {
+        case 64: return queue_prep<64, 16, 2, 1, true>(sm, nwork, grid);
+        case 32: return queue_prep<32, 16, 2, 1, true>(sm, nwork, grid);
+        case 16: return queue_prep<16, 16, 2, 1, true>(sm, nwork, grid);
+        default: return queue_prep<8, 8, 4, 2, true>(sm, nwork, grid);
+        }
+    }
+    switch (tc) {
+    case 64: return queue_prep<64, 16, 2, 1, false>(sm, nwork, grid);
+    case 32: return queue_prep<32, 16, 2, 1, false>(sm, nwork, grid);
+    case 16: return queue_prep<16, 16, 2, 1, false>(sm, nwork, grid);
+    case 4: return queue_prep<4, 4, 8, 4, false>(sm, nwork, grid);
+    default: return queue_prep<8, 8, 4, 2, false>(sm, nwork, grid);
+    }
+}
+
+#define QUEUE_LAUNCH(TC, CG, R1, R2, SHC) \
+    rcr_queue_kernel<TC, CG, R1, R2, SHC><<<grid, 256, sm, st>>>(passes, work_pass, work_item, nwork, head, pass_owner, active)
+
+int launch_rcr_queue(int tc, int shc, const RcrPass *passes, const int *work_pass, const int4 *work_item, int nwork,
+                     int *head, const int *pass_owner, const int *active, size_t sm, int grid, cudaStream_t st)
+{
+    if (nwork <= 0) return FMM_OK;
+    if (shc) {
+        switch (tc) {
+        case 64: QUEUE_LAUNCH(64, 16, 2, 1, true); break;
+        case 32: QUEUE_LAUNCH(32, 16, 2, 1, true); break;
+        case 16: QUEUE_LAUNCH(16, 16, 2, 1, true); break;
+        default: QUEUE_LAUNCH(8, 8, 4, 2, true); break;
+        }
+    } else {
+        switch (tc) {
+        case 64: QUEUE_LAUNCH(64, 16, 2, 1, false); break;
+        case 32: QUEUE_LAUNCH(32, 16, 2, 1, false); break;
+        case 16: QUEUE_LAUNCH(16, 16, 2, 1, false); break;
+        case 4: QUEUE_LAUNCH(4, 4, 8, 4, false); break;
+        default: QUEUE_LAUNCH(8, 8, 4, 2, false); break;
+        }
+    }
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+#undef QUEUE_LAUNCH
+
+void rcr_list_items(const RcrList &Lst, std::vector<int4> &items)
+{
+    items.clear();
+    int nkeys = (int)Lst.key_beg.size() - 1;
+    for (int d = 0; d < nkeys; d++)
+        for (int a = Lst.key_beg[d]; a < Lst.key_beg[d + 1]; a += Lst.tc)
+            items.push_back(make_int4(d, a, std::min(Lst.tc, Lst.key_beg[d + 1] - a), Lst.key_w[d]));
 }
 
 // Items of a pass for nrhs right-hand sides: each direction's translations x right-hand
@@ -311,34 +408,17 @@ static int ensure_items(RcrList &Lst, int nrhs)
     return FMM_OK;
 }
 
-int launch_rcr_pass(RcrList &Lst, int p, int pin, int pout, int atomic, const float *H, int hstride,
-                    const float2 *PH, int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst,
-                    int nrhs, int nsrc, int ndst, cudaStream_t st)
+int launch_rcr_pass(RcrList &Lst, RcrPass ps, cudaStream_t st)
 {
     if (Lst.key_beg.empty() || Lst.key_beg.back() == 0) return FMM_OK;
     {
-        int e = ensure_items(Lst, nrhs);
+        int e = ensure_items(Lst, ps.nrhs);
         if (e) return e;
     }
-    RcrPass ps;
-    ps.p = p;
-    ps.pin = pin;
-    ps.pout = pout;
-    ps.atomic = atomic;
-    ps.nrhs = nrhs;
-    ps.nsrc = nsrc;
-    ps.ndst = ndst;
-    ps.hstride = hstride;
-    ps.phstride = phstride;
-    ps.phoff = phoff;
-    ps.H = H;
-    ps.PH = PH;
-    ps.Cc = Cc;
-    ps.src = src;
-    ps.dst = dst;
     ps.items = Lst.items;
     ps.g_src = Lst.src;
     ps.g_dst = Lst.dst;
+    const int p = ps.p;
     size_t sm = rcr_tile_smem(p, Lst.tc, Lst.shc);
     if (Lst.shc) {
         switch (Lst.tc) {

@@ -303,22 +303,59 @@ static int launch_m2l_level(Plan *P, int l, const char *tname)
     return FMM_OK;
 }
 
+static RcrPass make_pass(int p, int pin, int pout, int atomic, const float *H, int hstride, const float2 *PH,
+                         int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst, int nrhs, int nsrc,
+                         int ndst)
+{
+    RcrPass ps;
+    ps.p = p;
+    ps.pin = pin;
+    ps.pout = pout;
+    ps.atomic = atomic;
+    ps.nrhs = nrhs;
+    ps.nsrc = nsrc;
+    ps.ndst = ndst;
+    ps.hstride = hstride;
+    ps.phstride = phstride;
+    ps.phoff = phoff;
+    ps.H = H;
+    ps.PH = PH;
+    ps.Cc = Cc;
+    ps.src = src;
+    ps.dst = dst;
+    ps.items = nullptr;
+    ps.g_src = ps.g_dst = nullptr;
+    return ps;
+}
+
 // One batched FP32 pass of the mixed path for level l: PASS_M2M (level l into its parents),
 // PASS_M2L (level l), PASS_L2L (parents into level l).
-int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st)
+RcrList *pass32_desc(Plan *P, int l, int which, int nrhs, RcrPass &ps)
 {
     const int pmax = P->pmax, rs = rot_size(pmax), w = 2 * pmax - 1;
     LevelDev &L = P->lev[l];
-    if (which == PASS_M2L && L.tc.on) return launch_tc_m2l(P, l, nrhs, st);
-    if (which == PASS_M2L)
-        return launch_rcr_pass(L.m2l, L.p, L.p, L.p, 1, P->Hsr32, rs, P->PHsr32, w, pmax - 1, L.Csr32, L.Cm32, L.Dl32,
-                               nrhs, L.nb, L.nb, st);
+    if (which == PASS_M2L) {
+        ps = make_pass(L.p, L.p, L.p, 1, P->Hsr32, rs, P->PHsr32, w, pmax - 1, L.Csr32, L.Cm32, L.Dl32, nrhs, L.nb, L.nb);
+        return &L.m2l;
+    }
+    if (l <= P->lmin) return nullptr;
     LevelDev &PL = P->lev[l - 1];
-    if (which == PASS_M2M)
-        return launch_rcr_pass(L.m2m, PL.p, L.p, PL.p, 1, P->Hss32, rs, P->PHss32, w, pmax - 1, L.Crr32, L.Cm32, PL.Cm32,
-                               nrhs, L.nb, PL.nb, st);
-    return launch_rcr_pass(L.l2l, PL.p, PL.p, L.p, 0, P->Hrr32, rs, P->PHrr32, w, pmax - 1, L.Crr32L ? L.Crr32L : L.Crr32,
-                           PL.Dl32, L.Dl32, nrhs, PL.nb, L.nb, st);
+    if (which == PASS_M2M) {
+        ps = make_pass(PL.p, L.p, PL.p, 1, P->Hss32, rs, P->PHss32, w, pmax - 1, L.Crr32, L.Cm32, PL.Cm32, nrhs, L.nb,
+                       PL.nb);
+        return &L.m2m;
+    }
+    ps = make_pass(PL.p, PL.p, L.p, 0, P->Hrr32, rs, P->PHrr32, w, pmax - 1, L.Crr32L ? L.Crr32L : L.Crr32, PL.Dl32,
+                   L.Dl32, nrhs, PL.nb, L.nb);
+    return &L.l2l;
+}
+
+int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st)
+{
+    if (which == PASS_M2L && P->lev[l].tc.on) return launch_tc_m2l(P, l, nrhs, st);
+    RcrPass ps;
+    RcrList *Lst = pass32_desc(P, l, which, nrhs, ps);
+    return Lst ? launch_rcr_pass(*Lst, ps, st) : FMM_OK;
 }
 
 // The mixed path's translation passes for nrhs columns: zero the expansions, M2M up, the

@@ -1,5 +1,6 @@
 // Plan creation, the public C ABI, and the GMRES / iterative-refinement solver.
 #include "plan.h"
+#include "gmres_core.h"
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -527,197 +528,78 @@ static void axpby(Plan *P, double a, const double2 *x, double b, double2 *y, siz
     axpby_kernel<<<blas_grid(n), 256, 0, P->stream>>>(a, x, b, y, n);
 }
 
-// Restarted GMRES on R columns at once (lockstep): every Krylov step applies the operator to
-// all R columns in one batched matvec; classical Gram-Schmidt applied twice (CGS2), FP64
-// vectors on the device, Hessenberg least squares by Givens rotations on the host per
-// column.  A column stops extending its basis once its residual estimate is below tol[r]
-// (its new basis vectors are zero).  Solves A X = B at `precision`; X (device) holds the
-// initial guess.  Convergence of column r is relative to bref[r].
-static int gmres_batch(Plan *P, const double2 *B, double2 *X, int R, const std::vector<double> &tol, int maxit,
-                       int restart, int precision, const std::vector<double> &bref, std::vector<int> &iters,
-                       std::vector<double> &res, int transpose)
+namespace fmm {
+void launch_axpby(double a, const double2 *x, double b, double2 *y, size_t n, cudaStream_t st)
 {
-    const int n = P->nf, m = restart;
-    const size_t vj = (size_t)R * n; // Krylov vector j of column r at j * vj + r * n
-    std::vector<std::vector<double2>> H(R, std::vector<double2>((size_t)(m + 1) * m)), g(R, std::vector<double2>(m + 1)),
-        cs(R, std::vector<double2>(m)), sn(R, std::vector<double2>(m));
-    std::vector<double2> h1, h2;
-    std::vector<double> beta, hn, alpha(R);
-    std::vector<int> kdim(R), running(R);
-    iters.assign(R, 0);
-    res.assign(R, 0.0);
-    int total = 0;
-    while (true) {
-        // R = B - A X, its norms, and which columns still need work
-        int st = run_matvec(P, X, P->gm_r, precision, transpose, R);
-        if (st) return st;
-        axpby(P, 1.0, B, -1.0, P->gm_r, (size_t)R * n);
-        if ((st = bnorms(P, P->gm_r, R, beta))) return st;
-        int any = 0;
-        for (int r = 0; r < R; r++) {
-            res[r] = bref[r] > 0 ? beta[r] / bref[r] : 0.0;
-            if (!std::isfinite(res[r])) { fmm_set_error("GMRES residual of column %d is not finite", r); return FMM_ERR_BREAKDOWN; }
-            running[r] = res[r] > tol[r];
-            any |= running[r];
-            alpha[r] = running[r] ? 1.0 / beta[r] : 0.0;
-            kdim[r] = 0;
-            std::fill(g[r].begin(), g[r].end(), make_double2(0, 0));
-            g[r][0] = make_double2(beta[r], 0);
-        }
-        if (!any || total >= maxit) break;
-        if ((st = bscale(P, alpha, P->gm_r, P->gm_V, R))) return st;
-        int j = 0;
-        for (; j < m && total < maxit; j++) {
-            double2 *Vj = P->gm_V + (size_t)j * vj, *W = P->gm_w;
-            if ((st = run_matvec(P, Vj, W, precision, transpose, R))) return st;
-            if ((st = bdots(P, P->gm_V, vj, n, W, n, j + 1, R, h1))) return st;
-            baxpy_kernel<<<dim3(blas_grid(n) / 2 + 1, 1, R), 256, 0, P->stream>>>(P->gm_V, vj, n, j + 1, P->gm_dev_h, j + 1, W, n, n);
-            if ((st = bdots(P, P->gm_V, vj, n, W, n, j + 1, R, h2))) return st;
-            baxpy_kernel<<<dim3(blas_grid(n) / 2 + 1, 1, R), 256, 0, P->stream>>>(P->gm_V, vj, n, j + 1, P->gm_dev_h, j + 1, W, n, n);
-            if ((st = bnorms(P, W, R, hn))) return st;
-            total++;
-            any = 0;
-            for (int r = 0; r < R; r++) {
-                alpha[r] = 0.0;
-                if (!running[r]) continue;
-                iters[r]++;
-                std::vector<double2> &Hr = H[r], &gr = g[r], &c_ = cs[r], &s_ = sn[r];
-                for (int i = 0; i <= j; i++) {
-                    double2 a = h1[(size_t)r * (j + 1) + i], b = h2[(size_t)r * (j + 1) + i];
-                    Hr[(size_t)i * m + j] = make_double2(a.x + b.x, a.y + b.y);
-                }
-                double h = hn[r];
-                // previous rotations [c s; -conj(s) c], c real
-                for (int i = 0; i < j; i++) {
-                    double2 a = Hr[(size_t)i * m + j], bq = Hr[(size_t)(i + 1) * m + j], c = c_[i], sv = s_[i];
-                    Hr[(size_t)i * m + j] = make_double2(c.x * a.x + sv.x * bq.x - sv.y * bq.y, c.x * a.y + sv.x * bq.y + sv.y * bq.x);
-                    Hr[(size_t)(i + 1) * m + j] =
-                        make_double2(-(sv.x * a.x + sv.y * a.y) + c.x * bq.x, -(sv.x * a.y - sv.y * a.x) + c.x * bq.y);
-                }
-                double2 a = Hr[(size_t)j * m + j];
-                double an = hypot(a.x, a.y), den = hypot(an, h);
-                kdim[r] = j + 1;
-                if (den == 0.0) { // the basis is exhausted: nothing more to add for this column
-                    kdim[r] = j;
-                    running[r] = 0;
-                    continue;
-                }
-                double2 c, sv;
-                if (an == 0.0) { c = make_double2(0, 0); sv = make_double2(1, 0); }
-                else { c = make_double2(an / den, 0); sv = make_double2(a.x / an * h / den, a.y / an * h / den); }
-                c_[j] = c;
-                s_[j] = sv;
-                Hr[(size_t)j * m + j] = make_double2(c.x * a.x + sv.x * h, c.x * a.y + sv.y * h);
-                double2 gj = gr[j];
-                gr[j + 1] = make_double2(-(sv.x * gj.x + sv.y * gj.y), -(sv.x * gj.y - sv.y * gj.x));
-                gr[j] = make_double2(c.x * gj.x, c.x * gj.y);
-                res[r] = hypot(gr[j + 1].x, gr[j + 1].y) / bref[r];
-                if (h == 0.0 || res[r] <= tol[r]) { running[r] = 0; continue; }
-                alpha[r] = 1.0 / h;
-                any = 1;
-            }
-            if (j + 1 < m) {
-                if ((st = bscale(P, alpha, W, P->gm_V + (size_t)(j + 1) * vj, R))) return st;
-            }
-            if (!any) { j++; break; }
-        }
-        // X_r += V_r y_r, y_r from the triangular systems (zero beyond kdim[r])
-        int kmax = 0;
-        for (int r = 0; r < R; r++) kmax = std::max(kmax, kdim[r]);
-        std::vector<double2> Y((size_t)R * std::max(kmax, 1), make_double2(0, 0));
-        for (int r = 0; r < R; r++) {
-            std::vector<double2> &Hr = H[r];
-            for (int i = kdim[r] - 1; i >= 0; i--) {
-                double2 acc = g[r][i];
-                for (int q = i + 1; q < kdim[r]; q++) {
-                    double2 hq = Hr[(size_t)i * m + q], yq = Y[(size_t)r * kmax + q];
-                    acc.x -= hq.x * yq.x - hq.y * yq.y;
-                    acc.y -= hq.x * yq.y + hq.y * yq.x;
-                }
-                double2 d = Hr[(size_t)i * m + i];
-                double dd = d.x * d.x + d.y * d.y;
-                Y[(size_t)r * kmax + i] = make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd);
-            }
-        }
-        if (kmax > 0) {
-            for (auto &v : Y) v = make_double2(-v.x, -v.y); // baxpy subtracts
-            FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_dev_h, Y.data(), sizeof(double2) * Y.size(), cudaMemcpyHostToDevice, P->stream));
-            baxpy_kernel<<<dim3(blas_grid(n) / 2 + 1, 1, R), 256, 0, P->stream>>>(P->gm_V, vj, n, kmax, P->gm_dev_h, kmax, X, n, n);
-        }
-        FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
-    }
-    return FMM_OK;
+    axpby_kernel<<<blas_grid(n), 256, 0, st>>>(a, x, b, y, n);
 }
+} // namespace fmm
 
-// Solve for R columns at `precision`.  FMM_MIXED runs iterative refinement: FP64 residual
-// B - A X, inner batched GMRES on the mixed-precision matvec for the correction, X += D.
+// The columns of one plan for gmres_core / solve_core: R right-hand sides of nf entries one
+// after another, Krylov vector j of column r at V + j R nf + r nf; the operator or its
+// transpose.
+struct PlanOps {
+    Plan *P;
+    int R, transpose;
+    size_t vj() const { return (size_t)R * P->nf; }
+    double2 *V(int j) { return P->gm_V + (size_t)j * vj(); }
+    double2 *r() { return P->gm_r; }
+    double2 *w() { return P->gm_w; }
+    double2 *b() { return P->gm_b; }
+    double2 *x() { return P->gm_x; }
+    double2 *d() { return P->gm_d; }
+    int matvec(const double2 *x, double2 *y, int precision) { return run_matvec(P, x, y, precision, transpose, R); }
+    void axpby(double a, const double2 *x, double b, double2 *y) { ::axpby(P, a, x, b, y, vj()); }
+    int norms(const double2 *W, std::vector<double> &out) { return bnorms(P, W, R, out); }
+    int scale(const std::vector<double> &alpha, const double2 *X, double2 *Y) { return bscale(P, alpha, X, Y, R); }
+    int dots(int nvec, const double2 *W, std::vector<double2> &out)
+    {
+        return bdots(P, P->gm_V, vj(), P->nf, W, P->nf, nvec, R, out);
+    }
+    void sub_dots(int nvec, double2 *W)
+    {
+        baxpy_kernel<<<dim3(blas_grid(P->nf) / 2 + 1, 1, R), 256, 0, P->stream>>>(P->gm_V, vj(), P->nf, nvec, P->gm_dev_h,
+                                                                                  nvec, W, P->nf, P->nf);
+    }
+    int add_basis(std::vector<double2> &y, int kmax, double2 *X)
+    {
+        for (auto &v : y) v = make_double2(-v.x, -v.y); // baxpy subtracts
+        FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_dev_h, y.data(), sizeof(double2) * y.size(), cudaMemcpyHostToDevice, P->stream));
+        baxpy_kernel<<<dim3(blas_grid(P->nf) / 2 + 1, 1, R), 256, 0, P->stream>>>(P->gm_V, vj(), P->nf, kmax, P->gm_dev_h,
+                                                                                  kmax, X, P->nf, P->nf);
+        return FMM_OK;
+    }
+    int copy(double2 *dst, const double2 *src)
+    {
+        FMM_CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(double2) * vj(), cudaMemcpyDeviceToDevice, P->stream));
+        return FMM_OK;
+    }
+    int zero(double2 *dst)
+    {
+        FMM_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(double2) * vj(), P->stream));
+        return FMM_OK;
+    }
+    double2 *tmp_alloc()
+    {
+        double2 *t = nullptr;
+        cudaError_t e = cudaMallocAsync(&t, sizeof(double2) * vj(), P->stream);
+        if (e != cudaSuccess) { fmm_set_error("solver workspace: %s", cudaGetErrorString(e)); return nullptr; }
+        return t;
+    }
+    void tmp_free(double2 *t) { cudaFreeAsync(t, P->stream); }
+    int sync()
+    {
+        FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+        return FMM_OK;
+    }
+    void active(const std::vector<int> &) {} // the batched pass applies every column
+};
+
 static int solve_batch(Plan *P, int R, double tol, int maxit, int restart, int precision, std::vector<int> &iters,
                        std::vector<double> &relres, int transpose = 0)
 {
-    int n = P->nf, st;
-    std::vector<double> bnorm;
-    if ((st = bnorms(P, P->gm_b, R, bnorm))) return st;
-    for (auto &b : bnorm) if (b == 0.0) b = 1.0;
-    std::vector<double> tolv(R, tol);
-    if (precision == FMM_FP64)
-        return gmres_batch(P, P->gm_b, P->gm_x, R, tolv, maxit, restart, FMM_FP64, bnorm, iters, relres, transpose);
-    iters.assign(R, 0);
-    relres.assign(R, 0.0);
-    std::vector<double> rn, itol(R);
-    std::vector<int> it_in;
-    std::vector<double> rr_in;
-    int total = 0;
-    // a zero initial guess needs no FP64 matvec for its residual: the FP64 matvec costs about
-    // 20 mixed ones, so the first correction is solved to 0.5 tol (no lower than 5e-7, a few
-    // times the mixed operator's noise: inner targets near that floor stall GMRES) and one or
-    // two FP64 residuals confirm it
-    std::vector<double> xn;
-    if ((st = bnorms(P, P->gm_x, R, xn))) return st;
-    bool x_zero = true;
-    for (double v : xn) x_zero = x_zero && v == 0.0;
-    for (int outer = 0; outer < 20; outer++) {
-        // residual in FP64; columns already below tol get a zero right-hand side
-        if (outer == 0 && x_zero) {
-            FMM_CUDA_TRY(cudaMemcpyAsync(P->gm_w, P->gm_b, sizeof(double2) * (size_t)R * n, cudaMemcpyDeviceToDevice, P->stream));
-        } else {
-            if ((st = run_matvec(P, P->gm_x, P->gm_w, FMM_FP64, transpose, R))) return st;
-            axpby(P, 1.0, P->gm_b, -1.0, P->gm_w, (size_t)R * n);
-        }
-        if ((st = bnorms(P, P->gm_w, R, rn))) return st;
-        int any = 0;
-        std::vector<double> keep(R);
-        for (int r = 0; r < R; r++) {
-            relres[r] = rn[r] / bnorm[r];
-            keep[r] = relres[r] > tol ? 1.0 : 0.0;
-            any |= relres[r] > tol;
-            itol[r] = std::min(0.1, std::max(5e-7, 0.5 * tol / std::max(relres[r], 1e-300)));
-        }
-        if (!any || total >= maxit) break;
-        // inner right-hand sides in gm_d's partner slot: scale converged columns to zero
-        if ((st = bscale(P, keep, P->gm_w, P->gm_w, R))) return st;
-        FMM_CUDA_TRY(cudaMemsetAsync(P->gm_d, 0, sizeof(double2) * (size_t)R * n, P->stream));
-        std::vector<double> rref(rn);
-        for (auto &v : rref) if (v == 0.0) v = 1.0;
-        // gmres_batch uses gm_r, gm_w (as W), gm_V: move the right-hand sides out of gm_w
-        double2 *rhs = nullptr;
-        FMM_CUDA_TRY(cudaMallocAsync(&rhs, sizeof(double2) * (size_t)R * n, P->stream));
-        FMM_CUDA_TRY(cudaMemcpyAsync(rhs, P->gm_w, sizeof(double2) * (size_t)R * n, cudaMemcpyDeviceToDevice, P->stream));
-        // the mixed matvec is not bitwise reproducible (FP32 atomics), so its residual floor is
-        // ~1e-7; an inner solve that cannot get further hands back to an FP64 residual after a
-        // few restart cycles instead of running to maxit
-        int inner_cap = std::min(maxit - total, std::max(4 * restart, 200));
-        st = gmres_batch(P, rhs, P->gm_d, R, itol, inner_cap, restart, FMM_MIXED, rref, it_in, rr_in, transpose);
-        cudaFreeAsync(rhs, P->stream);
-        if (st) return st;
-        int step = 0;
-        for (int r = 0; r < R; r++) {
-            iters[r] += it_in[r];
-            step = std::max(step, it_in[r]);
-        }
-        total += std::max(step, 1);
-        axpby(P, 1.0, P->gm_d, 1.0, P->gm_x, (size_t)R * n);
-    }
-    return FMM_OK;
+    PlanOps o{P, R, transpose};
+    return solve_core(o, R, tol, maxit, restart, precision, iters, relres);
 }
 
 static int solve_entry(Plan *P, const cuDoubleComplex *b, cuDoubleComplex *x, int R, double tol, int maxit, int restart,

@@ -37,6 +37,20 @@ struct TcM2L {
     int n_items = 0, items_nrhs = 0;
 };
 
+// One batched FP32 translation pass as the tile kernels read it.
+struct RcrPass {
+    int p, pin, pout, atomic;        // RCR order, source order, destination order
+    int nrhs, nsrc, ndst;            // right-hand sides; boxes per right-hand side in src and dst
+    int hstride, phstride, phoff;    // per-direction strides of H and the phases; phase index m + phoff
+    const float *H;
+    const float2 *PH;
+    const float2 *Cc;                // coaxial blocks, item.w selects one (stride coax_size(p))
+    const float2 *src;               // [boxes][rhs][pin^2]
+    float2 *dst;                     // [boxes][rhs][pout^2]
+    const int4 *items;               // (direction, first, count, coaxial block) over columns e = t nrhs + r
+    const int *g_src, *g_dst;        // source and destination box of translation t
+};
+
 struct LevelDev {
     int nb = 0, p = 0;
     int *parent = nullptr;        // [nb], index in level l-1 (l > lmin)
@@ -154,6 +168,11 @@ void drop_graph(Plan *P);
 
 enum { PASS_M2M = 0, PASS_M2L = 1, PASS_L2L = 2 };
 int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st);
+// the list and descriptor of a batched SIMT pass (items not set), or null where the level has none
+RcrList *pass32_desc(Plan *P, int l, int which, int nrhs, RcrPass &ps);
+
+// plan.cu: y = a x + b y over n entries
+void launch_axpby(double a, const double2 *x, double b, double2 *y, size_t n, cudaStream_t st);
 
 // tc_m2l.cu
 int gen_dense_m2l(Plan *P, int l, double2 *T);   // passes.cu
@@ -166,8 +185,14 @@ int build_rcr_lists(Plan *P);
 int tune_rcr_tiles(Plan *P);
 size_t rcr_tile_smem(int p, int tc, int shc);
 extern const size_t MAX_TILE_SMEM;
-int launch_rcr_pass(RcrList &Lst, int p, int pin, int pout, int atomic, const float *H, int hstride,
-                    const float2 *PH, int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst,
-                    int nrhs, int nsrc, int ndst, cudaStream_t st);
+int launch_rcr_pass(RcrList &Lst, RcrPass ps, cudaStream_t st);
+// work items (direction, first column, count, coaxial block) of a list for one right-hand side
+void rcr_list_items(const RcrList &Lst, std::vector<int4> &out);
+// persistent work-queue launch over many passes of one tile shape (tc, shc); smem for the
+// largest order among them; grid from rcr_queue_prepare (resident CTAs)
+int rcr_queue_prepare(int tc, int shc, size_t smem, int nwork, int *grid);
+// (pass_owner, active: items of pass i run only where active[pass_owner[i]] != 0; null: all)
+int launch_rcr_queue(int tc, int shc, const RcrPass *passes, const int *work_pass, const int4 *work_item, int nwork,
+                     int *head, const int *pass_owner, const int *active, size_t smem, int grid, cudaStream_t st);
 
 } // namespace fmm

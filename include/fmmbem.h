@@ -147,6 +147,36 @@ int fmm_solve_many(fmm_plan *const *plans, int n, const cuDoubleComplex *const *
                    double tol, int maxit, int restart, int precision, int nthreads, int *iters, double *relres,
                    int *status);
 
+/* A scene: n plans (bodies of their own meshes and wavenumbers, or one mesh at several
+ * frequencies) solved in lockstep.  Their unknowns form one vector, plan i at offsets[i]
+ * (offsets[n] = the total).  A mixed scene matvec applies every plan's operator with one set
+ * of launches whatever n is: one P2M kernel over all leaf boxes, persistent work-queue
+ * launches per octree level for the M2M and L2L passes and one for all M2L passes (longest
+ * tiles first, one launch per tile shape), one fused L2P + near-field kernel, all replayed
+ * as a CUDA graph; FMM_FP64 runs each plan's FP64 matvec concurrently on the plans' streams.
+ * Every plan needs its mixed-precision tables and must be on one device; the scene uses
+ * the plans' buffers, so a plan is not used elsewhere while a scene call runs, and is
+ * destroyed only after its scenes.  No counterpart in the reference. */
+typedef struct fmm_scene fmm_scene;
+int fmm_scene_create(fmm_plan *const *plans, int n, fmm_scene **scene);
+int fmm_scene_destroy(fmm_scene *scene);
+/* total unknowns; offsets (n + 1 entries) may be NULL */
+int fmm_scene_unknowns(const fmm_scene *scene, long long *total, long long *offsets);
+/* y = A x for all plans at once; x, y of `total` entries, host or device */
+int fmm_scene_matvec(fmm_scene *scene, const cuDoubleComplex *x, cuDoubleComplex *y, int precision);
+/* All plans' systems by one lockstep GMRES (FMM_MIXED: FP64-refined, as fmm_gmres): every
+ * Krylov step is one scene matvec, and a body whose residual estimate is below tol stops
+ * extending its basis while the others continue.  b and x (initial guess in, solution out)
+ * have `total` entries, host or device; iters and relres (n entries each) may be NULL.
+ * Returns FMM_ERR_NOT_CONVERGED if a body missed tol. */
+int fmm_scene_solve(fmm_scene *scene, const cuDoubleComplex *b, cuDoubleComplex *x, double tol, int maxit,
+                    int restart, int precision, int *iters, double *relres);
+/* The last fmm_scene_solve: wall seconds, and the device time (ms) and count of its mixed and
+ * FP64 scene matvecs (CUDA events around each); the rest is the Krylov vector work and the
+ * host.  Any pointer may be NULL. */
+int fmm_scene_timings(const fmm_scene *scene, double *solve_s, double *mixed_ms, int *mixed_calls, double *fp64_ms,
+                      int *fp64_calls);
+
 /* Reverse-mode derivative of a far-field objective with respect to the vertex positions.
  * x solves A x = b, b the plane wave exp(i k dir.c) at the centroids (dir NULL: b does not
  * depend on the mesh); p = F x is the scattered field at the npts points pts (fmm_far_field).
