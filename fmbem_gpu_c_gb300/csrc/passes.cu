@@ -7,7 +7,9 @@
 // e^{i m alpha} e^{-i m' gamma} H_n^{m'm}(beta) (translation.cu:1221-1235), so one real
 // table H per direction serves both rotations and the phases are applied elementwise.
 // The FP64 path is owner-computes: each destination box is owned by one CTA that accumulates
-// all its translations in shared memory and writes once (no atomics, bit-reproducible).
+// all its translations in shared memory and writes once (no atomics, bit-reproducible); on
+// levels with few boxes a box's sources are split over several CTAs whose partial sums are
+// added in a fixed order.
 // The mixed path runs the batched direction-grouped tiles of batched.cu, which add into the
 // expansions with FP32 atomics, so mixed results vary in the last bits from run to run.
 #include "plan.h"
@@ -175,7 +177,8 @@ __global__ void m2l_kernel(int p, int pmax, int pp, const int *__restrict__ sr_b
                            const typename Cx<T>::t *__restrict__ Cm, const int *__restrict__ parent,
                            const unsigned char *__restrict__ octant, const T *__restrict__ Hrr,
                            const typename Cx<T>::t *__restrict__ PHrr, const typename Cx<T>::t *__restrict__ Crr,
-                           const typename Cx<T>::t *__restrict__ Dpar, typename Cx<T>::t *__restrict__ Dl)
+                           const typename Cx<T>::t *__restrict__ Dpar, typename Cx<T>::t *__restrict__ Dl,
+                           typename Cx<T>::t *__restrict__ part)
 {
     typedef typename Cx<T>::t C;
     extern __shared__ unsigned char smraw[];
@@ -184,21 +187,42 @@ __global__ void m2l_kernel(int p, int pmax, int pp, const int *__restrict__ sr_b
     C *sW1 = sX + E2, *sW2 = sW1 + E2, *sY = sW2 + E2;
     int b = blockIdx.x, rs = rot_size(pmax), w = 2 * pmax - 1, cs = coax_size(p);
     // owner-computes: the L2L from the parent and every M2L source, accumulated in shared
-    // memory and written once
+    // memory and written once.  With gridDim.y = S > 1 (levels with few boxes), CTA (b, c)
+    // takes the c-th of S runs of box b's sources (run 0 also the L2L) and writes its partial
+    // sum to part[c][b]; m2l_reduce_kernel adds the runs in order.
+    const int S = gridDim.y, c = blockIdx.y, s0 = sr_beg[b], ns = sr_beg[b + 1] - s0;
+    const int sa = s0 + (int)((long long)ns * c / S), sb = s0 + (int)((long long)ns * (c + 1) / S);
     for (int i = threadIdx.x; i < P2; i += blockDim.x) sY[i] = mk2((T)0, (T)0);
     __syncthreads();
-    if (pp > 0) {
+    if (pp > 0 && c == 0) {
         // L2L: parent local (order pp) translated to this box, truncated to p
         int o = octant[b];
         rcr_block<T>(pp, pmax, Hrr + (size_t)o * rs, PHrr + (size_t)o * w, Crr, Dpar + (size_t)parent[b] * pp * pp, pp,
                      sX, sW1, sW2, sY, p);
     }
-    for (int s = sr_beg[b]; s < sr_beg[b + 1]; s++) {
+    for (int s = sa; s < sb; s++) {
         int src = sr_src[s], dir = sr_dir[s];
         rcr_block<T>(p, pmax, Hsr + (size_t)dir * rs, PHsr + (size_t)dir * w, Csr + (size_t)c_dir_dist[dir] * cs,
                      Cm + (size_t)src * P2, p, sX, sW1, sW2, sY, p);
     }
-    for (int i = threadIdx.x; i < P2; i += blockDim.x) Dl[(size_t)b * P2 + i] = sY[i];
+    C *out = S > 1 ? part + ((size_t)c * gridDim.x + b) * P2 : Dl + (size_t)b * P2;
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) out[i] = sY[i];
+}
+
+// Dl[b] = sum over c of part[c][b], c in order (the result does not depend on the schedule)
+template <typename T>
+__global__ void m2l_reduce_kernel(int S, size_t n, const typename Cx<T>::t *__restrict__ part, typename Cx<T>::t *__restrict__ Dl)
+{
+    typedef typename Cx<T>::t C;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        C a = part[i];
+        for (int c = 1; c < S; c++) {
+            C v = part[(size_t)c * n + i];
+            a.x += v.x;
+            a.y += v.y;
+        }
+        Dl[i] = a;
+    }
 }
 
 
@@ -296,8 +320,17 @@ static int launch_m2l_level(Plan *P, int l, const char *tname)
     int pe = pp > L.p ? pp : L.p;
     size_t sm = 4 * (size_t)pe * pe * sizeof(C);
     timer_begin(P, tname);
-    m2l_kernel<T><<<L.nb, block_for(pe), sm, st>>>(L.p, pmax, pp, L.sr_beg, L.sr_src, L.sr_dir, Hsr, PHsr, Csr, Cm,
-                                                     L.parent, L.octant, Hrr, PHrr, Crr, Dpar, Dl);
+    // FP64 levels with few boxes split each box's sources over S CTAs (P->m2l_split, sized at
+    // plan creation so that the level fills the GPU) and add the runs in a second pass
+    const int S = f64 ? std::max(1, L.m2l_split) : 1;
+    C *part = S > 1 ? (C *)P->m2l_part64 : nullptr;
+    m2l_kernel<T><<<dim3(L.nb, S), block_for(pe), sm, st>>>(L.p, pmax, pp, L.sr_beg, L.sr_src, L.sr_dir, Hsr, PHsr, Csr,
+                                                              Cm, L.parent, L.octant, Hrr, PHrr, Crr, Dpar, Dl, part);
+    if (S > 1) {
+        size_t n = (size_t)L.nb * L.p * L.p;
+        int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+        m2l_reduce_kernel<T><<<blocks, 256, 0, st>>>(S, n, part, Dl);
+    }
     timer_end(P);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;

@@ -92,7 +92,7 @@ static void free_plan(Plan *P)
         for (RcrList *R : {&L.m2l, &L.m2m, &L.l2l}) { F(R->items); F(R->src); F(R->dst); }
         F(L.tc.B); F(L.tc.items);
     }
-    F(P->tc_err);
+    F(P->tc_err); F(P->m2l_part64);
     F(P->Hsr64); F(P->PHsr64); F(P->Hsr32); F(P->PHsr32);
     F(P->V_dev); F(P->F_dev); F(P->elem_leaf); F(P->leaf_beg); F(P->leaf_elem);
     F(P->U64); F(P->Rv64); F(P->U32); F(P->Rv32); F(P->near_beg); F(P->near_col); F(P->near64); F(P->near32);
@@ -211,6 +211,23 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
             CTRY(dev_alloc(P, (void **)&L.Cm32, sizeof(float2) * n));
             CTRY(dev_alloc(P, (void **)&L.Dl32, sizeof(float2) * n));
         }
+    }
+    {
+        // FP64 M2L of levels with few boxes: split each box's sources over up to 16 CTAs so
+        // that the level has ~4 CTAs per SM (each run keeps >= 8 translations)
+        int dev = 0, nsm = 152;
+        CTRY(cudaGetDevice(&dev));
+        CTRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        size_t part = 0;
+        for (int l = P->lmin; l <= P->lmax; l++) {
+            LevelDev &L = P->lev[l];
+            long long target = 4LL * nsm, per_box = L.nb ? L.num_sr / L.nb : 0;
+            int S = L.nb > 0 && L.nb < target ? (int)std::min<long long>(16, (target + L.nb - 1) / L.nb) : 1;
+            S = (int)std::max<long long>(1, std::min<long long>(S, per_box / 8));
+            L.m2l_split = S;
+            if (S > 1) part = std::max(part, (size_t)S * L.nb * L.p * L.p);
+        }
+        if (part) CTRY(dev_alloc(P, (void **)&P->m2l_part64, sizeof(double2) * part));
     }
     TRY(gen_element_tables(P));
     TRY(gen_near_field(P));

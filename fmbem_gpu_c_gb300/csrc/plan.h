@@ -72,6 +72,7 @@ struct LevelDev {
     // L2L (parents -> this level)
     RcrList m2l, m2m, l2l;
     TcM2L tc;
+    int m2l_split = 1;            // FP64 M2L: CTAs per box (source runs), > 1 on levels with few boxes
 };
 
 struct Timer {
@@ -118,6 +119,7 @@ struct Plan {
     cudaGraphExec_t graph_exec = nullptr; // captured mixed translation passes for graph_nrhs columns
     int graph_nrhs = 0, graph_seen = 0;
     int *tc_err = nullptr;        // set by the tensor-core M2L when one of its waits gives up
+    double2 *m2l_part64 = nullptr; // FP64 M2L partial sums of split levels [run][box][p^2]
     size_t device_bytes = 0;
     char mixed_note[160] = "plan was created without build_mixed";
     // FP32 expansions scaled by degree (low k t): multipole d_n M_n, local L_n / d_n per level
