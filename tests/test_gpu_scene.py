@@ -88,3 +88,28 @@ def test_scene_rejects_unsuitable_plans(fm, bodies):
     with pytest.raises(fm.FmmError, match="appears twice"):
         fm.Scene([bodies[0], bodies[1], bodies[0]])
     fp64_only.close()
+
+
+def test_scene_frequency_sweep_matches_mie(fm, oracle):
+    """One mesh at four frequencies (one plan each, orders from the truncation rule): the
+    lockstep solve of the Burton-Miller rigid problem against the Mie series."""
+    V, F = fm.icosphere(4, 0.1)
+    freqs = [500.0, 1000.0, 2000.0, 3000.0]
+    plans = []
+    for f in freqs:
+        k = 2 * np.pi * f / 343.0
+        plans.append(fm.Plan(V, F, k=k, depth=4, rule=1, a=0.5, b=0.0, c=-1.0, alpha=1j / k))
+    sc = fm.Scene(plans)
+    d = np.array([0.0, 0.0, 1.0])
+    x, it, rr, ok = sc.solve([p.plane_wave(d) for p in plans], tol=1e-7, maxit=1000, restart=60, precision=fm.FMM_MIXED)
+    assert ok
+    i = np.arange(40) + 0.5
+    z = 1 - 2 * i / 40
+    ph = np.pi * (1 + 5 ** 0.5) * i
+    pts = np.stack([np.sqrt(1 - z * z) * np.cos(ph), np.sqrt(1 - z * z) * np.sin(ph), z], axis=1)
+    for p, f, xi in zip(plans, freqs, sc.split(x)):
+        k = 2 * np.pi * f / 343.0
+        assert rel(p.far_field(xi, pts), oracle.mie_rigid(k, 0.1, pts)) < 0.02, f
+    sc.close()
+    for p in plans:
+        p.close()
