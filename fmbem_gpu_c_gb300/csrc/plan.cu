@@ -558,6 +558,7 @@ void launch_axpby(double a, const double2 *x, double b, double2 *y, size_t n, cu
 struct PlanOps {
     Plan *P;
     int R, transpose;
+    std::vector<int> on;          // columns whose matvec results are used (empty: all)
     size_t vj() const { return (size_t)R * P->nf; }
     double2 *V(int j) { return P->gm_V + (size_t)j * vj(); }
     double2 *r() { return P->gm_r; }
@@ -565,7 +566,24 @@ struct PlanOps {
     double2 *b() { return P->gm_b; }
     double2 *x() { return P->gm_x; }
     double2 *d() { return P->gm_d; }
-    int matvec(const double2 *x, double2 *y, int precision) { return run_matvec(P, x, y, precision, transpose, R); }
+    // The FP64 matvec runs column by column, so columns that are switched off are skipped
+    // (y = 0 for them); the mixed pass applies all columns at once.
+    int matvec(const double2 *x, double2 *y, int precision)
+    {
+        bool all = true;
+        for (int v : on) all = all && v;
+        if (precision == FMM_MIXED || on.empty() || all) return run_matvec(P, x, y, precision, transpose, R);
+        for (int r = 0; r < R; r++) {
+            const size_t o = (size_t)r * P->nf;
+            if (on[r]) {
+                int st = run_matvec(P, x + o, y + o, precision, transpose, 1);
+                if (st) return st;
+            } else {
+                FMM_CUDA_TRY(cudaMemsetAsync(y + o, 0, sizeof(double2) * P->nf, P->stream));
+            }
+        }
+        return FMM_OK;
+    }
     void axpby(double a, const double2 *x, double b, double2 *y) { ::axpby(P, a, x, b, y, vj()); }
     int norms(const double2 *W, std::vector<double> &out) { return bnorms(P, W, R, out); }
     int scale(const std::vector<double> &alpha, const double2 *X, double2 *Y) { return bscale(P, alpha, X, Y, R); }
@@ -609,13 +627,13 @@ struct PlanOps {
         FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
         return FMM_OK;
     }
-    void active(const std::vector<int> &) {} // the batched pass applies every column
+    void active(const std::vector<int> &a) { on = a; }
 };
 
 static int solve_batch(Plan *P, int R, double tol, int maxit, int restart, int precision, std::vector<int> &iters,
                        std::vector<double> &relres, int transpose = 0)
 {
-    PlanOps o{P, R, transpose};
+    PlanOps o{P, R, transpose, {}};
     return solve_core(o, R, tol, maxit, restart, precision, iters, relres);
 }
 
