@@ -374,27 +374,44 @@ int launch_rcr_queue(int tc, int shc, const RcrPass *passes, const int *work_pas
 }
 #undef QUEUE_LAUNCH
 
-void rcr_list_items(const RcrList &Lst, std::vector<int4> &items)
+void rcr_list_items(const RcrList &Lst, std::vector<int4> &items) { build_items(Lst, 1, Lst.tc, 0, true, items); }
+
+// Work items over the columns e = t nrhs + r of a list: tiles of at most `width` columns of
+// one direction (or octant), item .w = the direction's coaxial block when coax_w.  Where the
+// expansions a pass touches for nrhs columns (ws_bytes) are more than L2 keeps, the
+// destination boxes are cut into Morton ranges and the items ordered range by range, so that
+// the tiles in flight share their sources and destinations in L2.  Each direction's
+// translations are sorted by the Morton rank of their destination, so a range is one
+// contiguous run of every direction.
+static const size_t L2_BUDGET = 48u << 20;
+
+void build_items(const RcrList &Lst, int nrhs, int width, size_t ws_bytes, bool coax_w, std::vector<int4> &items)
 {
     items.clear();
-    int nkeys = (int)Lst.key_beg.size() - 1;
-    for (int d = 0; d < nkeys; d++)
-        for (int a = Lst.key_beg[d]; a < Lst.key_beg[d + 1]; a += Lst.tc)
-            items.push_back(make_int4(d, a, std::min(Lst.tc, Lst.key_beg[d + 1] - a), Lst.key_w[d]));
+    const int nkeys = (int)Lst.key_beg.size() - 1, nd = std::max(Lst.ndst_rank, 1);
+    const long long nblk = std::min<long long>(nd, std::max<long long>(1, (long long)((ws_bytes + L2_BUDGET - 1) / L2_BUDGET)));
+    const int *rk = Lst.dst_rank.data();
+    for (long long k = 0; k < nblk; k++) {
+        const int lo = (int)(k * nd / nblk), hi = (int)((k + 1) * nd / nblk);
+        for (int d = 0; d < nkeys; d++) {
+            int a0 = Lst.key_beg[d], a1 = Lst.key_beg[d + 1];
+            if (nblk > 1) {
+                a0 = (int)(std::lower_bound(rk + Lst.key_beg[d], rk + Lst.key_beg[d + 1], lo) - rk);
+                a1 = (int)(std::lower_bound(rk + Lst.key_beg[d], rk + Lst.key_beg[d + 1], hi) - rk);
+            }
+            const long long e0 = (long long)a0 * nrhs, e1 = (long long)a1 * nrhs;
+            for (long long a = e0; a < e1; a += width)
+                items.push_back(make_int4(d, (int)a, (int)std::min<long long>(width, e1 - a), coax_w ? Lst.key_w[d] : 0));
+        }
+    }
 }
 
-// Items of a pass for nrhs right-hand sides: each direction's translations x right-hand
-// sides, cut into groups of at most tc columns.  Rebuilt when nrhs changes.
-static int ensure_items(RcrList &Lst, int nrhs)
+// Device items of a SIMT pass for nrhs right-hand sides, rebuilt when nrhs changes.
+static int ensure_items(RcrList &Lst, int nrhs, size_t ws_bytes)
 {
     if (Lst.items_nrhs == nrhs) return FMM_OK;
     std::vector<int4> items;
-    int nkeys = (int)Lst.key_beg.size() - 1;
-    for (int d = 0; d < nkeys; d++) {
-        long long e0 = (long long)Lst.key_beg[d] * nrhs, e1 = (long long)Lst.key_beg[d + 1] * nrhs;
-        for (long long a = e0; a < e1; a += Lst.tc)
-            items.push_back(make_int4(d, (int)a, (int)std::min<long long>(Lst.tc, e1 - a), Lst.key_w[d]));
-    }
+    build_items(Lst, nrhs, Lst.tc, ws_bytes, true, items);
     if (items.size() > Lst.items_cap) {
         if (Lst.items) cudaFree(Lst.items);
         Lst.items = nullptr;
@@ -412,7 +429,8 @@ int launch_rcr_pass(RcrList &Lst, RcrPass ps, cudaStream_t st)
 {
     if (Lst.key_beg.empty() || Lst.key_beg.back() == 0) return FMM_OK;
     {
-        int e = ensure_items(Lst, ps.nrhs);
+        size_t ws = ((size_t)ps.nsrc * ps.pin * ps.pin + (size_t)ps.ndst * ps.pout * ps.pout) * sizeof(float2) * ps.nrhs;
+        int e = ensure_items(Lst, ps.nrhs, ws);
         if (e) return e;
     }
     ps.items = Lst.items;
@@ -457,28 +475,42 @@ static void pick_tile(int p, int &tc, int &shc)
     shc = 0;
 }
 
+// drank: Morton rank of each destination box among the ndst boxes of its level.  The list is
+// sorted by key, and within a key by the destination's Morton rank (two stable counting sorts).
 static int upload_list(Plan *P, RcrList &Lst, const std::vector<int> &key, const std::vector<int> &src,
-                       const std::vector<int> &dst, int nkeys, const std::vector<int> &key_w, int p)
+                       const std::vector<int> &dst, int nkeys, const std::vector<int> &key_w, int p,
+                       const std::vector<int> &drank, int ndst)
 {
     int tc, shc;
     pick_tile(p, tc, shc);
     size_t T = key.size();
+    std::vector<int> byrank(std::max<size_t>(T, 1));
+    {
+        std::vector<int> rc(ndst + 1, 0);
+        for (size_t i = 0; i < T; i++) rc[drank[dst[i]] + 1]++;
+        for (int r = 0; r < ndst; r++) rc[r + 1] += rc[r];
+        for (size_t i = 0; i < T; i++) byrank[rc[drank[dst[i]]]++] = (int)i;
+    }
     std::vector<int> cnt(nkeys + 1, 0);
     for (size_t i = 0; i < T; i++) cnt[key[i] + 1]++;
     for (int d = 0; d < nkeys; d++) cnt[d + 1] += cnt[d];
     std::vector<int> gs(std::max<size_t>(T, 1)), gd(std::max<size_t>(T, 1)), fill(nkeys, 0);
-    for (size_t i = 0; i < T; i++) {
+    Lst.dst_rank.assign(T, 0);
+    for (size_t q = 0; q < T; q++) {
+        const int i = byrank[q];
         int pos = cnt[key[i]] + fill[key[i]]++;
         gs[pos] = src[i];
         gd[pos] = dst[i];
+        Lst.dst_rank[pos] = drank[dst[i]];
     }
+    Lst.ndst_rank = ndst;
     Lst.key_beg.assign(cnt.begin(), cnt.end());
     Lst.key_w = key_w;
     Lst.tc = tc;
     Lst.shc = shc;
     Lst.items_nrhs = 0;
     if (T == 0) return FMM_OK;
-    int e = ensure_items(Lst, 1);
+    int e = ensure_items(Lst, 1, 0);
     if (e) return e;
     FMM_CUDA_TRY(dev_alloc(P, (void **)&Lst.src, sizeof(int) * T));
     FMM_CUDA_TRY(dev_alloc(P, (void **)&Lst.dst, sizeof(int) * T));
@@ -491,6 +523,17 @@ static int upload_list(Plan *P, RcrList &Lst, const std::vector<int> &key, const
 // the M2M pairs (box -> parent) and the L2L pairs (parent -> box) grouped by octant.
 int build_rcr_lists(Plan *P)
 {
+    // Morton rank of every box of every level (the level sets hold the boxes' Morton numbers
+    // in first-occurrence order)
+    std::vector<std::vector<int>> rank(P->lmax + 1);
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        const std::vector<long long> &keys = P->tree.sets[l];
+        std::vector<int> ord(keys.size());
+        for (size_t i = 0; i < ord.size(); i++) ord[i] = (int)i;
+        std::sort(ord.begin(), ord.end(), [&](int a, int b) { return keys[a] < keys[b]; });
+        rank[l].assign(keys.size(), 0);
+        for (size_t r = 0; r < ord.size(); r++) rank[l][ord[r]] = (int)r;
+    }
     for (int l = P->lmin; l <= P->lmax; l++) {
         LevelDev &L = P->lev[l];
         if (L.num_sr > 0) {
@@ -506,7 +549,7 @@ int build_rcr_lists(Plan *P)
                     key[t] = dir[t];
                 }
             std::vector<int> kw(P->dir_dist, P->dir_dist + NDIR);
-            int st = upload_list(P, L.m2l, key, src, dst, NDIR, kw, L.p);
+            int st = upload_list(P, L.m2l, key, src, dst, NDIR, kw, L.p, rank[l], L.nb);
             if (st) return st;
         }
         if (l > P->lmin) {
@@ -520,9 +563,9 @@ int build_rcr_lists(Plan *P)
                 self[b] = b;
             }
             std::vector<int> kw(8, 0);
-            int st = upload_list(P, L.m2m, key, self, par, 8, kw, PL.p);
+            int st = upload_list(P, L.m2m, key, self, par, 8, kw, PL.p, rank[l - 1], PL.nb);
             if (st) return st;
-            st = upload_list(P, L.l2l, key, par, self, 8, kw, PL.p);
+            st = upload_list(P, L.l2l, key, par, self, 8, kw, PL.p, rank[l], L.nb);
             if (st) return st;
         }
     }

@@ -21,6 +21,8 @@ struct RcrList {
     size_t items_cap = 0;
     int *src = nullptr, *dst = nullptr;
     std::vector<int> key_beg, key_w;
+    std::vector<int> dst_rank;    // Morton rank of each translation's destination (list order)
+    int ndst_rank = 0;            // boxes of the destination level
     int n_items = 0, items_nrhs = 0;
     int tc = 8, shc = 0;          // columns per item; rotation/coaxial blocks staged in shared memory
 };
@@ -190,6 +192,9 @@ extern const size_t MAX_TILE_SMEM;
 int launch_rcr_pass(RcrList &Lst, RcrPass ps, cudaStream_t st);
 // work items (direction, first column, count, coaxial block) of a list for one right-hand side
 void rcr_list_items(const RcrList &Lst, std::vector<int4> &out);
+// items for nrhs columns in tiles of `width`, ordered by destination Morton ranges where the
+// pass's expansions (ws_bytes) exceed L2
+void build_items(const RcrList &Lst, int nrhs, int width, size_t ws_bytes, bool coax_w, std::vector<int4> &items);
 // persistent work-queue launch over many passes of one tile shape (tc, shc); smem for the
 // largest order among them; grid from rcr_queue_prepare (resident CTAs)
 int rcr_queue_prepare(int tc, int shc, size_t smem, int nwork, int *grid);

@@ -395,14 +395,8 @@ static int ensure_tc_items(LevelDev &L, int nrhs)
 {
     TcM2L &g = L.tc;
     if (g.items_nrhs == nrhs) return FMM_OK;
-    const RcrList &Lst = L.m2l;
     std::vector<int4> items;
-    int nkeys = (int)Lst.key_beg.size() - 1;
-    for (int d = 0; d < nkeys; d++) {
-        long long e0 = (long long)Lst.key_beg[d] * nrhs, e1 = (long long)Lst.key_beg[d + 1] * nrhs;
-        for (long long a = e0; a < e1; a += TC_M)
-            items.push_back(make_int4(d, (int)a, (int)std::min<long long>(TC_M, e1 - a), 0));
-    }
+    build_items(L.m2l, nrhs, TC_M, 2 * (size_t)L.nb * L.p * L.p * sizeof(float2) * nrhs, false, items);
     if (items.size() > g.items_cap) {
         if (g.items) cudaFree(g.items);
         g.items = nullptr;
