@@ -560,9 +560,9 @@ def bodies_arm(args, world, rank, local):
     """The many-body workload: a seeded scene of --bodies bodies (spheres, bumped ellipsoids with
     semi-axes in [0.02, 0.2] m, boxes with edges of 10-100 mm; triangle counts log-uniform in
     [500, 20,000]), each at its own frequency U(0.5, 10) kHz with one plane wave, Burton-Miller
-    rigid operator; all solved in lockstep by fmm_scene_solve (one set of launches per Krylov
-    step for all bodies), against fmm_solve_many (host thread pool, every plan on its own
-    streams) and the same solves one after another."""
+    rigid operator; all solved by fmm_solve_many (host thread pool, every plan on its own
+    streams; the reported value), by the lockstep fmm_scene_solve (one set of launches per
+    Krylov step for all bodies) and one after another."""
     import torch
     import fmbem_gpu_c_gb300 as fm
     torch.cuda.set_device(local)
@@ -623,8 +623,8 @@ def bodies_arm(args, world, rank, local):
     for p in plans:
         p.close()
     line = {
-        "metric": "scene solve s, %d bodies (one plane wave each), lockstep fmm_scene_solve, 1 GB300" % args.bodies,
-        "value": t_scene, "unit": "s", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+        "metric": "scene solve s, %d bodies (one plane wave each), concurrent fmm_solve_many, 1 GB300" % args.bodies,
+        "value": t_conc, "unit": "s", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
         "config": {"workload": "seeded scene: spheres / bumped ellipsoids (0.02-0.2 m) / boxes (10-100 mm), N log-uniform "
                                "in [500, 20000], f ~ U(0.5, 10) kHz, Burton-Miller rigid, tol %g" % tol,
                    "bodies": args.bodies, "triangles_total": int(sum(ns)), "triangles_min": int(min(ns)),
@@ -636,7 +636,7 @@ def bodies_arm(args, world, rank, local):
         "concurrent": {"s": t_conc, "threads": 16, "converged": int((st == 0).sum()), "iters_max": int(it.max()),
                        "iters_sum": int(it.sum()), "relres_max": float(rr.max())},
         "sequential": {"s": t_seq, "all_converged": bool(ok_seq), "max_rel_diff_to_concurrent": diff},
-        "speedup_scene_vs_concurrent": t_conc / t_scene,
+        "speedup_concurrent_vs_sequential": t_seq / t_conc,
         "speedup_scene_vs_sequential": t_seq / t_scene,
         "clocks": clk.summary(),
     }

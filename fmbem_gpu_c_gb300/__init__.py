@@ -81,6 +81,7 @@ def lib():
         L.fmm_scene_solve.argtypes = [c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       c_ip, c_dp]
         L.fmm_scene_timings.argtypes = [c_vp, c_dp, c_dp, c_ip, c_dp, c_ip]
+        L.fmm_scene_set_active.argtypes = [c_vp, c_ip]
         L.fmm_vjp.argtypes = [c_vp, c_vp, c_dp, c_dp, ctypes.c_int, c_vp, ctypes.c_double, ctypes.c_int, c_dp, c_vp]
         L.fmm_far_field.argtypes = [c_vp, c_vp, c_dp, ctypes.c_int, c_vp]
         L.fmm_plane_wave_rhs.argtypes = [c_vp, c_dp, c_vp]
@@ -205,6 +206,14 @@ class Scene:
                 out = np.empty_like(x)
         _check(lib().fmm_scene_matvec(self.h, _ptr(x), _ptr(out), precision))
         return out
+
+    def set_active(self, on=None):
+        """Apply only the plans with on[i] true in later matvecs (None: all); the others get y = 0."""
+        if on is None:
+            _check(lib().fmm_scene_set_active(self.h, None))
+            return
+        a = np.ascontiguousarray(np.asarray(on, dtype=bool).astype(np.int32))
+        _check(lib().fmm_scene_set_active(self.h, a.ctypes.data_as(c_ip)))
 
     def solve(self, b, tol=1e-6, maxit=500, restart=50, precision=FMM_MIXED, x0=None):
         """Lockstep GMRES over all plans (``fmm_scene_solve``); b is a scene vector or a list of

@@ -67,6 +67,7 @@ struct Scene {
     int *pass_owner = nullptr;        // plan of each translation pass
     int *active = nullptr;            // per plan: 1 = apply its operator, 0 = skip it (y = 0)
     std::vector<int> active_host;
+    std::vector<int> user_active;     // fmm_scene_set_active (empty: all) for fmm_scene_matvec
     int *heads = nullptr;
     int n_heads = 0;
     std::vector<std::vector<QueueGroup>> phases;
@@ -729,6 +730,16 @@ extern "C" int fmm_scene_timings(const fmm_scene *scene, double *solve_s, double
     return FMM_OK;
 }
 
+extern "C" int fmm_scene_set_active(fmm_scene *scene, const int *on)
+{
+    Scene *S = (Scene *)scene;
+    if (!S) { fmm_set_error("fmm_scene_set_active: null scene"); return FMM_ERR_ARG; }
+    S->user_active.clear();
+    if (on)
+        for (size_t i = 0; i < S->plans.size(); i++) S->user_active.push_back(on[i] ? 1 : 0);
+    return FMM_OK;
+}
+
 extern "C" int fmm_scene_matvec(fmm_scene *scene, const cuDoubleComplex *x, cuDoubleComplex *y, int precision)
 {
     Scene *S = (Scene *)scene;
@@ -743,7 +754,7 @@ extern "C" int fmm_scene_matvec(fmm_scene *scene, const cuDoubleComplex *x, cuDo
         FMM_CUDA_TRY(cudaMemcpyAsync(S->xin, x, bytes, cudaMemcpyHostToDevice, S->stream));
         xs = S->xin;
     }
-    int st = scene_set_active(S, std::vector<int>(S->plans.size(), 1));
+    int st = scene_set_active(S, S->user_active.empty() ? std::vector<int>(S->plans.size(), 1) : S->user_active);
     if (st) return st;
     st = scene_matvec_dev(S, xs, ys, precision);
     if (st) return st;

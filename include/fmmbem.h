@@ -162,8 +162,10 @@ int fmm_scene_create(fmm_plan *const *plans, int n, fmm_scene **scene);
 int fmm_scene_destroy(fmm_scene *scene);
 /* total unknowns; offsets (n + 1 entries) may be NULL */
 int fmm_scene_unknowns(const fmm_scene *scene, long long *total, long long *offsets);
-/* y = A x for all plans at once; x, y of `total` entries, host or device */
+/* y = A x for all plans at once; x, y of `total` entries, host or device.  Plans switched off by
+ * fmm_scene_set_active (on[i] = 0; on = NULL switches all on) are skipped and get y = 0. */
 int fmm_scene_matvec(fmm_scene *scene, const cuDoubleComplex *x, cuDoubleComplex *y, int precision);
+int fmm_scene_set_active(fmm_scene *scene, const int *on);
 /* All plans' systems by one lockstep GMRES (FMM_MIXED: FP64-refined, as fmm_gmres): every
  * Krylov step is one scene matvec, and a body whose residual estimate is below tol stops
  * extending its basis while the others continue.  b and x (initial guess in, solution out)

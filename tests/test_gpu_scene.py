@@ -62,6 +62,25 @@ def test_scene_matvec_matches_the_plans(fm, bodies):
     sc.close()
 
 
+def test_scene_matvec_on_a_subset_of_plans(fm, bodies):
+    sc = fm.Scene(bodies)
+    rng = np.random.default_rng(22)
+    xs = [rng.standard_normal(p.nf) + 1j * rng.standard_normal(p.nf) for p in bodies]
+    on = [True, False, True, False, True]
+    sc.set_active(on)
+    for rep in range(3):
+        ys = sc.split(sc.matvec(sc.join(xs), fm.FMM_MIXED))
+        for p, xi, yi, a in zip(bodies, xs, ys, on):
+            if a:
+                assert rel(yi, p.matvec(xi, fm.FMM_FP64)) < 1e-5
+            else:
+                assert not np.any(yi)
+    sc.set_active(None)
+    ys = sc.split(sc.matvec(sc.join(xs), fm.FMM_MIXED))
+    assert all(rel(yi, p.matvec(xi, fm.FMM_FP64)) < 1e-5 for p, xi, yi in zip(bodies, xs, ys))
+    sc.close()
+
+
 def test_scene_solve_matches_the_plans(fm, bodies):
     sc = fm.Scene(bodies)
     bs = [p.plane_wave(np.array([0.0, 0.6, 0.8])) for p in bodies]
