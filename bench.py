@@ -21,6 +21,7 @@ import argparse
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -96,7 +97,9 @@ class ClockSampler:
     def __init__(self, gpu):
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % gpu)
+        # the raw samples go to FMMBEM_CLOCKS_DIR (default: the system's temporary directory)
+        out = os.environ.get("FMMBEM_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out, "fmmbem_clocks_rank%d_%d.csv" % (gpu, os.getpid()))
 
     def __enter__(self):
         try:
