@@ -44,14 +44,24 @@ int gmres_core(Ops &o, const double2 *B, double2 *X, int R, const std::vector<do
     iters.assign(R, 0);
     res.assign(R, 0.0);
     int total = 0;
+    // columns whose X changed in the last restart cycle (all at first): only their residuals
+    // are recomputed; the others keep the norm of the same X from before.  (Columns that stop
+    // near the mixed operator's noise floor restart after a few steps, many times; recomputing
+    // every column each time would cost a full matvec per restart.)
+    std::vector<int> changed(R, 1);
+    std::vector<double> beta_prev(R, 0.0);
     const std::vector<int> all(R, 1);
     while (true) {
         // R = B - A X, its norms, and which columns still need work
-        o.active(all);
+        o.active(changed);
         int st = o.matvec(X, o.r(), precision);
         if (st) return st;
         o.axpby(1.0, B, -1.0, o.r());
+        o.active(all);
         if ((st = o.norms(o.r(), beta))) return st;
+        for (int r = 0; r < R; r++)
+            if (!changed[r]) beta[r] = beta_prev[r];
+        beta_prev = beta;
         int any = 0;
         for (int r = 0; r < R; r++) {
             res[r] = bref[r] > 0 ? beta[r] / bref[r] : 0.0;
@@ -64,6 +74,7 @@ int gmres_core(Ops &o, const double2 *B, double2 *X, int R, const std::vector<do
             g[r][0] = make_double2(beta[r], 0);
         }
         if (!any || total >= maxit) break;
+        std::vector<int> ran(running);
         if ((st = o.scale(alpha, o.r(), o.V(0)))) return st;
         int j = 0;
         for (; j < m && total < maxit; j++) {
@@ -139,6 +150,9 @@ int gmres_core(Ops &o, const double2 *B, double2 *X, int R, const std::vector<do
                 Y[(size_t)r * kmax + i] = make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd);
             }
         }
+        // a column that ran in this cycle may have a new X (and its residual vector is needed
+        // if it runs again); one that did not run kept its X
+        changed = ran;
         if (kmax > 0 && (st = o.add_basis(Y, kmax, X))) return st;
         if ((st = o.sync())) return st;
     }
