@@ -267,21 +267,19 @@ __global__ void __launch_bounds__(256, 2) rcr_tile_kernel(RcrPass ps)
 // atomic counter, zeroed before the launch; no CTA waits on another.
 template <int TC, int CG, int R1, int R2, bool SHC>
 __global__ void __launch_bounds__(256, 2) rcr_queue_kernel(const RcrPass *__restrict__ passes, const int *__restrict__ work_pass,
-                                                           const int4 *__restrict__ work_item, int nwork, int *head,
-                                                           const int *__restrict__ pass_owner, const int *__restrict__ active)
+                                                           const int4 *__restrict__ work_item, const int *__restrict__ nwork,
+                                                           int *head)
 {
     extern __shared__ float4 smem4[];
     __shared__ int s_src[TC], s_dst[TC];
     __shared__ int s_w;
+    const int n = *nwork;
     for (;;) {
         if (threadIdx.x == 0) s_w = atomicAdd(head, 1);
         __syncthreads();
         const int w = s_w;
-        if (w >= nwork) break;
-        const int pi = work_pass[w];
-        // items of passes whose owner is switched off (a converged body) are skipped
-        if (!active || active[pass_owner[pi]])
-            rcr_tile<TC, CG, R1, R2, SHC>(passes[pi], work_item[w], smem4, s_src, s_dst);
+        if (w >= n) break;
+        rcr_tile<TC, CG, R1, R2, SHC>(passes[work_pass[w]], work_item[w], smem4, s_src, s_dst);
         __syncthreads();
     }
 }
@@ -347,12 +345,11 @@ int rcr_queue_prepare(int tc, int shc, size_t sm, int nwork, int *grid)
 }
 
 #define QUEUE_LAUNCH(TC, CG, R1, R2, SHC) \
-    rcr_queue_kernel<TC, CG, R1, R2, SHC><<<grid, 256, sm, st>>>(passes, work_pass, work_item, nwork, head, pass_owner, active)
+    rcr_queue_kernel<TC, CG, R1, R2, SHC><<<grid, 256, sm, st>>>(passes, work_pass, work_item, nwork, head)
 
-int launch_rcr_queue(int tc, int shc, const RcrPass *passes, const int *work_pass, const int4 *work_item, int nwork,
-                     int *head, const int *pass_owner, const int *active, size_t sm, int grid, cudaStream_t st)
+int launch_rcr_queue(int tc, int shc, const RcrPass *passes, const int *work_pass, const int4 *work_item,
+                     const int *nwork, int *head, size_t sm, int grid, cudaStream_t st)
 {
-    if (nwork <= 0) return FMM_OK;
     if (shc) {
         switch (tc) {
         case 64: QUEUE_LAUNCH(64, 16, 2, 1, true); break;

@@ -198,8 +198,8 @@ void build_items(const RcrList &Lst, int nrhs, int width, size_t ws_bytes, bool 
 // persistent work-queue launch over many passes of one tile shape (tc, shc); smem for the
 // largest order among them; grid from rcr_queue_prepare (resident CTAs)
 int rcr_queue_prepare(int tc, int shc, size_t smem, int nwork, int *grid);
-// (pass_owner, active: items of pass i run only where active[pass_owner[i]] != 0; null: all)
-int launch_rcr_queue(int tc, int shc, const RcrPass *passes, const int *work_pass, const int4 *work_item, int nwork,
-                     int *head, const int *pass_owner, const int *active, size_t smem, int grid, cudaStream_t st);
+// (*nwork: the number of items, read on the device)
+int launch_rcr_queue(int tc, int shc, const RcrPass *passes, const int *work_pass, const int4 *work_item,
+                     const int *nwork, int *head, size_t smem, int grid, cudaStream_t st);
 
 } // namespace fmm

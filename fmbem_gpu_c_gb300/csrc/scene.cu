@@ -13,7 +13,9 @@
 // Each phase's queue holds (pass, tile) items longest first; the resident CTAs of the
 // persistent kernel take them from an atomic head, so uneven bodies share the GPU without a
 // host round trip per body.  Phases follow one another in stream order: nothing waits on
-// the device.  From the second call on the whole matvec replays as one CUDA graph.
+// the device.  From the second call on the whole matvec replays as one CUDA graph.  Plans
+// can be switched off (converged bodies of a solve): a compaction kernel at the start of the
+// graph keeps, in order, the queue, P2M and L2P items of the switched-on plans only.
 // The lockstep GMRES (gmres_core.h) then costs one scene matvec, three batched dot
 // launches and one host synchronisation per Krylov step for all bodies together; a body
 // whose residual is below tol stops extending its basis while the others continue.
@@ -42,8 +44,18 @@ struct BodyDev {
 struct QueueGroup {               // one persistent launch: the passes of one tile shape in a phase
     int tc = 8, shc = 0, nwork = 0, head = 0, grid = 1;
     size_t smem = 0;
-    int *work_pass = nullptr;
+    int *work_pass = nullptr;         // the items of the switched-on plans (compacted per matvec)
     int4 *work_item = nullptr;
+};
+
+// One list that the compaction kernel filters by the plans' switches, order kept: n items of
+// w0 (and w1) 32-bit words from src0 (src1) to dst0 (dst1); the count to *count.
+struct CompactJob {
+    int n, w0, w1;
+    const int *owner;
+    const int *src0, *src1;
+    int *dst0, *dst1;
+    int *count;
 };
 
 constexpr int SCENE_SIDE = 4;
@@ -64,7 +76,10 @@ struct Scene {
     int2 *zero_items = nullptr;       // (segment, first float2) in chunks of ZERO_CHUNK
     int *zero_owner = nullptr;        // plan of each segment
     int n_zero = 0;
-    int *pass_owner = nullptr;        // plan of each translation pass
+    CompactJob *jobs = nullptr;       // the queue groups, then the P2M and L2P item lists
+    int n_jobs = 0;
+    int *counts = nullptr;            // items left after compaction, per job
+    int2 *p2m_all = nullptr, *l2p_all = nullptr;
     int *active = nullptr;            // per plan: 1 = apply its operator, 0 = skip it (y = 0)
     std::vector<int> active_host;
     std::vector<int> user_active;     // fmm_scene_set_active (empty: all) for fmm_scene_matvec
@@ -122,46 +137,76 @@ __global__ void scene_zero_kernel(float2 *const *ptr, const long long *len, cons
     for (long long i = it.y + threadIdx.x; i < end; i += blockDim.x) p[i] = make_float2(0.f, 0.f);
 }
 
+// Order-keeping compaction of every job's items to those of switched-on plans: one CTA of
+// 1024 threads per job, a block-wide prefix count per 1024 items.
+__global__ void __launch_bounds__(1024) scene_compact_kernel(const CompactJob *__restrict__ jobs,
+                                                             const int *__restrict__ active)
+{
+    const CompactJob J = jobs[blockIdx.x];
+    __shared__ int warp_sum[32], base_s;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) base_s = 0;
+    __syncthreads();
+    for (int b0 = 0; b0 < J.n; b0 += 1024) {
+        const int i = b0 + tid;
+        const bool keep = i < J.n && active[J.owner[i]];
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) warp_sum[wid] = __popc(m);
+        __syncthreads();
+        if (wid == 0) {
+            int v = warp_sum[lane], x = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            warp_sum[lane] = x - v; // exclusive
+        }
+        __syncthreads();
+        const int base = base_s;
+        if (keep) {
+            const int pos = base + warp_sum[wid] + __popc(m & ((1u << lane) - 1));
+            for (int q = 0; q < J.w0; q++) J.dst0[(size_t)pos * J.w0 + q] = J.src0[(size_t)i * J.w0 + q];
+            for (int q = 0; q < J.w1; q++) J.dst1[(size_t)pos * J.w1 + q] = J.src1[(size_t)i * J.w1 + q];
+        }
+        __syncthreads();
+        if (tid == 1023) base_s = base + warp_sum[31] + __popc(m);
+        __syncthreads();
+    }
+    if (tid == 0) *J.count = base_s;
+}
+
 // C_b[n,m] = ik sum_e x_e U_e[n,m] for leaf box b of plan it.x (the plan's p2m_kernel for one
 // column in FP32)
 __global__ void scene_p2m_kernel(const BodyDev *__restrict__ bodies, const int2 *__restrict__ items,
-                                 const double2 *__restrict__ x, const int *__restrict__ active)
+                                 const int *__restrict__ nitems, const double2 *__restrict__ x)
 {
-    const int2 it = items[blockIdx.x];
-    if (!active[it.x]) return;
-    const BodyDev &bd = bodies[it.x];
-    const int b = it.y, ppl = bd.pl * bd.pl;
-    float2 *out = bd.Cm + (size_t)b * ppl;
-    const double2 *xb = x + bd.off;
-    const int s0 = bd.leaf_beg[b], s1 = bd.leaf_beg[b + 1];
-    for (int i = threadIdx.x; i < ppl; i += blockDim.x) {
-        float ar = 0.f, ai = 0.f;
-        for (int s = s0; s < s1; s++) {
-            int e = bd.leaf_elem[s];
-            double2 xe = xb[e];
-            float xr = (float)(-bd.k * xe.y), xi = (float)(bd.k * xe.x);
-            float2 u = bd.U[(size_t)e * ppl + i];
-            ar += xr * u.x - xi * u.y;
-            ai += xr * u.y + xi * u.x;
+    const int n = *nitems;
+    for (int w = blockIdx.x; w < n; w += gridDim.x) {
+        const int2 it = items[w];
+        const BodyDev &bd = bodies[it.x];
+        const int b = it.y, ppl = bd.pl * bd.pl;
+        float2 *out = bd.Cm + (size_t)b * ppl;
+        const double2 *xb = x + bd.off;
+        const int s0 = bd.leaf_beg[b], s1 = bd.leaf_beg[b + 1];
+        for (int i = threadIdx.x; i < ppl; i += blockDim.x) {
+            float ar = 0.f, ai = 0.f;
+            for (int s = s0; s < s1; s++) {
+                int e = bd.leaf_elem[s];
+                double2 xe = xb[e];
+                float xr = (float)(-bd.k * xe.y), xi = (float)(bd.k * xe.x);
+                float2 u = bd.U[(size_t)e * ppl + i];
+                ar += xr * u.x - xi * u.y;
+                ai += xr * u.y + xi * u.x;
+            }
+            out[i] = make_float2(ar, ai);
         }
-        out[i] = make_float2(ar, ai);
     }
 }
 
-// y_e = a x_e + sum_near A_ej x_j + sum_nm D[n,m] Rv_e[n,m]: one warp per element, eight
-// elements of one plan per block (the plan's l2p_near_kernel for one column); y_e = 0 for a
-// plan that is switched off
-__global__ void scene_l2p_kernel(const BodyDev *__restrict__ bodies, const int2 *__restrict__ items,
-                                 const double2 *__restrict__ x, double2 *__restrict__ y, const int *__restrict__ active)
+static __device__ __forceinline__ void l2p_element(const BodyDev &bd, int e, const double2 *__restrict__ x,
+                                                   double2 *__restrict__ y)
 {
-    const int2 it = items[blockIdx.x];
-    const BodyDev &bd = bodies[it.x];
-    const int lane = threadIdx.x & 31, e = it.y + (threadIdx.x >> 5);
-    if (e >= bd.nf) return;
-    if (!active[it.x]) {
-        if (lane == 0) y[bd.off + e] = make_double2(0.0, 0.0);
-        return;
-    }
+    const int lane = threadIdx.x & 31;
     const double2 *xb = x + bd.off;
     float ar = 0.f, ai = 0.f;
     for (int s = bd.near_beg[e] + lane; s < bd.near_beg[e + 1]; s += 32) {
@@ -187,6 +232,22 @@ __global__ void scene_l2p_kernel(const BodyDev *__restrict__ bodies, const int2 
         y[bd.off + e] = make_double2(bd.a.x * xe.x - bd.a.y * xe.y + (double)ar, bd.a.x * xe.y + bd.a.y * xe.x + (double)ai);
     }
 }
+
+// y_e = a x_e + sum_near A_ej x_j + sum_nm D[n,m] Rv_e[n,m]: one warp per element, eight
+// elements of one plan per item (the plan's l2p_near_kernel for one column), over the items of
+// the switched-on plans (y of the others is zeroed before)
+__global__ void scene_l2p_kernel(const BodyDev *__restrict__ bodies, const int2 *__restrict__ items,
+                                 const int *__restrict__ nitems, const double2 *__restrict__ x, double2 *__restrict__ y)
+{
+    const int n = *nitems;
+    for (int w = blockIdx.x; w < n; w += gridDim.x) {
+        const int2 it = items[w];
+        const BodyDev &bd = bodies[it.x];
+        const int e = it.y + (threadIdx.x >> 5);
+        if (e < bd.nf) l2p_element(bd, e, x, y);
+    }
+}
+
 
 // out[plan * nvec + j] += conj(V_j) . W over the chunk's range (grid: x = chunk, y = j); the
 // chunks of switched-off plans (whose W is zero) are skipped
@@ -358,13 +419,14 @@ static int build_scene(Scene *S)
         int st;
         if ((st = upload(S, &S->bodies, bodies))) return st;
         if ((st = upload(S, &S->passes, passes))) return st;
-        if ((st = upload(S, &S->p2m_items, p2m))) return st;
-        if ((st = upload(S, &S->l2p_items, l2p))) return st;
+        if ((st = upload(S, &S->p2m_all, p2m))) return st;
+        if ((st = upload(S, &S->l2p_all, l2p))) return st;
+        FMM_CUDA_TRY(salloc(S, &S->p2m_items, sizeof(int2) * p2m.size()));
+        FMM_CUDA_TRY(salloc(S, &S->l2p_items, sizeof(int2) * l2p.size()));
         if ((st = upload(S, &S->zero_ptr, zptr))) return st;
         if ((st = upload(S, &S->zero_len, zlen))) return st;
         if ((st = upload(S, &S->zero_items, zitems))) return st;
         if ((st = upload(S, &S->zero_owner, zowner))) return st;
-        if ((st = upload(S, &S->pass_owner, powner))) return st;
         S->active_host.assign(n, 1);
         if ((st = upload(S, &S->active, S->active_host))) return st;
         if ((st = upload(S, &S->chunks, chunks))) return st;
@@ -377,6 +439,10 @@ static int build_scene(Scene *S)
     FMM_CUDA_TRY(salloc(S, &S->heads, sizeof(int) * std::max(S->n_heads, 1)));
     int nphase = ph_m2l + 1 + n_up;
     S->phases.assign(nphase, {});
+    const int ng = (int)keys.size();
+    S->n_jobs = ng + 2;
+    FMM_CUDA_TRY(salloc(S, &S->counts, sizeof(int) * S->n_jobs));
+    std::vector<CompactJob> jobs(S->n_jobs);
     for (size_t g = 0; g < keys.size(); g++) {
         std::vector<Work> &W = work[g];
         std::stable_sort(W.begin(), W.end(), [](const Work &a, const Work &b) { return a.cost > b.cost; });
@@ -394,9 +460,30 @@ static int build_scene(Scene *S)
         G.smem = smem[g];
         int st;
         if ((st = rcr_queue_prepare(G.tc, G.shc, G.smem, G.nwork, &G.grid))) return st;
-        if ((st = upload(S, &G.work_pass, wp))) return st;
-        if ((st = upload(S, &G.work_item, wi))) return st;
+        std::vector<int> own(W.size());
+        for (size_t q = 0; q < W.size(); q++) own[q] = powner[wp[q]];
+        int *wp_all = nullptr, *own_d = nullptr;
+        int4 *wi_all = nullptr;
+        if ((st = upload(S, &wp_all, wp))) return st;
+        if ((st = upload(S, &wi_all, wi))) return st;
+        if ((st = upload(S, &own_d, own))) return st;
+        FMM_CUDA_TRY(salloc(S, &G.work_pass, sizeof(int) * wp.size()));
+        FMM_CUDA_TRY(salloc(S, &G.work_item, sizeof(int4) * wi.size()));
+        jobs[g] = CompactJob{G.nwork, 1, 4, own_d, wp_all, (const int *)wi_all, G.work_pass, (int *)G.work_item, S->counts + g};
         S->phases[keys[g].phase].push_back(G);
+    }
+    {
+        std::vector<int> own_p(p2m.size()), own_l(l2p.size());
+        for (size_t q = 0; q < p2m.size(); q++) own_p[q] = p2m[q].x;
+        for (size_t q = 0; q < l2p.size(); q++) own_l[q] = l2p[q].x;
+        int *op = nullptr, *ol = nullptr, st;
+        if ((st = upload(S, &op, own_p))) return st;
+        if ((st = upload(S, &ol, own_l))) return st;
+        jobs[ng] = CompactJob{(int)p2m.size(), 2, 0, op, (const int *)S->p2m_all, nullptr, (int *)S->p2m_items, nullptr,
+                              S->counts + ng};
+        jobs[ng + 1] = CompactJob{(int)l2p.size(), 2, 0, ol, (const int *)S->l2p_all, nullptr, (int *)S->l2p_items, nullptr,
+                                  S->counts + ng + 1};
+        if ((st = upload(S, &S->jobs, jobs))) return st;
     }
     FMM_CUDA_TRY(salloc(S, &S->xin, sizeof(double2) * S->N));
     FMM_CUDA_TRY(salloc(S, &S->yout, sizeof(double2) * S->N));
@@ -414,15 +501,21 @@ static int scene_translate(Scene *S)
     scene_zero_kernel<<<std::max(S->n_zero, 1), 256, 0, st>>>(S->zero_ptr, S->zero_len, S->zero_owner, S->zero_items,
                                                              S->n_zero, S->heads, S->n_heads, S->active);
     FMM_CUDA_TRY(cudaGetLastError());
-    if (S->n_p2m) scene_p2m_kernel<<<S->n_p2m, 128, 0, st>>>(S->bodies, S->p2m_items, S->xin, S->active);
+    // the work of the switched-on plans only, in the same order; y = 0 for the others
+    scene_compact_kernel<<<S->n_jobs, 1024, 0, st>>>(S->jobs, S->active);
+    FMM_CUDA_TRY(cudaGetLastError());
+    FMM_CUDA_TRY(cudaMemsetAsync(S->yout, 0, sizeof(double2) * S->N, st));
+    const int ng = S->n_jobs - 2;
+    if (S->n_p2m)
+        scene_p2m_kernel<<<std::min(S->n_p2m, 152 * 16), 128, 0, st>>>(S->bodies, S->p2m_items, S->counts + ng, S->xin);
     FMM_CUDA_TRY(cudaGetLastError());
     int ev = 0;
     for (auto &groups : S->phases) {
         if (groups.empty()) continue;
         if (groups.size() == 1) {
             const QueueGroup &G = groups[0];
-            int e = launch_rcr_queue(G.tc, G.shc, S->passes, G.work_pass, G.work_item, G.nwork, S->heads + G.head,
-                                     S->pass_owner, S->active, G.smem, G.grid, st);
+            int e = launch_rcr_queue(G.tc, G.shc, S->passes, G.work_pass, G.work_item, S->counts + G.head,
+                                     S->heads + G.head, G.smem, G.grid, st);
             if (e) return e;
             continue;
         }
@@ -433,8 +526,8 @@ static int scene_translate(Scene *S)
         for (int q = 0; q < ns; q++) FMM_CUDA_TRY(cudaStreamWaitEvent(S->side[q], fork, 0));
         for (size_t g = 0; g < groups.size(); g++) {
             const QueueGroup &G = groups[g];
-            int e = launch_rcr_queue(G.tc, G.shc, S->passes, G.work_pass, G.work_item, G.nwork, S->heads + G.head,
-                                     S->pass_owner, S->active, G.smem, G.grid, S->side[g % SCENE_SIDE]);
+            int e = launch_rcr_queue(G.tc, G.shc, S->passes, G.work_pass, G.work_item, S->counts + G.head,
+                                     S->heads + G.head, G.smem, G.grid, S->side[g % SCENE_SIDE]);
             if (e) return e;
         }
         for (int q = 0; q < ns; q++) {
@@ -443,7 +536,9 @@ static int scene_translate(Scene *S)
             FMM_CUDA_TRY(cudaStreamWaitEvent(st, join, 0));
         }
     }
-    if (S->n_l2p) scene_l2p_kernel<<<S->n_l2p, 256, 0, st>>>(S->bodies, S->l2p_items, S->xin, S->yout, S->active);
+    if (S->n_l2p)
+        scene_l2p_kernel<<<std::min(S->n_l2p, 152 * 8), 256, 0, st>>>(S->bodies, S->l2p_items, S->counts + ng + 1, S->xin,
+                                                                      S->yout);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
