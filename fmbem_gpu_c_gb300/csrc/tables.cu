@@ -741,6 +741,19 @@ struct BasisSh {
     double2 *ph;
 };
 
+// Factors of the basis recurrences that depend only on (n, m), tabulated on the host with the
+// same expressions (FP64 square roots and divisions are slow on this GPU; the results are the
+// same to the bit): fac[i] = sqrt((2i+1)/(2i)), s3[m] = sqrt(2m+3), la/lb the three-term
+// Legendre coefficients at n(n+1)/2 + m, and coefA(n, m) / coefB(n, m) at
+// (n + 1) W + m + pb + 1 for n = -1..pb, |m| <= pb + 1 (W = 2 pb + 3).
+struct BasisTab {
+    const double *fac, *s3, *la, *lb, *cA, *cB;
+    int W, pb;
+};
+
+__device__ __forceinline__ double tabA(const BasisTab &T, int n, int m) { return T.cA[(n + 1) * T.W + m + T.pb + 1]; }
+__device__ __forceinline__ double tabB(const BasisTab &T, int n, int m) { return T.cB[(n + 1) * T.W + m + T.pb + 1]; }
+
 __device__ __forceinline__ double2 basis_R(const BasisSh &B, int pb, int n, int m)
 {
     // R_n^m = j_n Q_n^{|m|} e^{i m phi}; zero outside the valid range
@@ -755,7 +768,8 @@ __device__ __forceinline__ double2 basis_R(const BasisSh &B, int pb, int n, int 
 // The basis of order pb at v, spread over the warp: lane 0 runs the spherical Bessel
 // recurrence, lane m (and m + 32) the Legendre column m (its diagonal entry as a product, then
 // the same three-term recurrence in n as legendre_Q), every lane a few phases.
-__device__ __forceinline__ void basis_prepare(const BasisSh &B, int pb, double k, const double *v, int lane)
+__device__ __forceinline__ void basis_prepare(const BasisSh &B, const BasisTab &T, int pb, double k, const double *v,
+                                              int lane)
 {
     double r = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     double ct = 1.0, phi = 0.0;
@@ -764,14 +778,14 @@ __device__ __forceinline__ void basis_prepare(const BasisSh &B, int pb, double k
     const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
     for (int m = lane; m < pb; m += 32) {
         double q = 0.28209479177387814; // 1/sqrt(4 pi)
-        for (int i = 1; i <= m; i++) q = sqrt((2.0 * i + 1.0) / (2.0 * i)) * st * q;
+        for (int i = 1; i <= m; i++) q = __ldg(T.fac + i) * st * q;
         B.Q[m * (m + 1) / 2 + m] = q;
         if (m + 1 < pb) {
-            double q1 = sqrt(2.0 * m + 3.0) * ct * q, q0 = q;
+            double q1 = __ldg(T.s3 + m) * ct * q, q0 = q;
             B.Q[(m + 1) * (m + 2) / 2 + m] = q1;
             for (int n = m + 2; n < pb; n++) {
-                double a = sqrt((4.0 * n * n - 1.0) / ((double)n * n - (double)m * m));
-                double b = sqrt(((n - 1.0) * (n - 1.0) - (double)m * m) / (4.0 * (n - 1.0) * (n - 1.0) - 1.0));
+                const int ix = n * (n + 1) / 2 + m;
+                double a = __ldg(T.la + ix), b = __ldg(T.lb + ix);
                 double q2 = a * (ct * q1 - b * q0);
                 B.Q[n * (n + 1) / 2 + m] = q2;
                 q0 = q1;
@@ -788,14 +802,15 @@ __device__ __forceinline__ void basis_prepare(const BasisSh &B, int pb, double k
 }
 
 // nh . grad R_n^m from the staged basis of orders up to n+1 (integral.cu:284-331)
-__device__ __forceinline__ double2 basis_dirdev(const BasisSh &B, int pb, double k, int n, int mm, const double *nh)
+__device__ __forceinline__ double2 basis_dirdev(const BasisSh &B, const BasisTab &T, int pb, double k, int n, int mm,
+                                                const double *nh)
 {
-    double2 t0 = csub(cscale(basis_R(B, pb, n + 1, mm + 1), coefB(n + 1, -(mm + 1))),
-                      cscale(basis_R(B, pb, n - 1, mm + 1), coefB(n, mm)));
-    double2 t1 = csub(cscale(basis_R(B, pb, n + 1, mm - 1), coefB(n + 1, mm - 1)),
-                      cscale(basis_R(B, pb, n - 1, mm - 1), coefB(n, -mm)));
-    double2 t2 = csub(cscale(basis_R(B, pb, n - 1, mm), coefA(n - 1, mm)),
-                      cscale(basis_R(B, pb, n + 1, mm), coefA(n, mm)));
+    double2 t0 = csub(cscale(basis_R(B, pb, n + 1, mm + 1), tabB(T, n + 1, -(mm + 1))),
+                      cscale(basis_R(B, pb, n - 1, mm + 1), tabB(T, n, mm)));
+    double2 t1 = csub(cscale(basis_R(B, pb, n + 1, mm - 1), tabB(T, n + 1, mm - 1)),
+                      cscale(basis_R(B, pb, n - 1, mm - 1), tabB(T, n, -mm)));
+    double2 t2 = csub(cscale(basis_R(B, pb, n - 1, mm), tabA(T, n - 1, mm)),
+                      cscale(basis_R(B, pb, n + 1, mm), tabA(T, n, mm)));
     double2 f0 = make_double2(0.5 * k * nh[0], -0.5 * k * nh[1]);
     double2 f1 = make_double2(0.5 * k * nh[0], 0.5 * k * nh[1]);
     return cadd(cadd(cmul(f0, t0), cmul(f1, t1)), cscale(t2, k * nh[2]));
@@ -808,7 +823,7 @@ __host__ __device__ __forceinline__ int basis_per_warp(int pb) { return basis_ph
 
 __global__ void element_tables_kernel(const double *V, const int *F, const int *elem_leaf, const double *box_ctr,
                                       int nf, int pl, double k, double2 bco, double2 cco, double2 alpha,
-                                      int rule, double2 *U, double2 *Rv)
+                                      int rule, BasisTab T, double2 *U, double2 *Rv)
 {
     extern __shared__ double2 smem2[];
     double *smem = (double *)smem2;
@@ -835,9 +850,9 @@ __global__ void element_tables_kernel(const double *V, const int *F, const int *
             for (int a = 0; a < 3; a++) v[a] = nod[a] * bb[0] + nod[3 + a] * bb[1] + nod[6 + a] * bb[2] - c[a];
             double wq = c_rule_w[rule][q] * J;
             __syncwarp();
-            basis_prepare(B, pb, k, v, lane);
+            basis_prepare(B, T, pb, k, v, lane);
             for (int i = lane; i < ppl; i += 32) {
-                int n = (int)sqrt((double)i);
+                int n = (int)sqrtf((float)i);
                 while (n * n > i) n--;
                 while ((n + 1) * (n + 1) <= i) n++;
                 int m = i - n * n - n;
@@ -849,7 +864,7 @@ __global__ void element_tables_kernel(const double *V, const int *F, const int *
                 }
                 if (cco.x != 0.0 || cco.y != 0.0) {
                     // directional derivative along nh (integral.cu:284-331)
-                    acc = cadd(acc, cmul(cco, basis_dirdev(B, pb, k, n, mm, nh)));
+                    acc = cadd(acc, cmul(cco, basis_dirdev(B, T, pb, k, n, mm, nh)));
                 }
                 Ue[i] = cadd(Ue[i], cscale(acc, wq));
             }
@@ -857,17 +872,17 @@ __global__ void element_tables_kernel(const double *V, const int *F, const int *
         }
         tri_centroid(nod, y);
         double v[3] = {y[0] - c[0], y[1] - c[1], y[2] - c[2]};
-        basis_prepare(B, pb, k, v, lane);
+        basis_prepare(B, T, pb, k, v, lane);
         double2 *Re = Rv + (size_t)e * ppl;
         for (int i = lane; i < ppl; i += 32) {
-            int n = (int)sqrt((double)i);
+            int n = (int)sqrtf((float)i);
             while (n * n > i) n--;
             while ((n + 1) * (n + 1) <= i) n++;
             int m = i - n * n - n;
             // L2P vector of R + alpha dR/dn at the centroid (Burton-Miller: the target-side
             // normal derivative of the far field)
             double2 r = basis_R(B, pb, n, m);
-            if (alpha.x != 0.0 || alpha.y != 0.0) r = cadd(r, cmul(alpha, basis_dirdev(B, pb, k, n, m, nh)));
+            if (alpha.x != 0.0 || alpha.y != 0.0) r = cadd(r, cmul(alpha, basis_dirdev(B, T, pb, k, n, m, nh)));
             Re[i] = r;
         }
         __syncwarp();
@@ -907,11 +922,41 @@ int gen_element_tables(Plan *P)
     int blocks = std::min((P->nf + warps - 1) / warps, 152 * 32);
     double2 bco = make_double2(P->opt.b_re, P->opt.b_im), cco = make_double2(P->opt.c_re, P->opt.c_im);
     double2 alpha = make_double2(P->opt.alpha_re, P->opt.alpha_im);
+    // the recurrence factors, with the expressions the device used to evaluate per point
+    const int W = 2 * pb + 3, ntri = pb * (pb + 1) / 2;
+    std::vector<double> tab((size_t)(pb + 1) + pb + 2 * ntri + 2 * (size_t)(pb + 2) * W, 0.0);
+    double *fac = tab.data(), *s3 = fac + pb + 1, *la = s3 + pb, *lb = la + ntri, *cA = lb + ntri,
+           *cB = cA + (size_t)(pb + 2) * W;
+    for (int i = 1; i <= pb; i++) fac[i] = sqrt((2.0 * i + 1.0) / (2.0 * i));
+    for (int m = 0; m < pb; m++) s3[m] = sqrt(2.0 * m + 3.0);
+    for (int n = 2; n < pb; n++)
+        for (int m = 0; m + 2 <= n; m++) {
+            la[n * (n + 1) / 2 + m] = sqrt((4.0 * n * n - 1.0) / ((double)n * n - (double)m * m));
+            lb[n * (n + 1) / 2 + m] = sqrt(((n - 1.0) * (n - 1.0) - (double)m * m) / (4.0 * (n - 1.0) * (n - 1.0) - 1.0));
+        }
+    for (int n = -1; n <= pb; n++)
+        for (int m = -(pb + 1); m <= pb + 1; m++) {
+            cA[(size_t)(n + 1) * W + m + pb + 1] = coefA(n, m);
+            cB[(size_t)(n + 1) * W + m + pb + 1] = coefB(n, m);
+        }
+    double *tab_dev = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&tab_dev, sizeof(double) * tab.size()));
+    FMM_CUDA_TRY(cudaMemcpy(tab_dev, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+    BasisTab T;
+    T.fac = tab_dev;
+    T.s3 = tab_dev + (s3 - fac);
+    T.la = tab_dev + (la - fac);
+    T.lb = tab_dev + (lb - fac);
+    T.cA = tab_dev + (cA - fac);
+    T.cB = tab_dev + (cB - fac);
+    T.W = W;
+    T.pb = pb;
     element_tables_kernel<<<blocks, 32 * warps, shm, P->stream>>>(P->V_dev, P->F_dev, P->elem_leaf, ctr_dev, P->nf, pl,
-                                                                   P->opt.k, bco, cco, alpha, P->opt.rule, P->U64,
+                                                                   P->opt.k, bco, cco, alpha, P->opt.rule, T, P->U64,
                                                                    P->Rv64);
     FMM_CUDA_TRY(cudaGetLastError());
     FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    cudaFree(tab_dev);
     if (P->opt.build_mixed) {
         FMM_CUDA_TRY(dev_alloc(P, (void **)&P->U32, sizeof(float2) * tbl));
         FMM_CUDA_TRY(dev_alloc(P, (void **)&P->Rv32, sizeof(float2) * tbl));
