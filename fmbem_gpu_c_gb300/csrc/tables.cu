@@ -638,23 +638,8 @@ __device__ double2 elem_integral_sgl(double k, const double *nod, int kern)
 // d2G/dn_x dn_y (p2Gp1np2n, integral.cu:603-622), taken here in forms that stay accurate for
 // the near pairs: the regularised (Maue) form off the element and the polar finite part on it.
 
-// int_T dG(x, y)/dn_y dS_x = int_T G (ik - 1/r) (y - x).ny / r; zero on the flat element itself
-__device__ double2 elem_dGdny(double k, const double *nod, const double *y, const double *ny, int rule)
-{
-    double nh[3];
-    double J = tri_normal(nod, nh);
-    double2 acc = make_double2(0.0, 0.0);
-    int nq = c_rule_n[rule];
-    for (int q = 0; q < nq; q++) {
-        const double *b = &c_rule_bary[rule][3 * q];
-        double x[3];
-        for (int a = 0; a < 3; a++) x[a] = nod[a] * b[0] + nod[3 + a] * b[1] + nod[6 + a] * b[2];
-        double2 g = green_k(k, x, y, ny, 1);   // G (ik - 1/r) (x - y).ny / r
-        double wq = c_rule_w[rule][q] * J;
-        acc.x -= wq * g.x; acc.y -= wq * g.y;
-    }
-    return acc;
-}
+// K' = int_T dG(x, y)/dn_y dS_x = int_T G (ik - 1/r) (y - x).ny / r (zero on the flat element
+// itself) is taken with the other regular integrals in elem_integrals_fused.
 
 // number of equal segments of an edge of length len seen from distance dist: no longer than
 // dist, so that the 8-point rule converges like 4.2^-16 on the 1/r^2 and 1/r^3 integrands
@@ -697,13 +682,10 @@ __device__ double2 elem_hyper_self(double k, const double *nod)
 // int_T d2G/dn_x dn_y dS_x at y off T (unit normal ny), regularised (Maue):
 //   k^2 (ny.nT) int_T G dS  -  oint_{dT} (ny x grad_y G) . dl,
 // the boundary traversed v0 -> v1 -> v2 (counter-clockwise about nT); grad_y G =
-// G (ik - 1/r) (y - x)/r.  The edge integrals are regular for y off the element.
-__device__ double2 elem_hyper_near(double k, const double *nod, const double *y, const double *ny, int rule)
+// G (ik - 1/r) (y - x)/r.  The edge integrals are regular for y off the element; this is the
+// boundary term (the surface term uses int G from elem_integrals_fused).
+__device__ double2 hyper_edges(double k, const double *nod, const double *y, const double *ny)
 {
-    double nT[3];
-    tri_normal(nod, nT);
-    double2 S = elem_integral(k, nod, y, rule, 0);
-    double dn = ny[0] * nT[0] + ny[1] * nT[1] + ny[2] * nT[2];
     double lr = 0.0, li = 0.0;
     for (int e = 0; e < 3; e++) {
         const double *va = nod + 3 * e, *vb = nod + 3 * ((e + 1) % 3);
@@ -728,8 +710,43 @@ __device__ double2 elem_hyper_near(double k, const double *nod, const double *y,
                 li += f * (gr * ai + gi * ar);
             }
     }
-    double kk = k * k * dn;
-    return make_double2(kk * S.x - lr, kk * S.y - li);
+    return make_double2(lr, li);
+}
+
+// The regular-rule integrals of one source element at an off-element collocation point y
+// (unit normal ny) in one pass over the quadrature points, each with the arithmetic and
+// summation order of its own routine: G -> int G (elem_integral kern 0), dGx -> int dG/dn_x
+// (kern 1), dGy -> int dG/dn_y (elem_dGdny), each only where its flag is set; nT the
+// element's unit normal.
+__device__ void elem_integrals_fused(double k, const double *nod, const double *y, const double *ny, int rule,
+                                     bool wG, bool wx, bool wy, double2 &G, double2 &dGx, double2 &dGy, double *nT)
+{
+    const double J = tri_normal(nod, nT);
+    G = dGx = dGy = make_double2(0.0, 0.0);
+    const int nq = c_rule_n[rule];
+    for (int q = 0; q < nq; q++) {
+        const double *b = &c_rule_bary[rule][3 * q];
+        double x[3];
+        for (int a = 0; a < 3; a++) x[a] = nod[a] * b[0] + nod[3 + a] * b[1] + nod[6 + a] * b[2];
+        double d0 = x[0] - y[0], d1 = x[1] - y[1], d2 = x[2] - y[2];
+        double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        double sn, cs;
+        sincos(k * r, &sn, &cs);
+        double inv = 1.0 / (4.0 * FMM_PI * r);
+        double gr = cs * inv, gi = sn * inv, ar = -1.0 / r, ai = k;
+        double wq = c_rule_w[rule][q] * J;
+        if (wG) { G.x += wq * gr; G.y += wq * gi; }
+        if (wx) {
+            double dn = (d0 * nT[0] + d1 * nT[1] + d2 * nT[2]) / r;
+            double2 g = make_double2((gr * ar - gi * ai) * dn, (gr * ai + gi * ar) * dn);
+            dGx.x += wq * g.x; dGx.y += wq * g.y;
+        }
+        if (wy) {
+            double dn = (d0 * ny[0] + d1 * ny[1] + d2 * ny[2]) / r;
+            double2 g = make_double2((gr * ar - gi * ai) * dn, (gr * ai + gi * ar) * dn);
+            dGy.x -= wq * g.x; dGy.y -= wq * g.y;
+        }
+    }
 }
 
 // ----------------------------------------------------------------------------- element tables
@@ -1005,13 +1022,28 @@ __global__ void near_field_kernel(const double *V, const int *F, int nf, const i
             double2 v = make_double2(0.0, 0.0);
             bool sgl = (i == j);
             bool hb = bco.x != 0.0 || bco.y != 0.0, hc = cco.x != 0.0 || cco.y != 0.0;
-            if (hb) v = cadd(v, cmul(bco, sgl ? elem_integral_sgl(k, nod, 0) : elem_integral(k, nod, y, rule, 0)));
-            if (hc) v = cadd(v, cmul(cco, sgl ? elem_integral_sgl(k, nod, 1) : elem_integral(k, nod, y, rule, 1)));
-            if (bm) {
-                double2 w = make_double2(0.0, 0.0);
-                if (hb && !sgl) w = cadd(w, cmul(bco, elem_dGdny(k, nod, y, ny, rule)));
-                if (hc) w = cadd(w, cmul(cco, sgl ? elem_hyper_self(k, nod) : elem_hyper_near(k, nod, y, ny, rule)));
-                v = cadd(v, cmul(alpha, w));
+            if (sgl) {
+                if (hb) v = cadd(v, cmul(bco, elem_integral_sgl(k, nod, 0)));
+                if (hc) v = cadd(v, cmul(cco, elem_integral_sgl(k, nod, 1)));
+                if (bm && hc) v = cadd(v, cmul(alpha, cmul(cco, elem_hyper_self(k, nod))));
+            } else {
+                // every regular-rule integral of the pair from one evaluation of G per point
+                double2 G, dGx, dGy;
+                double nT[3];
+                elem_integrals_fused(k, nod, y, ny, rule, hb || (bm && hc), hc, bm && hb, G, dGx, dGy, nT);
+                if (hb) v = cadd(v, cmul(bco, G));
+                if (hc) v = cadd(v, cmul(cco, dGx));
+                if (bm) {
+                    double2 w = make_double2(0.0, 0.0);
+                    if (hb) w = cadd(w, cmul(bco, dGy));
+                    if (hc) {
+                        // Maue form: k^2 (ny.nT) int G - boundary term
+                        double dn = ny[0] * nT[0] + ny[1] * nT[1] + ny[2] * nT[2], kk = k * k * dn;
+                        double2 l = hyper_edges(k, nod, y, ny);
+                        w = cadd(w, cmul(cco, make_double2(kk * G.x - l.x, kk * G.y - l.y)));
+                    }
+                    v = cadd(v, cmul(alpha, w));
+                }
             }
             out[s] = v;
         }

@@ -263,7 +263,7 @@ __device__ CDn<N> elem_integral_sgl_d(double k, const Dn<N> *nod, int kern)
 }
 
 // ---------------------------------------------------------------- Burton-Miller terms in duals
-// The same forms as tables.cu (elem_dGdny, elem_hyper_near, elem_hyper_self); the numbers of
+// The same forms as tables.cu (elem_integrals_fused, hyper_edges, elem_hyper_self); the numbers of
 // edge segments follow from the values, as there, and are held fixed by the derivative.
 __device__ __forceinline__ int edge_segments_v(double len, double dist)
 {
