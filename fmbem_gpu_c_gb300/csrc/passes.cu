@@ -430,16 +430,21 @@ static int translate32_direct(Plan *P, int nrhs)
         int e = launch_pass32(P, l, PASS_M2L, nrhs, sl);
         if (e) return e;
         timer_end(P, sl);
+        FMM_CUDA_TRY(cudaEventRecord(P->m2l_ev[l], sl));
     }
-    for (int i = 0; i < P->nside; i++) {
-        FMM_CUDA_TRY(cudaEventRecord(P->join_ev[i], P->side[i]));
-        FMM_CUDA_TRY(cudaStreamWaitEvent(st, P->join_ev[i], 0));
-    }
+    // L2L into level l adds the parents' locals once level l's M2L (and the L2L above it) is
+    // complete, so the top of the downward pass overlaps the M2L of the deeper levels
+    FMM_CUDA_TRY(cudaStreamWaitEvent(st, P->m2l_ev[lmin], 0));
     for (int l = lmin + 1; l <= lmax; l++) {
+        FMM_CUDA_TRY(cudaStreamWaitEvent(st, P->m2l_ev[l], 0));
         timer_begin(P, l2l_names[l]);
         int e = launch_pass32(P, l, PASS_L2L, nrhs, st);
         if (e) return e;
         timer_end(P);
+    }
+    for (int i = 0; i < P->nside; i++) {
+        FMM_CUDA_TRY(cudaEventRecord(P->join_ev[i], P->side[i]));
+        FMM_CUDA_TRY(cudaStreamWaitEvent(st, P->join_ev[i], 0));
     }
     if (P->profiling == 1) cudaEventRecord(P->phase.end, st);
     return FMM_OK;

@@ -112,6 +112,8 @@ static void free_plan(Plan *P)
         if (P->join_ev[i]) cudaEventDestroy(P->join_ev[i]);
     }
     if (P->fork_ev) cudaEventDestroy(P->fork_ev);
+    for (cudaEvent_t &e : P->m2l_ev)
+        if (e) cudaEventDestroy(e);
     delete P;
 }
 
@@ -153,6 +155,7 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
         CTRY(cudaEventCreateWithFlags(&P->join_ev[i], cudaEventDisableTiming));
     }
     CTRY(cudaEventCreateWithFlags(&P->fork_ev, cudaEventDisableTiming));
+    for (cudaEvent_t &e : P->m2l_ev) CTRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     if (const char *ns = getenv("FMMBEM_M2L_STREAMS")) P->nside = std::max(1, std::min(NSIDE, atoi(ns)));
     if (build_tree(P->V, P->F, opt->s, opt->depth, P->tree) != 0 || P->tree.lmax > FMM_MAX_LEVEL) {
         fmm_set_error("octree build failed (lmax=%d)", P->tree.lmax);

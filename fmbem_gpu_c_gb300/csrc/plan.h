@@ -117,7 +117,8 @@ struct Plan {
     cudaStream_t stream = nullptr;
     cudaStream_t side[NSIDE] = {};  // non-blocking side streams, forked from and joined to `stream`
     cudaEvent_t fork_ev = nullptr, join_ev[NSIDE] = {};
-    int nside = 3;                // side streams in use (FMMBEM_M2L_STREAMS, 1..NSIDE)
+    cudaEvent_t m2l_ev[FMM_MAX_LEVEL + 2] = {}; // end of each level's M2L on its side stream
+    int nside = 2;                // side streams in use (FMMBEM_M2L_STREAMS, 1..NSIDE)
     cudaGraphExec_t graph_exec = nullptr; // captured mixed translation passes for graph_nrhs columns
     int graph_nrhs = 0, graph_seen = 0;
     int *tc_err = nullptr;        // set by the tensor-core M2L when one of its waits gives up
