@@ -32,6 +32,7 @@ struct RcrList {
 struct TcM2L {
     int on = 0;                   // this level's mixed M2L runs on the tensor cores
     int KC = 40, nch = 0, nhalf = 1, CH = 0, Nmma = 0;
+    int res = 0;                  // the whole operator of a direction stays in shared memory (p <= 8)
     float *B = nullptr;           // [dir][half][chunk][hi, lo][Nmma x KC core-matrix tile]
     size_t B_bytes = 0;
     int4 *items = nullptr;        // (direction, first column, count, 0), 128 columns each

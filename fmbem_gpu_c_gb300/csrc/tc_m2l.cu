@@ -23,7 +23,10 @@
 //              32 columns at a time in shared memory and add them into the destination local
 //              expansions with coalesced FP32 atomics, overlapping the next tile's MMAs.
 // Four shared-memory stages of KC = 16; every wait has a time limit, after which the thread sets
-// the plan's error flag and stops.
+// the plan's error flag and stops.  Where one output half's whole operator fits beside the A
+// stages (p <= 8), it stays resident instead: each CTA takes a contiguous range of tiles, warp 1
+// copies a direction's operator once per run of its tiles (operator-full barrier), and the MMA
+// warp releases it after the run's last tile (a commit to the operator-empty barrier).
 #include "plan.h"
 #include <algorithm>
 #include <cstdlib>
@@ -47,6 +50,7 @@ struct TcPass {
     const int *g_src, *g_dst;
     int nrhs, nsrc, ndst;
     int p, K, nch, nhalf, CH, Nmma, ntiles;
+    int res;                      // operator resident: one output half, whole operator in shared memory
     const float *B;
     const float2 *src;
     float2 *dst;
@@ -54,9 +58,12 @@ struct TcPass {
 };
 
 static size_t tc_stage_bytes(int Nmma) { return (size_t)8 * TC_KC * (TC_M + Nmma); }
-static size_t tc_smem_bytes(int Nmma)
+// res = 0: stages of (A hi, A lo, B hi, B lo); res = 1: stages of (A hi, A lo) and the whole
+// operator of one direction (nch chunks of B hi, B lo) resident
+static size_t tc_smem_bytes(int Nmma, int res, int nch)
 {
-    return TC_STAGES * tc_stage_bytes(Nmma) + 4 * 32 * TC_EPI_LD * sizeof(float) + (2 * TC_STAGES + 4) * 8 + 16;
+    size_t main = res ? TC_STAGES * (size_t)8 * TC_KC * TC_M + (size_t)nch * 8 * TC_KC * Nmma : TC_STAGES * tc_stage_bytes(Nmma);
+    return main + 4 * 32 * TC_EPI_LD * sizeof(float) + (2 * TC_STAGES + 6) * 8 + 16;
 }
 
 // Output halves and MMA width for order p: each half holds CH coefficients (2 CH real outputs,
@@ -70,9 +77,12 @@ static bool tc_geometry(int p, TcM2L &g)
         g.Nmma = (2 * g.CH + 15) / 16 * 16;
         if (g.Nmma <= 256) break;
     }
-    if (tc_smem_bytes(g.Nmma) > TC_SMEM_MAX) return false;
     g.KC = TC_KC;
     g.nch = (K + TC_KC - 1) / TC_KC;
+    if (tc_smem_bytes(g.Nmma, 0, g.nch) > TC_SMEM_MAX) return false;
+    // one output half whose whole operator fits beside the A stages (p <= 8): the operator
+    // stays in shared memory while a CTA's consecutive tiles keep its direction
+    g.res = g.nhalf == 1 && tc_smem_bytes(g.Nmma, 1, g.nch) <= TC_SMEM_MAX ? 1 : 0;
     return true;
 }
 
@@ -126,13 +136,20 @@ __device__ __forceinline__ int tile_box(const TcPass &ps, int4 it, int r, bool s
 __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const int Nmma = ps.Nmma, K = ps.K, P2 = ps.p * ps.p, nch = ps.nch;
-    const uint32_t tA = (uint32_t)TC_M * TC_KC * 4, tB = (uint32_t)Nmma * TC_KC * 4, stage = 2 * tA + 2 * tB;
-    float *epi = reinterpret_cast<float *>(smem + TC_STAGES * stage);
+    const int Nmma = ps.Nmma, K = ps.K, P2 = ps.p * ps.p, nch = ps.nch, res = ps.res;
+    const uint32_t tA = (uint32_t)TC_M * TC_KC * 4, tB = (uint32_t)Nmma * TC_KC * 4, stage = 2 * tA + (res ? 0 : 2 * tB);
+    unsigned char *bres = smem + TC_STAGES * stage;  // resident operator (res)
+    float *epi = reinterpret_cast<float *>(bres + (res ? (size_t)nch * 2 * tB : 0));
     uint64_t *bars = reinterpret_cast<uint64_t *>(epi + 4 * 32 * TC_EPI_LD);
     uint64_t *full = bars, *empty = bars + TC_STAGES, *accf = bars + 2 * TC_STAGES, *acce = accf + 2;
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(acce + 2);
+    uint64_t *bfull = acce + 2, *bempty = bfull + 1;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bempty + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // tiles of this CTA: strided over the grid, or (res) one contiguous range, so that
+    // consecutive tiles share their direction and its resident operator
+    const int q_first = res ? (int)((long long)blockIdx.x * ps.ntiles / gridDim.x) : (int)blockIdx.x;
+    const int q_end = res ? (int)((long long)(blockIdx.x + 1) * ps.ntiles / gridDim.x) : ps.ntiles;
+    const int q_step = res ? 1 : (int)gridDim.x;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(512));
@@ -140,13 +157,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
     }
     if (tid == 32) {
         for (int s = 0; s < TC_STAGES; s++) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)), "r"(TC_AWARPS + 1));  // A warps + B copy
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)), "r"(TC_AWARPS + (res ? 0 : 1)));  // A warps (+ B copy)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)));  // MMA commit
         }
         for (int a = 0; a < 2; a++) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(accf + a)));   // MMA commit
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(smem_u32(acce + a)));   // 4 epilogue warps
         }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bfull)));   // operator copy (res)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bempty)));  // MMA commit (res)
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
@@ -160,10 +179,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
             const uint32_t idesc =
                 (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Nmma >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
             const uint32_t lbo = 128, sbo = 32 * TC_KC;
-            int g = 0, i = 0;
-            for (int q = blockIdx.x; q < ps.ntiles && ok; q += gridDim.x, i++) {
+            int g = 0, i = 0, loads = 0, cur = -1;
+            for (int q = q_first; q < q_end && ok; q += q_step, i++) {
                 const int a = i & 1;
                 ok = mbar_wait(smem_u32(acce + a), ((i >> 1) & 1) ^ 1);
+                if (ok && res && ps.items[q].x != cur) {
+                    // this tile's operator: the copy of the next direction run
+                    ok = mbar_wait(smem_u32(bfull), loads & 1);
+                    loads++;
+                    cur = ps.items[q].x;
+                }
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint32_t d_tmem = tmem + (uint32_t)(a * 256);
                 for (int c = 0; c < nch && ok; c++, g++) {
@@ -171,7 +196,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                     ok = mbar_wait(smem_u32(full + s), (g / TC_STAGES) & 1);
                     if (!ok) break;
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    const uint32_t a_hi = smem_u32(smem + s * stage), a_lo = a_hi + tA, b_hi = a_hi + 2 * tA, b_lo = b_hi + tB;
+                    const uint32_t a_hi = smem_u32(smem + s * stage), a_lo = a_hi + tA;
+                    const uint32_t b_hi = res ? smem_u32(bres) + (uint32_t)c * 2 * tB : a_hi + 2 * tA, b_lo = b_hi + tB;
 #pragma unroll
                     for (int ks = 0; ks < TC_KC / 8; ks++)
 #pragma unroll
@@ -191,14 +217,38 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                                      smem_u32(accf + a))
                                  : "memory");
+                // the last tile of a direction run releases the resident operator once its MMAs are done
+                if (ok && res && (q + 1 >= q_end || ps.items[q + 1].x != cur))
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_u32(bempty))
+                                 : "memory");
             }
         }
     } else if (warp == 1) {
         // ---------------------------------------------------------------- operator copies
-        if (lane == 0) {
+        if (lane == 0 && res) {
+            // one copy of a direction's whole operator per direction run
+            const uint32_t bytes = (uint32_t)nch * 2 * tB;
+            int loads = 0, cur = -1;
+            for (int q = q_first; q < q_end && ok; q += q_step) {
+                const int4 it = ps.items[q];
+                if (it.x == cur) continue;
+                if (loads > 0) {
+                    ok = mbar_wait(smem_u32(bempty), (loads - 1) & 1);
+                    if (!ok) break;
+                }
+                const uint32_t bar = smem_u32(bfull), dst = smem_u32(bres);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+                asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                             "l"(ps.B + (size_t)it.x * nch * 2 * Nmma * TC_KC), "r"(bytes), "r"(bar)
+                             : "memory");
+                loads++;
+                cur = it.x;
+            }
+        } else if (lane == 0) {
             const uint32_t bytes = 2 * tB;
             int g = 0;
-            for (int q = blockIdx.x; q < ps.ntiles && ok; q += gridDim.x) {
+            for (int q = q_first; q < q_end && ok; q += q_step) {
                 const int item = q / ps.nhalf, h = q - item * ps.nhalf;
                 const int4 it = ps.items[item];
                 const float *Bd = ps.B + (size_t)(it.x * ps.nhalf + h) * nch * 2 * Nmma * TC_KC;
@@ -223,7 +273,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
         const float *srcf = reinterpret_cast<const float *>(ps.src);
         const bool vec4 = (K & 3) == 0;
         int g = 0;
-        for (int q = blockIdx.x; q < ps.ntiles && ok; q += gridDim.x) {
+        for (int q = q_first; q < q_end && ok; q += q_step) {
             const int item = q / ps.nhalf;
             const int sb = tile_box(ps, ps.items[item], r, true);
             const float *row = srcf + (size_t)(sb < 0 ? 0 : sb) * K;
@@ -283,7 +333,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
         const int wq = warp & 3;  // TMEM lane quarter of this warp
         float *st = epi + (warp - TC_EPI0) * 32 * TC_EPI_LD;
         int i = 0;
-        for (int q = blockIdx.x; q < ps.ntiles && ok; q += gridDim.x, i++) {
+        for (int q = q_first; q < q_end && ok; q += q_step, i++) {
             const int a = i & 1, item = q / ps.nhalf, h = q - item * ps.nhalf;
             const int dbox = tile_box(ps, ps.items[item], wq * 32 + lane, false);
             const int co0 = h * ps.CH, nco = min(ps.CH, P2 - co0);
@@ -430,11 +480,12 @@ int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st)
     ps.CH = g.CH;
     ps.Nmma = g.Nmma;
     ps.ntiles = g.n_items * g.nhalf;
+    ps.res = g.res;
     ps.B = g.B;
     ps.src = L.Cm32;
     ps.dst = L.Dl32;
     ps.err = P->tc_err;
-    size_t sm = tc_smem_bytes(g.Nmma);
+    size_t sm = tc_smem_bytes(g.Nmma, g.res, g.nch);
     static size_t attr = 0;
     e = raise_smem_limit((const void *)m2l_tc_kernel, sm, &attr);
     if (e) return e;
