@@ -97,3 +97,22 @@ def test_tensor_m2l_in_the_transposed_operator(fm, oracle):
     orc = oracle.FMM(V, F, K1, T, [10, 10], a=0.3, b=0.7 + 0.2j, c=-1.0, rule=0)
     assert rel(at64, orc.apply(y, transpose=True)) < 1e-10
     plan.close()
+
+
+def test_many_columns_with_morton_ranges_and_resident_operator(fm):
+    """16 columns on the 81,920-triangle sphere with p = 8 at the leaves: the expansions of the
+    deep levels exceed the L2 budget, so the items run in Morton ranges of the destinations, and
+    the p = 8 tensor-core level keeps its operator resident.  Every column against its own
+    single-column matvec and two against FP64."""
+    V, F = fm.icosphere(6, 0.3)
+    P2 = {2: 30, 3: 20, 4: 14, 5: 10, 6: 8}
+    plan = make_plan(fm, "1", V, F, k=K2, depth=6, p_levels=P2, rule=0, a=0.5, b=0.0, c=-1.0)
+    assert plan.info.m2l_tensor[6] == 1
+    rng = np.random.default_rng(16)
+    X = rng.standard_normal((16, plan.nf)) + 1j * rng.standard_normal((16, plan.nf))
+    Y = plan.matvec(X.reshape(-1), fm.FMM_MIXED).reshape(16, -1)
+    for r in range(16):
+        assert rel(Y[r], plan.matvec(X[r], fm.FMM_MIXED)) < 1e-6, r
+    for r in (0, 15):
+        assert rel(Y[r], plan.matvec(X[r], fm.FMM_FP64)) < 1e-5, r
+    plan.close()
