@@ -620,6 +620,7 @@ static int ensure_rhs32(Plan *P, int nrhs)
         FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Dl32, sizeof(float2) * n * nrhs));
     }
     P->rhs_cap32 = nrhs;
+    P->buf_gen++;
     return FMM_OK;
 }
 

@@ -62,6 +62,7 @@ constexpr int SCENE_SIDE = 4;
 
 struct Scene {
     std::vector<Plan *> plans;
+    std::vector<int> buf_gen;         // each plan's expansion-buffer generation the scene was built on
     std::vector<long long> off;
     long long N = 0;
     int device = 0;
@@ -583,6 +584,13 @@ static int scene_matvec_dev(Scene *S, const double2 *x, double2 *y, int precisio
     cudaStream_t st = S->stream;
     const int n = (int)S->plans.size();
     if (precision == FMM_MIXED) {
+        // the scene's descriptors hold the plans' FP32 expansion addresses
+        for (int i = 0; i < n; i++)
+            if (S->plans[i]->buf_gen != S->buf_gen[i]) {
+                fmm_set_error("scene: plan %d's expansion buffers were reallocated (a mixed matvec with more right-hand "
+                              "sides) after fmm_scene_create; create the scene again", i);
+                return FMM_ERR_ARG;
+            }
         if (x != S->xin) FMM_CUDA_TRY(cudaMemcpyAsync(S->xin, x, sizeof(double2) * S->N, cudaMemcpyDeviceToDevice, st));
         int e = scene_mixed(S);
         if (e) return e;
@@ -775,6 +783,7 @@ extern "C" int fmm_scene_create(fmm_plan *const *plans, int n, fmm_scene **scene
     Scene *S = new Scene();
     S->plans.assign((Plan *const *)plans, (Plan *const *)plans + n);
     S->device = S->plans[0]->opt.device;
+    for (Plan *P : S->plans) S->buf_gen.push_back(P->buf_gen);
     int st = FMM_OK;
     if (cudaSetDevice(S->device) != cudaSuccess || cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess) {
         fmm_set_error("fmm_scene_create: %s", cudaGetErrorString(cudaGetLastError()));

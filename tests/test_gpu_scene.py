@@ -99,6 +99,26 @@ def test_scene_solve_matches_the_plans(fm, bodies):
     sc.close()
 
 
+def test_scene_refuses_plans_whose_buffers_moved(fm):
+    V, F = fm.icosphere(2, 0.1)
+    k = 2 * np.pi * 2000 / 343.0
+    plans = [fm.Plan(V, F, k=k * (1 + i), depth=2, p_levels={2: 8}, rule=1, a=0.5, b=0.0, c=-1.0) for i in range(2)]
+    sc = fm.Scene(plans)
+    x = np.ones(sc.n, dtype=np.complex128)
+    sc.matvec(x)
+    # a 4-column matvec of plan 1 reallocates its FP32 expansions
+    plans[1].matvec(np.ones(4 * plans[1].nf, dtype=np.complex128), fm.FMM_MIXED)
+    with pytest.raises(fm.FmmError, match="create the scene again"):
+        sc.matvec(x)
+    sc.close()
+    sc = fm.Scene(plans)
+    y = sc.split(sc.matvec(x))
+    assert all(rel(yi, p.matvec(np.ones(p.nf, dtype=np.complex128), fm.FMM_FP64)) < 1e-5 for p, yi in zip(plans, y))
+    sc.close()
+    for p in plans:
+        p.close()
+
+
 def test_scene_rejects_unsuitable_plans(fm, bodies):
     V, F = fm.icosphere(2, 0.1)
     fp64_only = fm.Plan(V, F, k=10.0, depth=2, p_levels={2: 8}, rule=1, a=0.5, b=0.0, c=-1.0, build_mixed=False)
