@@ -372,7 +372,7 @@ class Plan:
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:
-            lib().fmm_plan_destroy(self.h)
+            _check(lib().fmm_plan_destroy(self.h))  # refused while a scene uses the plan
             self.h = c_vp()
 
     def __del__(self):

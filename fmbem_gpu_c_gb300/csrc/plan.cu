@@ -286,7 +286,12 @@ extern "C" int fmm_plan_create_obj(const char *path, const fmm_options *opt, fmm
 
 extern "C" int fmm_plan_destroy(fmm_plan *plan)
 {
-    free_plan((Plan *)plan);
+    Plan *P = (Plan *)plan;
+    if (P && P->scene_refs > 0) {
+        fmm_set_error("fmm_plan_destroy: %d scene(s) still use this plan; destroy them first", P->scene_refs);
+        return FMM_ERR_ARG;
+    }
+    free_plan(P);
     return FMM_OK;
 }
 

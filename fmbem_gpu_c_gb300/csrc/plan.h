@@ -116,6 +116,7 @@ struct Plan {
     int nrhs_cap = 0;             // columns of xbuf / ybuf
     int rhs_cap32 = 1;            // right-hand sides the FP32 expansions (Cm32, Dl32) hold
     int buf_gen = 0;              // times Cm32 / Dl32 were reallocated (scenes hold their addresses)
+    int scene_refs = 0;           // scenes built on this plan (it is not destroyed before them)
     cudaStream_t stream = nullptr;
     cudaStream_t side[NSIDE] = {};  // non-blocking side streams, forked from and joined to `stream`
     cudaEvent_t fork_ev = nullptr, join_ev[NSIDE] = {};

@@ -800,6 +800,7 @@ extern "C" int fmm_scene_create(fmm_plan *const *plans, int n, fmm_scene **scene
         st = FMM_ERR_CUDA;
     }
     if (st) { free_scene(S); return st; }
+    for (Plan *P : S->plans) P->scene_refs++;
     *scene = (fmm_scene *)S;
     return FMM_OK;
 }
@@ -807,7 +808,10 @@ extern "C" int fmm_scene_create(fmm_plan *const *plans, int n, fmm_scene **scene
 extern "C" int fmm_scene_destroy(fmm_scene *scene)
 {
     Scene *S = (Scene *)scene;
-    if (S) cudaSetDevice(S->device);
+    if (S) {
+        cudaSetDevice(S->device);
+        for (Plan *P : S->plans) P->scene_refs--;
+    }
     free_scene(S);
     return FMM_OK;
 }

@@ -156,7 +156,7 @@ int fmm_solve_many(fmm_plan *const *plans, int n, const cuDoubleComplex *const *
  * as a CUDA graph; FMM_FP64 runs each plan's FP64 matvec concurrently on the plans' streams.
  * Every plan needs its mixed-precision tables and must be on one device; the scene uses
  * the plans' buffers, so a plan is not used elsewhere while a scene call runs, and is
- * destroyed only after its scenes.  A mixed matvec of a plan with more right-hand sides than
+ * destroyed only after its scenes (fmm_plan_destroy refuses while a scene uses the plan).  A mixed matvec of a plan with more right-hand sides than
  * before reallocates those buffers; the scene's mixed calls then fail (FMM_ERR_ARG) until it
  * is created again.  No counterpart in the reference. */
 typedef struct fmm_scene fmm_scene;

@@ -110,6 +110,9 @@ def test_scene_refuses_plans_whose_buffers_moved(fm):
     plans[1].matvec(np.ones(4 * plans[1].nf, dtype=np.complex128), fm.FMM_MIXED)
     with pytest.raises(fm.FmmError, match="create the scene again"):
         sc.matvec(x)
+    # a plan is not destroyed while a scene uses it
+    with pytest.raises(fm.FmmError, match="destroy them first"):
+        plans[0].close()
     sc.close()
     sc = fm.Scene(plans)
     y = sc.split(sc.matvec(x))
