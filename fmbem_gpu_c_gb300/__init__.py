@@ -81,6 +81,7 @@ def lib():
         L.fmm_scene_solve.argtypes = [c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       c_ip, c_dp]
         L.fmm_scene_timings.argtypes = [c_vp, c_dp, c_dp, c_ip, c_dp, c_ip]
+        L.fmm_selftest_bounded_wait.argtypes = [ctypes.c_int, c_ip, c_ip]
         L.fmm_scene_set_active.argtypes = [c_vp, c_ip]
         L.fmm_vjp.argtypes = [c_vp, c_vp, c_dp, c_dp, ctypes.c_int, c_vp, ctypes.c_double, ctypes.c_int, c_dp, c_vp]
         L.fmm_far_field.argtypes = [c_vp, c_vp, c_dp, ctypes.c_int, c_vp]
@@ -148,6 +149,14 @@ def _ptr(a):
     if hasattr(a, "data_ptr"):
         return ctypes.c_void_p(a.data_ptr())
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def selftest_bounded_wait(device=0):
+    """Run the tensor-core M2L's bounded barrier wait on a barrier nothing completes
+    (``fmm_selftest_bounded_wait``).  Returns (gave_up, completed_after_arrival)."""
+    g, c = ctypes.c_int(), ctypes.c_int()
+    _check(lib().fmm_selftest_bounded_wait(device, ctypes.byref(g), ctypes.byref(c)))
+    return bool(g.value), bool(c.value)
 
 
 def solve_many(plans, rhs, tol=1e-6, maxit=500, restart=50, precision=FMM_FP64, nthreads=8, x0=None):

@@ -106,8 +106,9 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
            ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
 }
 
-// wait for the phase of the given parity of an mbarrier, at most ~1 s of SM clock
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+// wait for the phase of the given parity of an mbarrier, at most `limit` SM clock cycles;
+// false when the wait gave up
+__device__ __forceinline__ bool mbar_wait_limit(uint32_t bar, uint32_t parity, long long limit)
 {
     long long t0 = clock64();
     while (true) {
@@ -115,9 +116,12 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
         asm volatile("{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\tselp.u32 %0, 1, 0, q;\n\t}"
                      : "=r"(done) : "r"(bar), "r"(parity) : "memory");
         if (done) return true;
-        if (clock64() - t0 > 2000000000LL) return false;
+        if (clock64() - t0 > limit) return false;
     }
 }
+
+// the kernel's waits: at most ~1 s of SM clock
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) { return mbar_wait_limit(bar, parity, 2000000000LL); }
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar)
 {
@@ -501,6 +505,41 @@ int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st)
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
+
+// The bounded wait on its own: an mbarrier that expects one arrival nobody makes is waited on
+// with a limit of `cycles` (out[0] = 1 if that wait gave up), then completed and waited on again
+// (out[1] = 1 if that wait saw the phase complete).
+__global__ void wait_probe_kernel(long long cycles, int *out)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    const uint32_t b = smem_u32(&bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b));
+    out[0] = mbar_wait_limit(b, 0, cycles) ? 0 : 1;
+    mbar_arrive(b);
+    out[1] = mbar_wait_limit(b, 0, cycles) ? 1 : 0;
+}
+
+} // namespace fmm
+
+extern "C" int fmm_selftest_bounded_wait(int device, int *gave_up, int *completed)
+{
+    using namespace fmm;
+    if (!gave_up || !completed) { fmm_set_error("fmm_selftest_bounded_wait: null argument"); return FMM_ERR_ARG; }
+    FMM_CUDA_TRY(cudaSetDevice(device));
+    int *d = nullptr, h[2] = {0, 0};
+    FMM_CUDA_TRY(cudaMalloc(&d, sizeof(h)));
+    wait_probe_kernel<<<1, 32>>>(2000000LL, d);  // ~1 ms at 2 GHz
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) { fmm_set_error("fmm_selftest_bounded_wait: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
+    *gave_up = h[0];
+    *completed = h[1];
+    return FMM_OK;
+}
+
+namespace fmm {
 
 int check_tc_error(Plan *P)
 {

@@ -181,6 +181,13 @@ int fmm_scene_solve(fmm_scene *scene, const cuDoubleComplex *b, cuDoubleComplex 
 int fmm_scene_timings(const fmm_scene *scene, double *solve_s, double *mixed_ms, int *mixed_calls, double *fp64_ms,
                       int *fp64_calls);
 
+/* Failure detection of the tensor-core M2L: its waits on shared-memory barriers give up after a
+ * time limit, set the plan's error flag and return, and the next mixed call reports the error.
+ * This runs one such wait on `device` on a barrier nothing completes, with a ~1 ms limit
+ * (*gave_up = 1 when it gave up), then completes the barrier and waits again (*completed = 1).
+ * No counterpart in the reference. */
+int fmm_selftest_bounded_wait(int device, int *gave_up, int *completed);
+
 /* Reverse-mode derivative of a far-field objective with respect to the vertex positions.
  * x solves A x = b, b the plane wave exp(i k dir.c) at the centroids (dir NULL: b does not
  * depend on the mesh); p = F x is the scattered field at the npts points pts (fmm_far_field).

@@ -116,3 +116,15 @@ def test_many_columns_with_morton_ranges_and_resident_operator(fm):
     for r in (0, 15):
         assert rel(Y[r], plan.matvec(X[r], fm.FMM_FP64)) < 1e-5, r
     plan.close()
+
+
+def test_bounded_wait_gives_up_and_leaves_the_context_usable(fm):
+    """Failure detection without a fault: the barrier wait the tensor-core M2L uses gives up
+    after its limit on a barrier nothing completes, reports it, and the GPU goes on working."""
+    gave_up, completed = fm.selftest_bounded_wait(0)
+    assert gave_up and completed
+    V, F = fm.icosphere(3, 0.1)
+    plan = make_plan(fm, "1", V, F, k=K1, depth=3, p_levels={2: 8, 3: 8}, rule=1, a=0.5, b=0.0, c=-1.0)
+    x = np.random.default_rng(3).standard_normal(plan.nf) + 0j
+    assert rel(plan.matvec(x, fm.FMM_MIXED), plan.matvec(x, fm.FMM_FP64)) < 1e-5
+    plan.close()
