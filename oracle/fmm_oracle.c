@@ -1,6 +1,6 @@
 /* FP64 CPU restatement of the reference FMM-BEM algorithm (the oracle).
  *
- * TEST INFRASTRUCTURE ONLY -- the checker for the GPU product, never linked by it.
+ * TEST INFRASTRUCTURE ONLY -- the reference the GPU product is tested against, never linked by it.
  *
  * What each part restates (paths within the reference project):
  *   aCoeff/bCoeff              translation.cu:189-212

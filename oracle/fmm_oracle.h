@@ -1,7 +1,7 @@
 /* FP64 CPU restatement of the reference FMM-BEM algorithm (the oracle).
  *
  * TEST INFRASTRUCTURE ONLY.  Built into oracle/_build/liboracle.so and loaded by tests/,
- * __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker.  The product
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg, to test against.  The product
  * library never links or calls it.
  *
  * Complex numbers are interleaved (re, im) doubles.  Coefficient vectors of order p hold

@@ -1,6 +1,6 @@
 """Octree oracle: a NumPy restatement of the reference's octree and interaction lists.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker for the GPU octree build; it is
+TEST INFRASTRUCTURE ONLY.  The GPU octree build is tested against this module; it is
 imported by ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg,
 never by the product library.
 

@@ -291,7 +291,7 @@ def test_rcr_translation_addition_theorem(oracle, p, off, k, box):
 
 def _coax_rr_mp(x, p, dps=60):
     """The coaxial (R|R) recurrence (translation.cu:678-771) in 60-digit arithmetic, entry
-    (m, n', n) -> value; exact enough to judge the FP64 tables in both triangles."""
+    (m, n', n) -> value; exact enough to check the FP64 tables in both triangles."""
     mp = pytest.importorskip("mpmath")
     mp.mp.dps = dps
 
