@@ -2,6 +2,7 @@
 // P2M/L2P, the near-field matrix by quadrature, far-field evaluation.  All in FP64; the
 // mixed-precision path receives FP32 copies.
 #include "plan.h"
+#include "coax_recurrence.cuh"
 #include <cstdio>
 #include <math.h>
 #include <vector>
@@ -297,76 +298,15 @@ int gen_rotation_matrices_f32(const double *alpha, const double *beta, const dou
 }
 
 // ----------------------------------------------------------------------------- coaxial
-// (S|R) or (R|R) coaxial blocks for translation length t along z, following
-// sparseCoaxTransMatGen (translation.cu:678-771) with the initial column of
-// srCoaxTransMatsInit / rrCoaxTransMatsInit (translation.cu:555-584, 919-949) in FP64.
-// One CTA per matrix; E[m][n'][n] lives in a global scratch slice.  The diagonal
-// recurrence over m is sequential across the block; the n recurrence for each m is
-// independent and runs one warp per m.
+// (S|R) or (R|R) coaxial blocks for translation length t along z (coax_recurrence.cuh:
+// sparseCoaxTransMatGen, translation.cu:678-771, in FP64).  One CTA per matrix; the
+// enlarged matrix E[m][n'][n] lives in a global scratch slice.
 __global__ void coax_kernel(double k, const double *tvals, int p, int sr, double2 *scratch, double2 *out)
 {
     int mat = blockIdx.x;
-    double t = tvals[mat];
-    int R = 2 * p - 1;
-    double2 *E = scratch + (size_t)mat * p * R * p;
-    double2 *C = out + (size_t)mat * coax_size(p);
-#define EE(m, np, n) E[((size_t)(m) * R + (np)) * p + (n)]
     extern __shared__ double sh[];
-    double *jn = sh, *yn = sh + R;
-    if (threadIdx.x == 0) {
-        sph_jn_array(R, k * t, jn);
-        if (sr) sph_yn_array(R, k * t, yn);
-    }
-    __syncthreads();
-    for (int np = threadIdx.x; np < R; np += blockDim.x) {
-        double sg = (np & 1) ? -1.0 : 1.0, f = sg * sqrt(2.0 * np + 1.0);
-        EE(0, np, 0) = make_double2(f * jn[np], sr ? f * yn[np] : 0.0);
-    }
-    __syncthreads();
-    for (int m = 0; m + 1 <= p - 1; m++) {
-        double den = coefB(m + 1, -m - 1);
-        for (int np = m + 1 + threadIdx.x; np <= 2 * p - 2 - (m + 1); np += blockDim.x) {
-            double t0 = coefB(np, -m - 1) / den, t1 = coefB(np + 1, m) / den;
-            double2 a = EE(m, np - 1, m), b = EE(m, np + 1, m);
-            EE(m + 1, np, m + 1) = make_double2(t0 * a.x - t1 * b.x, t0 * a.y - t1 * b.y);
-        }
-        __syncthreads();
-    }
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int m = warp; m <= p - 2; m += nw) {
-        for (int n = m; n + 1 <= p - 1; n++) {
-            double den = coefA(n, m);
-            for (int np = m + lane; np <= 2 * p - 2 - (n + 1); np += 32) {
-                double t0 = coefA(np - 1, m) / den, t1 = coefA(np, m) / den, t2 = coefA(n - 1, m) / den;
-                double2 e0 = (np - 1 >= m) ? EE(m, np - 1, n) : make_double2(0.0, 0.0);
-                double2 e1 = EE(m, np + 1, n);
-                double2 e2 = (n - 1 >= m) ? EE(m, np, n - 1) : make_double2(0.0, 0.0);
-                EE(m, np, n + 1) = make_double2(t0 * e0.x - t1 * e1.x + t2 * e2.x, t0 * e0.y - t1 * e1.y + t2 * e2.y);
-            }
-            __threadfence_block();
-            __syncwarp();
-        }
-    }
-    __syncthreads();
-    // (R|R): the recurrence forms the entries with n' < n, which are tiny at small k t, by
-    // cancellation and loses them (absolute error ~1e-16 against values down to (kt)^(n-n'));
-    // an L2L multiplies them by the large high-degree local coefficients.  They are taken from
-    // the exact coaxial symmetry (R|R)_{n'n} = (-1)^{n+n'} (R|R)_{nn'}, whose n' > n side the
-    // recurrence forms to full relative accuracy.  (S|R) is accurate in both triangles.
-    for (int m = 0; m < p; m++) {
-        int sz = p - m, off = coax_off(p, m);
-        for (int i = threadIdx.x; i < sz * sz; i += blockDim.x) {
-            int a = i % sz, b = i / sz; // a = n'-m, b = n-m
-            if (!sr && a < b) {
-                double2 v = EE(m, m + b, m + a);
-                double sg = ((a + b) & 1) ? -1.0 : 1.0;
-                C[off + i] = make_double2(sg * v.x, sg * v.y);
-            } else {
-                C[off + i] = EE(m, m + a, m + b);
-            }
-        }
-    }
-#undef EE
+    coax_matrix_cta(k * tvals[mat], p, sr, scratch + (size_t)mat * p * (2 * p - 1) * p, out + (size_t)mat * coax_size(p),
+                    sh, sh + 2 * p - 1);
 }
 
 // The mixed-precision path stores the coaxial blocks in FP32.  At high order and small k t

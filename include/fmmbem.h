@@ -243,9 +243,12 @@ int fmm_mesh_box(int n, double lx, double ly, double lz, double *V, int *nv, int
  * (0, 1e5] comes out as NaN.
  * The first call on each device looks up the scratch address (cudaGetSymbolAddress), which
  * loads the library's device code on that device if it is not loaded yet.  Make that first
- * call before any stream capture.  Calls share one scratch per device: two calls whose
- * kernels overlap (different streams or host threads without ordering) race and corrupt
- * each other's results, so order them on one stream or with events. */
+ * call before any stream capture.  The address is kept for the life of the process, so
+ * cudaDeviceReset of a device after its first call is not supported (the module can reload
+ * elsewhere).  Calls share one scratch per device: two calls whose kernels overlap
+ * (different streams or host threads without ordering) race and corrupt each other's
+ * results, so order them on one stream or with events.  A CUDA error already pending from
+ * the caller's earlier work is reported (FMM_ERR_CUDA) and nothing is launched. */
 int fmm_coax_matrices_noalloc(double k, const double *t, int n, int p, int sr, cuDoubleComplex *out,
                               cudaStream_t stream);
 

@@ -1,7 +1,9 @@
 """fmm_coax_matrices_noalloc, the coaxial-matrix generator for callers that must not let the
-library allocate device memory.  Two calls in a row through its shared fixed scratch must
-give the matrices of the regular (allocating) generator genSR/genRRSparseCoaxTransMat, and
-sizes beyond the scratch must be rejected.  The file name makes pytest collect it last."""
+library allocate device memory (an application that owns all device memory through its own
+pool, or a loop that cannot take the device synchronisation of cudaMalloc/cudaFree).  Two
+calls in a row through its shared fixed scratch must give the FP64 oracle's matrices and
+those of the regular (allocating) generator genSR/genRRSparseCoaxTransMat, and sizes beyond
+the scratch must be rejected.  The file name makes pytest collect it last."""
 import ctypes
 
 import numpy as np
@@ -36,23 +38,44 @@ def _regular(L, k, t, p, sr):
 
 def _noalloc(L, torch, k, t, p, sr):
     n = len(t)
-    td = torch.tensor(np.asarray(t, np.float32).astype(np.float64), device="cuda")
+    td = torch.tensor(np.asarray(t, np.float64), device="cuda")
     out = torch.full((n * _coax_size(p),), complex("nan"), dtype=torch.complex128, device="cuda")
-    st = L.fmm_coax_matrices_noalloc(float(np.float32(k)), td.data_ptr(), n, p, 1 if sr else 0, out.data_ptr(), None)
+    st = L.fmm_coax_matrices_noalloc(float(k), td.data_ptr(), n, p, 1 if sr else 0, out.data_ptr(), None)
     assert st == 0, L.fmm_last_error()
     torch.cuda.synchronize()
     return out.cpu().numpy()
 
 
-def test_noalloc_matches_regular_generator_twice(fm):
+# (S|R) at p = 30 on the 81,920-triangle workload's k, then (R|R) at p = 12 with small k t,
+# where the library takes the entries below the diagonal from the coaxial symmetry
+CASES = [(146.55, [0.3, 0.3354, 0.45, 0.7794], 30, True),
+         (18.32, [0.0433, 0.05, 0.0612], 12, False)]
+
+
+def test_noalloc_matches_fp64_oracle_twice(fm, oracle):
+    """Two calls in a row through the shared scratch, each matrix against the FP64 oracle's
+    coaxial recurrence (same relations, same symmetry rule) at 1e-12."""
     import torch
 
     L = _bind(fm)
-    cases = [(146.55, [0.3, 0.3354, 0.45, 0.7794], 30, True),   # first call: (S|R), p = 30
-             (18.32, [0.0433, 0.05, 0.0612], 12, False)]       # second call reuses the scratch: (R|R), p = 12
-    for k, t, p, sr in cases:
-        ref = _regular(L, np.float32(k), t, p, sr)
-        got = _noalloc(L, torch, k, t, p, sr)
+    for k, t, p, sr in CASES:
+        got = _noalloc(L, torch, k, t, p, sr).reshape(len(t), -1)
+        assert np.isfinite(got).all()
+        for i, ti in enumerate(t):
+            ref = oracle.coax(k, ti, p, sr)
+            assert np.linalg.norm(got[i] - ref) <= 1e-12 * np.linalg.norm(ref), (k, ti, p, sr)
+
+
+def test_noalloc_matches_regular_generator_twice(fm):
+    """The same two calls against the allocating generator of the reference's FP32 interface
+    (genSR/genRRSparseCoaxTransMat), at its float inputs."""
+    import torch
+
+    L = _bind(fm)
+    for k, t, p, sr in CASES:
+        tf = [float(np.float32(v)) for v in t]
+        ref = _regular(L, np.float32(k), tf, p, sr)
+        got = _noalloc(L, torch, float(np.float32(k)), tf, p, sr)
         assert np.isfinite(got).all()
         # the same relative tolerance as the coaxial-matrix checks of the regular generator
         assert np.linalg.norm(got.astype(np.complex64) - ref) <= 1e-6 * np.linalg.norm(ref)
