@@ -172,56 +172,94 @@ def make_mesh(fm):
     return fm.icosphere(SUBDIV, RADIUS)
 
 
+def cpu_mesh():
+    """The same icosphere as fm.icosphere (vertices rounded to 9 significant digits), built in
+    NumPy so that the CPU arm loads no library of this package."""
+    import meshes
+    return meshes.roundtrip(*meshes.icosphere(SUBDIV, RADIUS))
+
+
+# Leaf-level boxes on which the octree port runs FMMLevelSetNumSR (every k-th box; the
+# coarser levels run in full); its time is scaled to all boxes of the level.
+OCTREE_SR_SAMPLE = 4096
+
+
+def cpu_baseline_sample(steps=None, warmup=0):
+    """The CPU baseline on the machine's host cores: the reference's CPU path as far as it exists
+    (its octree build) plus a CPU matvec.  The reference's own sources are not on this machine,
+    so both are ports (test infrastructure under oracle/):
+
+    * matvec: the FP64 CPU restatement of the FMM (oracle/fmm_oracle.c) on all host cores
+      (bounded to ~10 s, or `steps` matvecs after `warmup`), and one matvec on one core;
+    * octree: oracle/octree_port.c, srcBoxes (fixed depth) + FMMLevelSet + FMMLevelSetNumSR
+      with the reference's own quadratic set algebra, on one core (the reference is serial),
+      FMMLevelSetNumSR of the leaf level on a strided sample of boxes, scaled.
+
+    Returns the cpu_baseline dict (value = all-cores matvec/s) and the all-cores time per
+    matvec."""
+    from oracle import oracle_py as O
+    V, F = cpu_mesh()
+    k = 2 * np.pi * FREQ / 343.0
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    T = O.tree_for_fmm(V, F, depth=DEPTH)
+    f = O.FMM(V, F, k, T, [P_LEVELS[l] for l in range(2, 7)], a=0.5, b=0.0, c=-1.0, rule=0, nthreads=cores)
+    fmm_setup = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(len(F)) + 1j * rng.standard_normal(len(F))
+    for _ in range(max(warmup, 1)):
+        f.apply(x)
+    n, t0 = 0, time.perf_counter()
+    if steps:
+        for _ in range(steps):
+            f.apply(x)
+        n = steps
+    else:
+        while time.perf_counter() - t0 < 10.0 and n < 50:
+            f.apply(x)
+            n += 1
+    dt = time.perf_counter() - t0
+    del f
+    f1 = O.FMM(V, F, k, T, [P_LEVELS[l] for l in range(2, 7)], a=0.5, b=0.0, c=-1.0, rule=0, nthreads=1)
+    t1 = time.perf_counter()
+    f1.apply(x)
+    dt1 = time.perf_counter() - t1
+    del f1
+    oc = O.port_octree(V, F, depth=DEPTH, sr_sample=OCTREE_SR_SAMPLE)
+    ot = oc["times"]
+    octree_s = ot["src_boxes_s"] + ot["level_sets_s"] + ot["sr_lists_s"]
+    leaf_ran = int((oc["srnum_%d" % DEPTH] >= 0).sum())
+    base = {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "full workload, %d FP64 matvecs of the CPU restatement (oracle) on %d threads in %.1f s"
+                      % (n, cores, dt),
+            "single_thread": {"value": 1.0 / dt1, "unit": UNIT, "cores": 1,
+                              "sample": "one FP64 matvec of the CPU restatement on 1 thread in %.1f s" % dt1},
+            "octree_build_s": octree_s,
+            "octree_build": {"cores": 1, "kind": "port", "lmax": oc["lmax"],
+                             "src_boxes_s": ot["src_boxes_s"], "level_sets_s": ot["level_sets_s"],
+                             "sr_lists_s": ot["sr_lists_s"], "sr_lists_s_run": ot["sr_lists_s_run"],
+                             "sample": "srcBoxes (depth %d) + FMMLevelSet + FMMLevelSetNumSR with the reference's "
+                                       "quadratic set algebra (oracle/octree_port.c); FMMLevelSetNumSR on levels 2-%d in "
+                                       "full and on %d of %d level-%d boxes (every k-th), scaled"
+                                       % (DEPTH, DEPTH - 1, leaf_ran, len(oc["set_%d" % DEPTH]), DEPTH)},
+            "fmm_setup_s": fmm_setup}
+    return base, dt / n
+
+
 def cpu_reference_arm(args, world, rank):
-    """Time the FP64 CPU restatement of the reference algorithm on all host cores."""
+    """--impl reference: the reference's CPU path on the machine's host cores (see
+    cpu_baseline_sample); `value` is the all-cores CPU matvec rate, steps and warm-up as given.
+    Loads no library of this package: the mesh is built in NumPy, and only oracle/ runs."""
     if rank != 0:
         return
-    from oracle import oracle_py as O
-    import fmbem_gpu_c_gb300 as fm
-    V, F = make_mesh(fm)
-    k = 2 * np.pi * FREQ / 343.0
-    T = O.tree_for_fmm(V, F, depth=DEPTH)
-    cores = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    f = O.FMM(V, F, k, T, [P_LEVELS[l] for l in range(2, 7)], a=0.5, b=0.0, c=-1.0, rule=0, nthreads=cores)
-    setup = time.perf_counter() - t0
-    rng = np.random.default_rng(0)
-    x = rng.standard_normal(len(F)) + 1j * rng.standard_normal(len(F))
-    for _ in range(args.warmup):
-        f.apply(x)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        f.apply(x)
-    dt = time.perf_counter() - t0
-    v = args.steps / dt
+    base, t_step = cpu_baseline_sample(steps=args.steps, warmup=args.warmup)
+    v = base["value"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c128", "data": "synthetic", "config": workload_config({"setup_s": setup}),
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "full workload, %d matvecs of the FP64 CPU restatement (oracle)" % args.steps},
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic", "config": workload_config(),
+            "cpu_baseline": base,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
-
-
-def cpu_baseline_sample():
-    """Oracle port on all host cores, bounded to ~10 s of CPU work."""
-    from oracle import oracle_py as O
-    import fmbem_gpu_c_gb300 as fm
-    V, F = make_mesh(fm)
-    k = 2 * np.pi * FREQ / 343.0
-    T = O.tree_for_fmm(V, F, depth=DEPTH)
-    cores = os.cpu_count() or 1
-    f = O.FMM(V, F, k, T, [P_LEVELS[l] for l in range(2, 7)], a=0.5, b=0.0, c=-1.0, rule=0, nthreads=cores)
-    rng = np.random.default_rng(0)
-    x = rng.standard_normal(len(F)) + 1j * rng.standard_normal(len(F))
-    y = f.apply(x)
-    n, t0 = 0, time.perf_counter()
-    while time.perf_counter() - t0 < 10.0 and n < 50:
-        f.apply(x)
-        n += 1
-    dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "full workload, %d FP64 matvecs of the CPU restatement (oracle) in %.1f s" % (n, dt)}, x, y
 
 
 def gpu_arm(args, world, rank, local):
@@ -391,17 +429,21 @@ def gpu_arm(args, world, rank, local):
                  "far_field_rel_err_plain": float(np.linalg.norm(ff64 - ffr) / nr),
                  "reference": "FP64-residual refinement to 1e-10 (%d inner iterations)" % itr}
 
+    # the metric's batched configuration (64 right-hand sides on the 200,000-triangle body),
+    # after the timed region and on its own clock record
+    head64 = None if args.no_head64 else head64_run(local)
+
     if rank != 0:
         return
     cpu = None
     if not args.no_cpu_baseline:
-        cpu, xc, yc_ref = cpu_baseline_sample()
+        cpu, _ = cpu_baseline_sample()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64 (FP32 translations and near field, FP64 input/output)", "data": "synthetic",
-        "config": workload_config({"setup_s": setup_s, "parallelism": "replicas" if world > 1 else "single",
-                                   "wall_s_timed_region": wall}),
+        "config": workload_config(),
+        "run": {"setup_s": setup_s, "parallelism": "replicas" if world > 1 else "single", "wall_s_timed_region": wall},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nf * 16, "d2h_bytes_per_step": nf * 16},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "tensor",
@@ -417,6 +459,7 @@ def gpu_arm(args, world, rank, local):
         "fp64_plain": {"value": fp64_rate, "unit": UNIT, "mixed_speedup": value / world / fp64_rate,
                        "mixed_vs_fp64_rel_err": rel_err},
         "solve": solve,
+        "head64": head64,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
     }
@@ -424,13 +467,14 @@ def gpu_arm(args, world, rank, local):
     plan.close()
 
 
-def head64_arm(args, world, rank, local):
+def head64_run(local):
     """The batched right-hand-side workload: a head-like body (ellipsoid 0.075/0.09/0.11 m with
     seeded degree-8 spherical-harmonic bumps of 1.5 mm, 200,000 triangles), 20 kHz, 64 plane
     waves on a Fibonacci sphere solved together (fmm_solve_batched, mixed precision with FP64
     refinement).  The plain FP64 path solves a subset of the columns (its cost per column does
     not depend on how many are solved together), scaled to 64.  Far-field errors at 32 points
-    against an FP64 reference refined to 1e-10 from the mixed solution."""
+    against an FP64 reference refined to 1e-10 from the mixed solution.  Returns the result
+    dict (solve seconds; lower is better)."""
     import torch
     import fmbem_gpu_c_gb300 as fm
     torch.cuda.set_device(local)
@@ -464,24 +508,31 @@ def head64_arm(args, world, rank, local):
         err_p.append(float(np.linalg.norm(plan.far_field(Xp[r], pts) - ref) / nr))
     info = plan.info
     t_plain = t_plain_sub * 64 / nsub
-    line = {
+    plan.close()
+    return {
         "metric": "solve s, 64 plane waves, mixed-prec batched vs FP64 plain at 1e-5 rel far-field err, 1 GB300",
         "value": t_mixed, "unit": "s", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
         "config": {"workload": "head-like bumped ellipsoid 0.075/0.09/0.11 m, 200,000 tri, 20 kHz (k = %.1f), "
                                "64 Fibonacci plane waves, depth 7, p = 40/30/20/14/10/8, Burton-Miller operator "
                                "(I/2 - M) - (i/k) N" % k,
-                   "num_elements": len(F), "lmax": info.lmax, "setup_s": setup_s, "tol": tol},
+                   "num_elements": len(F), "lmax": info.lmax, "tol": tol},
+        "setup_s": setup_s,
         "mixed": {"solve_s": t_mixed, "converged": bool(okm), "iters_max": int(itm.max()),
-                  "relres_max": float(rrm.max()), "far_field_rel_err_max": max(err_m)},
+                  "relres_max": float(rrm.max()), "far_field_rel_err_max": max(err_m),
+                  "far_field_columns_checked": nsub},
         "plain_fp64": {"solve_s_extrapolated": t_plain, "columns_timed": nsub, "solve_s_timed": t_plain_sub,
+                       "scaling": "x 64/%d (each column costs the same whether solved alone or together)" % nsub,
                        "converged": bool(okp), "iters_max": int(itp.max()), "far_field_rel_err_max": max(err_p)},
         "speedup": t_plain / t_mixed,
         "reference": "FP64-residual refinement to 1e-10 of %d columns (converged %s)" % (nsub, bool(okr)),
         "clocks": clk.summary(),
     }
+
+
+def head64_arm(args, world, rank, local):
+    line = head64_run(local)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    plan.close()
 
 
 def vjp_arm(args, world, rank, local):
@@ -656,6 +707,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-solve", dest="solve", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-head64", action="store_true", help="leave out the 64-plane-wave batched solve of the default line")
     ap.add_argument("--bodies", type=int, default=256, help="bodies of --workload bodies")
     ap.add_argument("--body-tri", default="500,20000", help="--workload bodies: range of the log-uniform triangle counts")
     ap.add_argument("--workload", default="sphere-cfg2", choices=["sphere-cfg2", "head64", "vjp", "bodies"],

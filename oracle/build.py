@@ -1,4 +1,5 @@
-"""Build the C oracle (test infrastructure) into oracle/_build/liboracle.so.
+"""Build the C oracle and the port of the reference's CPU octree build (test and baseline
+infrastructure) into oracle/_build/liboracle.so.
 
 Only the test suite, ``__graft_entry__`` and ``bench.py``'s CPU-baseline leg use the
 oracle.  ``build_reference()`` compiles the reference project's own sources through
@@ -13,12 +14,12 @@ REF_LIB = os.path.join(HERE, "_ref", "libfmmref.so")
 
 
 def build(force=False):
-    src = os.path.join(HERE, "fmm_oracle.c")
+    srcs = [os.path.join(HERE, f) for f in ("fmm_oracle.c", "octree_port.c")]
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in srcs):
         return LIB
-    cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off", "-std=gnu99",
-           src, "-o", LIB, "-lm"]
+    cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off", "-std=gnu99"] + srcs + [
+        "-o", LIB, "-lm"]
     subprocess.check_call(cmd)
     return LIB
 

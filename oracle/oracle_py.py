@@ -60,6 +60,8 @@ def lib():
         L.orc_diff_coeff.argtypes = [ctypes.c_double, c_dp, ctypes.c_int, c_dp, c_dp]
         L.orc_rule.argtypes = [ctypes.c_int, c_dp, c_dp]
         L.orc_rule.restype = ctypes.c_int
+        L.orc_port_octree.argtypes = [c_dp, c_ip, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_ip, c_ip,
+                                      c_ip, c_ip, ctypes.c_longlong, c_dp]
         L.orc_rot_size.restype = ctypes.c_int
         L.orc_coax_size.restype = ctypes.c_int
         _lib = L
@@ -315,4 +317,32 @@ def mie_impedance(k, a, beta, pts):
     out = np.zeros(len(pts), dtype=np.complex128)
     beta = complex(beta)
     lib().orc_mie_impedance(k, a, beta.real, beta.imag, len(pts), _d(pts), _d(out.view(np.float64)))
+    return out
+
+
+def port_octree(V, F, s=5, depth=0, sr_sample=0):
+    """The reference's CPU octree build (srcBoxes, FMMLevelSet, FMMLevelSetNumSR) restated in
+    C with its own quadratic set algebra (oracle/octree_port.c), timed.  Returns lmax, the level
+    sets and SR counts per level (-1 for boxes a sampled run left out), and the stage times
+    (srcBoxes, FMMLevelSet, FMMLevelSetNumSR as run, FMMLevelSetNumSR scaled to all boxes)."""
+    V = np.ascontiguousarray(V, dtype=np.float64)
+    F = np.ascontiguousarray(F, dtype=np.int32)
+    cap = 16 * len(F) + 64
+    sets = np.zeros(cap, np.int32)
+    srnum = np.zeros(cap, np.int32)
+    counts = np.zeros(16, np.int32)
+    times = np.zeros(4)
+    lmax = ctypes.c_int(0)
+    rc = lib().orc_port_octree(_d(V), _i(F), len(F), s, depth, sr_sample, ctypes.byref(lmax), _i(counts), _i(sets),
+                               _i(srnum), cap, _d(times))
+    if rc != 0:
+        raise RuntimeError("orc_port_octree failed (lmax %d)" % lmax.value)
+    out = {"lmax": lmax.value, "times": {"src_boxes_s": times[0], "level_sets_s": times[1], "sr_lists_s_run": times[2],
+                                         "sr_lists_s": times[3]}}
+    pos = 0
+    for l in range(2, lmax.value + 1):
+        n = int(counts[l])
+        out["set_%d" % l] = sets[pos:pos + n].copy()
+        out["srnum_%d" % l] = srnum[pos:pos + n].copy()
+        pos += n
     return out

@@ -10,10 +10,14 @@
  * genOctree (translation.cu:3007-3342) in the same order, with the GPU matrix generation
  * left out (it needs a device), so that the level sets, interaction lists, element-to-box
  * indices and translation index arrays come from the reference's own code.
+ * ref_near_lists() gives the leaf near lists I2 ∩ leaf set of that tree, and
+ * ref_octree_stage_times() times the reference's CPU octree stages on a mesh file, the work
+ * that oracle/octree_port.c restates for machines without the reference's sources.
  */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #include "translation.h"
 #include "octree.h"
 #include "integral.h"
@@ -321,4 +325,67 @@ extern "C" void ref_elem_hyper(float k, const float *nod9, const float *nrml3, c
     cuFloatComplex z = sgl ? triElemIntegral_p2Gp1np2n_sgl(k, nod, pt, wgt)
                            : triElemIntegral_p2Gp1np2n_nsgl(k, nod, nr, y, pt, wgt);
     out[0] = cuCrealf(z); out[1] = cuCimagf(z);
+}
+
+/* Leaf near lists of the last ref_octree_build: for each leaf box (leaf-set order) the boxes
+ * of I2(box) (its neighbours in x-y-z order, then itself; octree.c:497-505) that are in the
+ * leaf set, in that order (intersection, octree.c:425-437), as leaf-set indices (findSetInd).
+ * beg[B+1] and idx may be NULL to get the total only. */
+extern "C" long long ref_near_lists(int *beg, int *idx)
+{
+    int l = g_tree.oct.lmax;
+    const int *leaf = g_tree.oct.fmmLevelSet[l - g_tree.oct.lmin];
+    int set1[28], set2[28];
+    long long pos = 0;
+    if (beg) beg[0] = 0;
+    for (int i = 0; i < leaf[0]; i++) {
+        I2(leaf[i + 1], l, set1);
+        intersection(set1, leaf, set2);
+        for (int j = 0; j < set2[0]; j++) {
+            if (idx) idx[pos] = findSetInd(leaf, set2[j + 1]);
+            pos++;
+        }
+        if (beg) beg[i + 1] = (int)pos;
+    }
+    return pos;
+}
+
+static double ref_now(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+/* Seconds of the reference's CPU octree stages on an OBJ file: times[0] srcBoxes (or, with
+ * depth > 0, its fixed-depth variant), times[1] FMMLevelSet, times[2] FMMLevelSetNumSR.
+ * Returns lmax. */
+extern "C" int ref_octree_stage_times(const char *filename, int s, int depth, double *times)
+{
+    int numPt, numElem, lmax = 0;
+    double d;
+    cartCoord_d pt_min;
+    findNum(filename, &numPt, &numElem);
+    cartCoord_d *pt = (cartCoord_d *)malloc(numPt * sizeof(cartCoord_d));
+    triElem *elem = (triElem *)malloc(numElem * sizeof(triElem));
+    readOBJ(filename, pt, elem);
+    int *srcBoxSet = (int *)malloc((numElem + 1) * sizeof(int));
+    double t0 = ref_now();
+    if (depth > 0)
+        srcBoxesDepth(pt, elem, numElem, depth, srcBoxSet, &lmax, &d, &pt_min);
+    else
+        srcBoxes(pt, elem, numElem, s, srcBoxSet, &lmax, &d, &pt_min);
+    double t1 = ref_now();
+    int **sets = (int **)malloc((lmax - 1) * sizeof(int *));
+    FMMLevelSet(srcBoxSet, lmax, sets);
+    double t2 = ref_now();
+    int **num = (int **)malloc((lmax - 1) * sizeof(int *));
+    FMMLevelSetNumSR(sets, lmax, num);
+    double t3 = ref_now();
+    times[0] = t1 - t0;
+    times[1] = t2 - t1;
+    times[2] = t3 - t2;
+    for (int l = 0; l < lmax - 1; l++) { free(sets[l]); free(num[l]); }
+    free(sets); free(num); free(srcBoxSet); free(pt); free(elem);
+    return lmax;
 }

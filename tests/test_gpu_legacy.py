@@ -2,6 +2,7 @@
 matrix generators, through the C ABI."""
 import ctypes
 import os
+import re
 import tempfile
 
 import numpy as np
@@ -113,8 +114,10 @@ def test_genoctree_and_oprl(fm, oracle):
     L.destroyOctree(ctypes.byref(oct_))
 
 
-def test_coaxial_truncation_like_reference_main(fm, oracle):
-    """main.c: the p = 5 (S|R) matrix truncated to p = 2 equals the p = 2 matrix."""
+def test_coaxial_truncation_like_reference_main(fm, oracle, capfd):
+    """The calls of the reference's main.c (main.c:27-38), through the library: the p = 5 (S|R)
+    matrix truncated to p = 2 equals the p = 2 matrix, and the two matrices main.c prints
+    with printMat_cuFloatComplex agree."""
     L = fm.lib()
     L.genSRSparseCoaxTransMat.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     L.reduceSparseCoaxTransMat.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
@@ -123,9 +126,18 @@ def test_coaxial_truncation_like_reference_main(fm, oracle):
     m2 = np.zeros(5, np.complex64)
     assert L.genSRSparseCoaxTransMat(13.1, ctypes.byref(t), 1, 5, m5.ctypes.data) == 0
     assert L.genSRSparseCoaxTransMat(13.1, ctypes.byref(t), 1, 2, m2.ctypes.data) == 0
+    L.printMat_cuFloatComplex.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.printMat_cuFloatComplex(m2.ctypes.data, 1, 5, 1)
     red = np.zeros(5, np.complex64)
     L.reduceSparseCoaxTransMat(m5.ctypes.data, 5, red.ctypes.data, 2)
+    L.printMat_cuFloatComplex(red.ctypes.data, 1, 5, 1)
     assert np.allclose(red, m2, rtol=1e-5, atol=1e-7)
+    ctypes.CDLL(None).fflush(None)  # printf output is buffered when stdout is not a terminal
+    rows = [ln for ln in capfd.readouterr().out.splitlines() if ln.startswith("(")]
+    assert len(rows) == 2, rows
+    a, b = (np.array([complex(float(u), float(v)) for u, v in re.findall(r"\(([^,]+),([^)]+)\)", r)]) for r in rows)
+    assert len(a) == len(b) == 5 and np.allclose(a, b, rtol=1e-5, atol=1e-6)
+    assert np.allclose(a, m2, rtol=1e-5, atol=1e-6)
     g = np.load(os.path.join(GOLDEN, "tables_coax.npz"))
     ref = g["13.1_2.3_5_1"][0::2] + 1j * g["13.1_2.3_5_1"][1::2]
     assert np.linalg.norm(m5 - ref) <= 1e-5 * np.linalg.norm(ref)
