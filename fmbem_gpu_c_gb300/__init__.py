@@ -66,6 +66,10 @@ def lib():
         L.fmm_plan_create_obj.argtypes = [ctypes.c_char_p, ctypes.POINTER(Options), ctypes.POINTER(c_vp)]
         L.fmm_plan_destroy.argtypes = [c_vp]
         L.fmm_plan_info.argtypes = [c_vp, ctypes.POINTER(Info)]
+        L.fmm_plan_lists.argtypes = [c_vp, ctypes.c_int, c_vp, c_vp, c_vp, c_vp]
+        L.fmm_plan_direction.argtypes = [c_vp, ctypes.c_int, c_ip]
+        L.fmm_plan_near_lists.argtypes = [c_vp, c_vp, c_vp, ctypes.POINTER(ctypes.c_longlong), c_vp, c_vp,
+                                          ctypes.POINTER(ctypes.c_longlong)]
         L.fmm_matvec.argtypes = [c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_int]
         L.fmm_matvec_adjoint.argtypes = [c_vp, c_vp, c_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.fmm_gmres.argtypes = [c_vp, c_vp, c_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -292,6 +296,31 @@ class Plan:
         i = Info()
         _check(lib().fmm_plan_info(self.h, ctypes.byref(i)))
         return i
+
+    def lists(self, level):
+        """The M2L lists the matvecs read at `level` (fmm_plan_lists): (boxes, m2l_beg, m2l_src,
+        m2l_dir, offsets) with offsets[d] the integer box offset of direction d."""
+        nb, t = self.info.num_box[level], self.info.num_m2l[level]
+        boxes = np.zeros(nb, np.int64)
+        beg = np.zeros(nb + 1, np.int32)
+        src = np.zeros(max(t, 1), np.int32)
+        dr = np.zeros(max(t, 1), np.int32)
+        _check(lib().fmm_plan_lists(self.h, level, boxes.ctypes.data, beg.ctypes.data, src.ctypes.data, dr.ctypes.data))
+        off = np.zeros((316, 3), np.int32)
+        for d in range(316):
+            _check(lib().fmm_plan_direction(self.h, d, off[d].ctypes.data_as(c_ip)))
+        return boxes, beg, src[:t], dr[:t], off
+
+    def near_lists(self):
+        """Leaf near lists (fmm_plan_near_lists): (box_beg, box_idx, elem_beg, elem_col)."""
+        nbp, nep = ctypes.c_longlong(), ctypes.c_longlong()
+        _check(lib().fmm_plan_near_lists(self.h, None, None, ctypes.byref(nbp), None, None, ctypes.byref(nep)))
+        nb = self.info.num_box[self.info.lmax]
+        bb, bi = np.zeros(nb + 1, np.int32), np.zeros(max(nbp.value, 1), np.int32)
+        eb, ec = np.zeros(self.nf + 1, np.int32), np.zeros(max(nep.value, 1), np.int32)
+        _check(lib().fmm_plan_near_lists(self.h, bb.ctypes.data, bi.ctypes.data, ctypes.byref(nbp), eb.ctypes.data,
+                                         ec.ctypes.data, ctypes.byref(nep)))
+        return bb, bi[:nbp.value], eb, ec[:nep.value]
 
     def matvec(self, x, precision=FMM_FP64, out=None):
         """y = A x.  x: complex128 numpy array (host) or torch tensor (host or CUDA)."""

@@ -76,7 +76,8 @@ __global__ void sr_lists_kernel(const long long *boxes, const long long *skey, c
     if (!pass) count[i] = cnt;
 }
 
-// leaf near lists: I2 ∩ leaf set (octree.c:497-505), up to 27 boxes, self last
+// leaf near lists: I2 ∩ leaf set (octree.c:497-505, 425-437) in I2's order, up to 27
+// boxes: the neighbours in x-y-z order, then the box itself (I2 appends it after neighbors)
 __global__ void near_boxes_kernel(const long long *boxes, const long long *skey, const int *sidx, int nb, int l,
                                   int *nbr, int *nnb)
 {
@@ -214,9 +215,18 @@ int build_lists(Plan *P)
             near_boxes_kernel<<<blocks, 128, 0, P->stream>>>(boxes, skey, sidx, nb, l, nbr, nnb);
             near_count_kernel<<<(P->nf + 255) / 256, 256, 0, P->stream>>>(P->elem_leaf, P->nf, nbr, nnb, P->leaf_beg, ncount);
             FMM_CUDA_TRY(cudaGetLastError());
-            std::vector<int> nc(P->nf), nbeg(P->nf + 1, 0);
+            std::vector<int> nc(P->nf), nbeg(P->nf + 1, 0), hnbr((size_t)27 * nb), hnnb(nb);
             FMM_CUDA_TRY(cudaMemcpyAsync(nc.data(), ncount, sizeof(int) * P->nf, cudaMemcpyDeviceToHost, P->stream));
+            FMM_CUDA_TRY(cudaMemcpyAsync(hnbr.data(), nbr, sizeof(int) * 27 * nb, cudaMemcpyDeviceToHost, P->stream));
+            FMM_CUDA_TRY(cudaMemcpyAsync(hnnb.data(), nnb, sizeof(int) * nb, cudaMemcpyDeviceToHost, P->stream));
             FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+            // the box-level lists, kept on the host for fmm_plan_near_lists
+            P->near_box_beg.assign(nb + 1, 0);
+            P->near_box.clear();
+            for (int i = 0; i < nb; i++) {
+                P->near_box.insert(P->near_box.end(), hnbr.begin() + 27 * (size_t)i, hnbr.begin() + 27 * (size_t)i + hnnb[i]);
+                P->near_box_beg[i + 1] = (int)P->near_box.size();
+            }
             long long tot = 0;
             for (int e = 0; e < P->nf; e++) { tot += nc[e]; nbeg[e + 1] = (int)tot; }
             P->num_near = tot;

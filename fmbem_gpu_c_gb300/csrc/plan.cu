@@ -320,6 +320,59 @@ extern "C" int fmm_plan_info(const fmm_plan *plan, fmm_info *info)
     return FMM_OK;
 }
 
+extern "C" int fmm_plan_lists(const fmm_plan *plan, int level, long long *boxes, int *m2l_beg, int *m2l_src,
+                              int *m2l_dir)
+{
+    if (!plan) { fmm_set_error("null plan"); return FMM_ERR_ARG; }
+    const Plan *P = (const Plan *)plan;
+    if (level < P->lmin || level > P->lmax) {
+        fmm_set_error("fmm_plan_lists: level %d outside %d..%d", level, P->lmin, P->lmax);
+        return FMM_ERR_ARG;
+    }
+    const LevelDev &L = P->lev[level];
+    if (boxes)
+        for (int i = 0; i < L.nb; i++) boxes[i] = P->tree.sets[level][i];
+    if (m2l_beg) FMM_CUDA_TRY(cudaMemcpy(m2l_beg, L.sr_beg, sizeof(int) * (L.nb + 1), cudaMemcpyDeviceToHost));
+    if (m2l_src && L.num_sr)
+        FMM_CUDA_TRY(cudaMemcpy(m2l_src, L.sr_src, sizeof(int) * L.num_sr, cudaMemcpyDeviceToHost));
+    if (m2l_dir && L.num_sr) {
+        std::vector<short> d(L.num_sr);
+        FMM_CUDA_TRY(cudaMemcpy(d.data(), L.sr_dir, sizeof(short) * L.num_sr, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < L.num_sr; i++) m2l_dir[i] = d[i];
+    }
+    return FMM_OK;
+}
+
+extern "C" int fmm_plan_direction(const fmm_plan *plan, int dir, int *offset)
+{
+    if (!plan || !offset || dir < 0 || dir >= NDIR) { fmm_set_error("fmm_plan_direction: invalid argument"); return FMM_ERR_ARG; }
+    const Plan *P = (const Plan *)plan;
+    for (int s = 0; s < 343; s++)
+        if (P->dir_slot[s] == dir) {
+            offset[0] = s / 49 - 3;
+            offset[1] = (s / 7) % 7 - 3;
+            offset[2] = s % 7 - 3;
+            return FMM_OK;
+        }
+    fmm_set_error("fmm_plan_direction: direction %d not found", dir);
+    return FMM_ERR_ARG;
+}
+
+extern "C" int fmm_plan_near_lists(const fmm_plan *plan, int *box_beg, int *box_idx, long long *num_box_pairs,
+                                   int *elem_beg, int *elem_col, long long *num_elem_pairs)
+{
+    if (!plan) { fmm_set_error("null plan"); return FMM_ERR_ARG; }
+    const Plan *P = (const Plan *)plan;
+    if (num_box_pairs) *num_box_pairs = (long long)P->near_box.size();
+    if (num_elem_pairs) *num_elem_pairs = P->num_near;
+    if (box_beg) std::copy(P->near_box_beg.begin(), P->near_box_beg.end(), box_beg);
+    if (box_idx) std::copy(P->near_box.begin(), P->near_box.end(), box_idx);
+    if (elem_beg) FMM_CUDA_TRY(cudaMemcpy(elem_beg, P->near_beg, sizeof(int) * (P->nf + 1), cudaMemcpyDeviceToHost));
+    if (elem_col && P->num_near)
+        FMM_CUDA_TRY(cudaMemcpy(elem_col, P->near_col, sizeof(int) * P->num_near, cudaMemcpyDeviceToHost));
+    return FMM_OK;
+}
+
 static bool is_device_ptr(const void *p)
 {
     cudaPointerAttributes a;

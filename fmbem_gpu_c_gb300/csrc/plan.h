@@ -104,6 +104,7 @@ struct Plan {
     int *leaf_beg = nullptr, *leaf_elem = nullptr;
     double2 *U64 = nullptr, *Rv64 = nullptr;   // P2M / L2P element tables [nf * pleaf^2]
     float2 *U32 = nullptr, *Rv32 = nullptr;
+    std::vector<int> near_box_beg, near_box; // leaf near boxes (I2 ∩ leaf set, I2 order) from near_boxes_kernel
     int *near_beg = nullptr, *near_col = nullptr;
     double2 *near64 = nullptr;
     float2 *near32 = nullptr;

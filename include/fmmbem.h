@@ -104,6 +104,30 @@ int fmm_plan_create_obj(const char *path, const fmm_options *opt, fmm_plan **pla
 int fmm_plan_destroy(fmm_plan *plan);
 int fmm_plan_info(const fmm_plan *plan, fmm_info *info);
 
+/* Copies of the interaction lists the plan's matvecs read, for checking them against the
+ * reference's own.  Host buffers; any may be NULL; sizes from fmm_plan_info.
+ * fmm_plan_lists, level l (lmin..lmax):
+ *   boxes[num_box[l]]       Morton numbers of the level's boxes in the plan's order, which is
+ *                           the reference's fmmLevelSet order (FMMLevelSet, octree.c:890-906)
+ *   m2l_beg[num_box[l]+1]   M2L translations grouped by destination box: those of box i are
+ *                           m2l_beg[i] .. m2l_beg[i+1]-1, in the order of I4 ∩ level set
+ *                           (FMMLevelSetNumSR, octree.c:908-919), so m2l_beg[i+1]-m2l_beg[i] is
+ *                           srNumLevelArr[l-2][i] and m2l_src is srTransOriginArr[l-2]
+ *                           (genSRIdxArrs, translation.cu:2848-2922)
+ *   m2l_src[num_m2l[l]]     source box (index into boxes) of each translation
+ *   m2l_dir[num_m2l[l]]     its direction, 0..315 (fmm_plan_direction gives the box offset) */
+int fmm_plan_lists(const fmm_plan *plan, int level, long long *boxes, int *m2l_beg, int *m2l_src, int *m2l_dir);
+/* The integer box offset (destination minus source, in boxes of the level) of M2L
+ * direction dir. */
+int fmm_plan_direction(const fmm_plan *plan, int dir, int *offset);
+/* Near lists of the leaf level.  box_beg[num_box[lmax]+1] / box_idx[*num_box_pairs]: for each
+ * leaf box the leaf boxes of I2 ∩ leaf set in I2's order -- its neighbours in x-y-z order, then
+ * itself (I2, octree.c:497-505; intersection, octree.c:425-437).  elem_beg[num_elem+1] /
+ * elem_col[*num_elem_pairs]: for each element the elements of those boxes, box after box, each
+ * box's elements in increasing order: the rows of the near-field matrix. */
+int fmm_plan_near_lists(const fmm_plan *plan, int *box_beg, int *box_idx, long long *num_box_pairs, int *elem_beg,
+                        int *elem_col, long long *num_elem_pairs);
+
 /* y = A x for nrhs right-hand sides stored one after another (nf each).  precision is
  * FMM_FP64 (plain path, one column after another) or FMM_MIXED (FP32 translations and near
  * field, all columns in one batched pass).  x and y may be host or device pointers. */

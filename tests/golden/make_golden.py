@@ -17,7 +17,10 @@ fixtures here are its outputs on inputs this project generates:
   (triElemIntegral_pGp2n_*) and of d2G/dn_x dn_y (triElemIntegral_p2Gp1np2n_*), regular and
   singular.
 
-Usage:  python tests/golden/make_golden.py   (needs oracle/build_ref.sh to have run)
+* near-list fixtures: the leaf near lists I2 ∩ leaf set (octree.c:497-505) of every octree
+  case, as leaf-set indices (``make_golden.py near`` regenerates only these).
+
+Usage:  python tests/golden/make_golden.py [near]   (needs oracle/build_ref.sh to have run)
 """
 import ctypes
 import hashlib
@@ -226,8 +229,39 @@ def integral_ext(L):
     np.savez_compressed(os.path.join(HERE, "integral_ext.npz"), **res)
 
 
+def near_lists(L):
+    """Leaf near lists I2 ∩ leaf set of the reference's tree (ref_near_lists: I2, intersection
+    and findSetInd of octree.c) for every octree case: full arrays for the small cases, SHA-256
+    digests and sizes for the large ones (octree_near.npz, octree_near_meta.json)."""
+    L.ref_near_lists.restype = ctypes.c_longlong
+    L.ref_near_lists.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    full, meta = {}, {}
+    for name, subdiv, radius, s, depth, keep_full in OCTREE_CASES:
+        V, F = meshes.icosphere(subdiv, radius)
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "mesh.obj")
+            meshes.write_obj(path, V, F)
+            L.ref_octree_build(path.encode(), s, depth)
+        nb = L.ref_level_count(L.ref_lmax())
+        tot = L.ref_near_lists(None, None)
+        beg = np.zeros(nb + 1, np.int32)
+        idx = np.zeros(tot, np.int32)
+        L.ref_near_lists(ip(beg), ip(idx))
+        if keep_full:
+            full["%s_beg" % name], full["%s_idx" % name] = beg, idx
+        else:
+            meta[name] = {"beg": digest(beg), "idx": digest(idx), "num_pairs": int(tot)}
+        print("near", name, nb, tot, flush=True)
+    np.savez_compressed(os.path.join(HERE, "octree_near.npz"), **full)
+    with open(os.path.join(HERE, "octree_near_meta.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, sort_keys=True)
+
+
 def main():
     L = load_ref()
+    if sys.argv[1:] == ["near"]:
+        near_lists(L)
+        return
     meta = {}
     for case in OCTREE_CASES:
         meta[case[0]] = octree_case(L, *case)
@@ -237,6 +271,7 @@ def main():
     integral_ext(L)
     with open(os.path.join(HERE, "octree_meta.json"), "w") as fh:
         json.dump(meta, fh, indent=1, sort_keys=True)
+    near_lists(L)
 
 
 if __name__ == "__main__":

@@ -57,6 +57,22 @@ def test_octree_matches_reference(case):
             assert digest(val) == m["sha256"][key], key
 
 
+@pytest.mark.parametrize("case", ["ico2_r0.1_s5", "ico3_r0.1_s5", "ico3_r0.1_d3", "ico4_r0.3_s5", "ico5_r0.3_d5"])
+def test_near_lists_match_reference(case):
+    """Leaf near lists I2 ∩ leaf set, in I2's order (the box itself last), equal the reference's."""
+    near = np.load(os.path.join(GOLDEN, "octree_near.npz"))
+    nmeta = json.load(open(os.path.join(GOLDEN, "octree_near_meta.json")))
+    V, F, T = _oracle_tree(case)
+    nl = oo.near_lists(T["level_sets"], T["lmax"])
+    beg = np.concatenate([[0], np.cumsum([len(x) for x in nl])]).astype(np.int32)
+    idx = np.concatenate([np.asarray(x) for x in nl]).astype(np.int32)
+    if case + "_beg" in near.files:
+        assert np.array_equal(beg, near[case + "_beg"]) and np.array_equal(idx, near[case + "_idx"])
+    else:
+        assert digest(beg) == nmeta[case]["beg"] and digest(idx) == nmeta[case]["idx"]
+    assert all(x[-1] == i for i, x in enumerate(nl))
+
+
 def test_quadrature_and_green_vs_reference(oracle):
     """Element integrals of G and dG/dn (regular and singular) against the reference's FP32."""
     q = np.load(os.path.join(GOLDEN, "quadrature.npz"))
