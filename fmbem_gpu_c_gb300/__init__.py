@@ -66,6 +66,7 @@ def lib():
         L.fmm_plan_create_obj.argtypes = [ctypes.c_char_p, ctypes.POINTER(Options), ctypes.POINTER(c_vp)]
         L.fmm_plan_destroy.argtypes = [c_vp]
         L.fmm_plan_info.argtypes = [c_vp, ctypes.POINTER(Info)]
+        L.fmm_vjp_admittance.argtypes = [c_vp, c_vp, c_dp, ctypes.c_int, c_vp, c_vp, c_vp, c_dp]
         L.fmm_plan_lists.argtypes = [c_vp, ctypes.c_int, c_vp, c_vp, c_vp, c_vp]
         L.fmm_plan_direction.argtypes = [c_vp, ctypes.c_int, c_ip]
         L.fmm_plan_near_lists.argtypes = [c_vp, c_vp, c_vp, ctypes.POINTER(ctypes.c_longlong), c_vp, c_vp,
@@ -382,6 +383,21 @@ class Plan:
         _check(lib().fmm_vjp(self.h, _ptr(x), None if d is None else d.ctypes.data_as(c_dp), pts.ctypes.data_as(c_dp),
                              len(pts), _ptr(pbar), tol, precision, grad.ctypes.data_as(c_dp), _ptr(lam)))
         return grad, lam
+
+    def vjp_admittance(self, x, pts, pbar, lam):
+        """Admittance derivative (fmm_vjp_admittance) for b = i k beta, a = (1 + alpha b)/2:
+        returns (g, dJ_dbeta) with dJ = 2 Re sum_j g_j dbeta_j per element and dJ_dbeta =
+        (dJ/dRe beta, dJ/dIm beta) for one admittance on the whole surface.  lam: the adjoint
+        solution fmm_vjp returned for the same x, pts, pbar."""
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        pts = np.ascontiguousarray(pts, dtype=np.float64)
+        pbar = np.ascontiguousarray(pbar, dtype=np.complex128)
+        lam = np.ascontiguousarray(lam, dtype=np.complex128)
+        g = np.zeros(self.nf, dtype=np.complex128)
+        dj = np.zeros(2)
+        _check(lib().fmm_vjp_admittance(self.h, _ptr(x), pts.ctypes.data_as(c_dp), len(pts), _ptr(pbar), _ptr(lam),
+                                        _ptr(g), dj.ctypes.data_as(c_dp)))
+        return g, dj
 
     def far_field(self, p, pts):
         p = np.ascontiguousarray(p, dtype=np.complex128)

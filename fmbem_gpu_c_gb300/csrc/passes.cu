@@ -665,15 +665,18 @@ void launch_conj(Plan *P, const double2 *x, double2 *y, size_t n)
 
 // Near-field matrix transposed (CSR by source element), built on first use of the
 // transposed operator: (A^T y)_j collects A_ij y_i over the targets i near j.
-int build_transpose(Plan *P)
+// The transpose of the near-field pattern: row beginnings tb and columns tc by source
+// element, and for each transposed entry the position of the same pair in the forward CSR.
+static int near_transpose_pattern(Plan *P, std::vector<int> &tb, std::vector<int> &tc, std::vector<long long> &perm)
 {
-    if (P->nearT_beg) return FMM_OK;
     long long nnz = P->num_near;
     std::vector<int> beg(P->nf + 1), col(nnz);
     FMM_CUDA_TRY(cudaMemcpy(beg.data(), P->near_beg, sizeof(int) * (P->nf + 1), cudaMemcpyDeviceToHost));
     FMM_CUDA_TRY(cudaMemcpy(col.data(), P->near_col, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
-    std::vector<int> tb(P->nf + 1, 0), tc(nnz), fill(P->nf, 0);
-    std::vector<long long> perm(nnz);
+    std::vector<int> fill(P->nf, 0);
+    tb.assign(P->nf + 1, 0);
+    tc.resize(nnz);
+    perm.resize(nnz);
     for (long long s = 0; s < nnz; s++) tb[col[s] + 1]++;
     for (int j = 0; j < P->nf; j++) tb[j + 1] += tb[j];
     for (int i = 0; i < P->nf; i++)
@@ -683,6 +686,35 @@ int build_transpose(Plan *P)
             tc[pos] = i;
             perm[pos] = s;
         }
+    return FMM_OK;
+}
+
+// valsT = the near-field values `vals` (forward CSR order) in the transposed CSR order
+int near_transpose_values(Plan *P, const double2 *vals, double2 *valsT)
+{
+    std::vector<int> tb, tc;
+    std::vector<long long> perm;
+    int st = near_transpose_pattern(P, tb, tc, perm);
+    if (st) return st;
+    long long nnz = P->num_near;
+    long long *perm_dev = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&perm_dev, sizeof(long long) * std::max<long long>(1, nnz)));
+    FMM_CUDA_TRY(cudaMemcpy(perm_dev, perm.data(), sizeof(long long) * nnz, cudaMemcpyHostToDevice));
+    gather_kernel<<<152 * 8, 256, 0, P->stream>>>(vals, perm_dev, nnz, valsT);
+    FMM_CUDA_TRY(cudaGetLastError());
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    cudaFree(perm_dev);
+    return FMM_OK;
+}
+
+int build_transpose(Plan *P)
+{
+    if (P->nearT_beg) return FMM_OK;
+    long long nnz = P->num_near;
+    std::vector<int> tb, tc;
+    std::vector<long long> perm;
+    int st = near_transpose_pattern(P, tb, tc, perm);
+    if (st) return st;
     long long *perm_dev = nullptr;
     FMM_CUDA_TRY(cudaMalloc(&perm_dev, sizeof(long long) * std::max<long long>(1, nnz)));
     FMM_CUDA_TRY(cudaMemcpy(perm_dev, perm.data(), sizeof(long long) * nnz, cudaMemcpyHostToDevice));

@@ -160,6 +160,7 @@ void line_rule(int n, double *x, double *w);
 int gen_coax_tables(Plan *P);
 int gen_element_tables(Plan *P);
 int gen_near_field(Plan *P);
+int gen_operator_part(Plan *P, double2 bco, double2 cco, double2 *U, double2 *Rv_tmp, double2 *nearv);
 int launch_far_field(Plan *P, const double2 *p, const double *pts, int npts, double2 *out);
 int launch_plane_wave(Plan *P, const double *dir, double2 *rhs);
 int gen_rotation_matrices_f32(const double *alpha, const double *beta, const double *gamma, int n, int p, float2 *host_out);
@@ -172,6 +173,7 @@ int build_lists(Plan *P);
 // y = A x (or A^T x) for nrhs columns of nf entries, device pointers
 int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpose = 0, int nrhs = 1);
 int build_transpose(Plan *P);
+int near_transpose_values(Plan *P, const double2 *vals, double2 *valsT);
 void launch_conj(Plan *P, const double2 *x, double2 *y, size_t n);
 void drop_graph(Plan *P);
 

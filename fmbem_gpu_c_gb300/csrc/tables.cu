@@ -846,7 +846,9 @@ __global__ void element_tables_kernel(const double *V, const int *F, const int *
     }
 }
 
-int gen_element_tables(Plan *P)
+// The element tables of the operator with source coefficients (bco, cco) into U and Rv
+// (nf * pleaf^2 entries each), on the plan's stream, synchronised.
+static int launch_element_tables(Plan *P, double2 bco, double2 cco, double2 *U, double2 *Rv)
 {
     int st = upload_rules();
     if (st != FMM_OK) return st;
@@ -865,9 +867,6 @@ int gen_element_tables(Plan *P)
     double *ctr_dev = nullptr;
     FMM_CUDA_TRY(cudaMalloc(&ctr_dev, sizeof(double) * ctr.size()));
     FMM_CUDA_TRY(cudaMemcpy(ctr_dev, ctr.data(), sizeof(double) * ctr.size(), cudaMemcpyHostToDevice));
-    size_t tbl = (size_t)P->nf * pl * pl;
-    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->U64, sizeof(double2) * tbl));
-    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->Rv64, sizeof(double2) * tbl));
     int pb = pl + 1;
     int warps = 4;
     size_t shm = (size_t)basis_per_warp(pb) * warps * sizeof(double);
@@ -877,7 +876,6 @@ int gen_element_tables(Plan *P)
         if (e) return e;
     }
     int blocks = std::min((P->nf + warps - 1) / warps, 152 * 32);
-    double2 bco = make_double2(P->opt.b_re, P->opt.b_im), cco = make_double2(P->opt.c_re, P->opt.c_im);
     double2 alpha = make_double2(P->opt.alpha_re, P->opt.alpha_im);
     // the recurrence factors, with the expressions the device used to evaluate per point
     const int W = 2 * pb + 3, ntri = pb * (pb + 1) / 2;
@@ -909,11 +907,23 @@ int gen_element_tables(Plan *P)
     T.W = W;
     T.pb = pb;
     element_tables_kernel<<<blocks, 32 * warps, shm, P->stream>>>(P->V_dev, P->F_dev, P->elem_leaf, ctr_dev, P->nf, pl,
-                                                                   P->opt.k, bco, cco, alpha, P->opt.rule, T, P->U64,
-                                                                   P->Rv64);
+                                                                   P->opt.k, bco, cco, alpha, P->opt.rule, T, U, Rv);
     FMM_CUDA_TRY(cudaGetLastError());
     FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
     cudaFree(tab_dev);
+    cudaFree(ctr_dev);
+    return FMM_OK;
+}
+
+int gen_element_tables(Plan *P)
+{
+    int pl = P->pleaf;
+    size_t tbl = (size_t)P->nf * pl * pl;
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->U64, sizeof(double2) * tbl));
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->Rv64, sizeof(double2) * tbl));
+    double2 bco = make_double2(P->opt.b_re, P->opt.b_im), cco = make_double2(P->opt.c_re, P->opt.c_im);
+    int st = launch_element_tables(P, bco, cco, P->U64, P->Rv64);
+    if (st) return st;
     if (P->opt.build_mixed) {
         FMM_CUDA_TRY(dev_alloc(P, (void **)&P->U32, sizeof(float2) * tbl));
         FMM_CUDA_TRY(dev_alloc(P, (void **)&P->Rv32, sizeof(float2) * tbl));
@@ -934,7 +944,6 @@ int gen_element_tables(Plan *P)
         }
         FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
     }
-    cudaFree(ctr_dev);
     return FMM_OK;
 }
 
@@ -988,6 +997,23 @@ __global__ void near_field_kernel(const double *V, const int *F, int nf, const i
             out[s] = v;
         }
     }
+}
+
+// The FP64 element tables (P2M moments U) and near-field matrix of the operator part with
+// source coefficients (bco, cco) -- the plan's own a, b, c set aside -- into caller buffers of
+// nf * pleaf^2 and num_near entries (the adjoint path's derivatives in b and c).  The L2P
+// vectors do not depend on b and c; Rv_tmp (nf * pleaf^2 entries) receives a copy.
+int gen_operator_part(Plan *P, double2 bco, double2 cco, double2 *U, double2 *Rv_tmp, double2 *nearv)
+{
+    int st = launch_element_tables(P, bco, cco, U, Rv_tmp);
+    if (st) return st;
+    int blocks = std::min((P->nf + 7) / 8, 152 * 16);
+    double2 alpha = make_double2(P->opt.alpha_re, P->opt.alpha_im);
+    near_field_kernel<<<blocks, 256, 0, P->stream>>>(P->V_dev, P->F_dev, P->nf, P->near_beg, P->near_col, P->opt.k,
+                                                      bco, cco, alpha, P->opt.rule, nearv);
+    FMM_CUDA_TRY(cudaGetLastError());
+    FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    return FMM_OK;
 }
 
 int gen_near_field(Plan *P)

@@ -808,6 +808,19 @@ __global__ void vjp_far_source_kernel(const double *V, const int *F, int nf, int
     }
 }
 
+// g_beta[j] = i k ( (w_j - z_j) x_j - (alpha/2) mu_j x_j ): the admittance derivative per
+// element (see fmm_vjp_admittance)
+__global__ void vjp_admittance_kernel(int nf, double k, double2 alpha, const double2 *w, const double2 *z,
+                                      const double2 *mu, const double2 *x, double2 *g)
+{
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf; j += gridDim.x * blockDim.x) {
+        double2 gb = cmul(csub(w[j], z[j]), x[j]);
+        double2 ga = cmul(mu[j], x[j]);
+        double2 t = csub(gb, cscale(cmul(alpha, ga), 0.5));
+        g[j] = make_double2(-k * t.y, k * t.x);
+    }
+}
+
 } // namespace fmm
 
 using namespace fmm;
@@ -928,6 +941,106 @@ done:
 #undef VTRY
     for (void *q : {(void *)xd, (void *)pb, (void *)rhs, (void *)mu, (void *)tmp, (void *)D, (void *)Dz, (void *)Dp, (void *)Dm,
                     (void *)ptd, (void *)gd, (void *)ctr})
+        if (q) cudaFree(q);
+    return rc;
+}
+
+// Admittance derivative of the far-field objective of fmm_vjp.  For a locally reacting surface
+// dp/dn = i k beta_j p on element j the operator is A = a I + (1 + alpha d/dn_y)(L B + c M), with
+// B = diag(b_j), b_j = i k beta_j at the source elements and, with the Burton-Miller coupling,
+// a_i = (1 + alpha b_i)/2 at the targets; the far field is F x = M x - L_far (B x).  So
+//     dJ = 2 Re sum_j g_j dbeta_j,
+//     g_j = i k [ x_j (w_j - z_j) - (alpha/2) conj(lambda_j) x_j ],
+// w = (dF/db)^T conj(pbar) (the far-field operator with b = 1, c = 0), z = S^T conj(lambda) with
+// S = (1 + alpha d/dn_y) L: one transposed FP64 FMM pass of the plan with its element tables and
+// near-field matrix regenerated for (a, b, c) = (0, 1, 0), on temporary buffers that stand in for
+// the plan's own during the pass.
+extern "C" int fmm_vjp_admittance(fmm_plan *plan, const cuDoubleComplex *x, const double *pts, int npts,
+                                  const cuDoubleComplex *pbar, const cuDoubleComplex *lambda, cuDoubleComplex *g_beta,
+                                  double *dJ_dbeta)
+{
+    Plan *P = (Plan *)plan;
+    if (!P || !x || !pts || npts < 1 || !pbar || !lambda || (!g_beta && !dJ_dbeta)) {
+        fmm_set_error("fmm_vjp_admittance: invalid argument");
+        return FMM_ERR_ARG;
+    }
+    int nf = P->nf, pl = P->pleaf;
+    cudaStream_t st = P->stream;
+    int rc = build_transpose(P);
+    if (rc) return rc;
+    size_t tbl = (size_t)nf * pl * pl;
+    long long nnz = P->num_near;
+    double2 *xd = nullptr, *mu = nullptr, *pb = nullptr, *w = nullptr, *z = nullptr, *U = nullptr, *Rv = nullptr,
+            *nearL = nullptr, *nearTL = nullptr, *g = nullptr;
+    double *ptd = nullptr;
+    std::vector<double2> hg;
+#define ATRY(call)                                                                                                 \
+    do {                                                                                                           \
+        cudaError_t e_ = (call);                                                                                   \
+        if (e_ != cudaSuccess) { fmm_set_error("fmm_vjp_admittance: %s: %s", #call, cudaGetErrorString(e_)); rc = FMM_ERR_CUDA; goto done; } \
+    } while (0)
+    ATRY(cudaMalloc(&xd, sizeof(double2) * nf));
+    ATRY(cudaMalloc(&mu, sizeof(double2) * nf));
+    ATRY(cudaMalloc(&w, sizeof(double2) * nf));
+    ATRY(cudaMalloc(&z, sizeof(double2) * nf));
+    ATRY(cudaMalloc(&g, sizeof(double2) * nf));
+    ATRY(cudaMalloc(&pb, sizeof(double2) * npts));
+    ATRY(cudaMalloc(&ptd, sizeof(double) * 3 * npts));
+    ATRY(cudaMalloc(&U, sizeof(double2) * tbl));
+    ATRY(cudaMalloc(&Rv, sizeof(double2) * tbl));
+    ATRY(cudaMalloc(&nearL, sizeof(double2) * (nnz + 1)));
+    ATRY(cudaMalloc(&nearTL, sizeof(double2) * (nnz + 1)));
+    ATRY(cudaMemcpyAsync(xd, x, sizeof(double2) * nf, cudaMemcpyDefault, st));
+    ATRY(cudaMemcpyAsync(w, lambda, sizeof(double2) * nf, cudaMemcpyDefault, st));
+    ATRY(cudaMemcpyAsync(pb, pbar, sizeof(double2) * npts, cudaMemcpyDefault, st));
+    ATRY(cudaMemcpyAsync(ptd, pts, sizeof(double) * 3 * npts, cudaMemcpyDefault, st));
+    launch_conj(P, w, mu, nf); // mu = conj(lambda)
+    ATRY(cudaGetLastError());
+    if ((rc = gen_operator_part(P, make_double2(1.0, 0.0), make_double2(0.0, 0.0), U, Rv, nearL))) goto done;
+    if ((rc = near_transpose_values(P, nearL, nearTL))) goto done;
+    {
+        // z = S^T mu with the single-layer part standing in for the plan's operator
+        double2 *sU = P->U64, *sN = P->near64, *sNT = P->nearT64;
+        fmm_options so = P->opt;
+        P->U64 = U;
+        P->near64 = nearL;
+        P->nearT64 = nearTL;
+        P->opt.a_re = P->opt.a_im = 0.0;
+        P->opt.b_re = 1.0;
+        P->opt.b_im = 0.0;
+        P->opt.c_re = P->opt.c_im = 0.0;
+        rc = run_matvec(P, mu, z, FMM_FP64, 1, 1);
+        cudaError_t e2 = cudaStreamSynchronize(st);
+        P->U64 = sU;
+        P->near64 = sN;
+        P->nearT64 = sNT;
+        P->opt = so;
+        if (rc) goto done;
+        ATRY(e2);
+    }
+    {
+        const int T = 128, B = std::min((nf + T - 1) / T, 152 * 8);
+        // w = (dF/db)^T conj(pbar): the far-field operator -int G of unit b
+        vjp_adjoint_rhs_kernel<<<B, T, 0, st>>>(P->V_dev, P->F_dev, nf, P->opt.k, P->opt.rule, make_double2(-1.0, 0.0),
+                                                make_double2(0.0, 0.0), ptd, npts, pb, w);
+        vjp_admittance_kernel<<<B, T, 0, st>>>(nf, P->opt.k, make_double2(P->opt.alpha_re, P->opt.alpha_im), w, z, mu, xd, g);
+        ATRY(cudaGetLastError());
+        hg.resize(nf);
+        ATRY(cudaMemcpyAsync(hg.data(), g, sizeof(double2) * nf, cudaMemcpyDeviceToHost, st));
+        ATRY(cudaStreamSynchronize(st));
+        if (g_beta) ATRY(cudaMemcpy(g_beta, hg.data(), sizeof(double2) * nf, cudaMemcpyDefault));
+        if (dJ_dbeta) {
+            double sr = 0.0, si = 0.0;
+            for (int j = 0; j < nf; j++) { sr += hg[j].x; si += hg[j].y; }
+            dJ_dbeta[0] = 2.0 * sr;  // dJ/dRe(beta) = 2 Re g
+            dJ_dbeta[1] = -2.0 * si; // dJ/dIm(beta) = 2 Re(i g)
+        }
+        rc = FMM_OK;
+    }
+done:
+#undef ATRY
+    for (void *q : {(void *)xd, (void *)mu, (void *)pb, (void *)w, (void *)z, (void *)U, (void *)Rv, (void *)nearL,
+                    (void *)nearTL, (void *)g, (void *)ptd})
         if (q) cudaFree(q);
     return rc;
 }

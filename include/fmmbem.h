@@ -226,6 +226,22 @@ int fmm_selftest_bounded_wait(int device, int *gave_up, int *completed);
 int fmm_vjp(fmm_plan *plan, const cuDoubleComplex *x, const double *dir, const double *pts, int npts,
             const cuDoubleComplex *pbar, double tol, int precision, double *grad, cuDoubleComplex *lambda);
 
+/* Derivative of the same objective with respect to the surface admittance, for a plan built
+ * for a locally reacting surface dp/dn = i k beta p: b = i k beta and, with the Burton-Miller
+ * coupling alpha, a = (1 + alpha b)/2.  With beta allowed to vary per element,
+ *     dJ = 2 Re sum_j g_beta[j] dbeta_j,
+ * and for one admittance on the whole surface dJ_dbeta[0] = dJ/dRe(beta), dJ_dbeta[1] =
+ * dJ/dIm(beta).  x, pts, pbar as for fmm_vjp and lambda the adjoint solution fmm_vjp returned
+ * for them (no second adjoint solve).  The derivative of the operator in b is its
+ * single-layer part (1 + alpha d/dn_y) L, applied transposed by one FP64 FMM pass with element
+ * tables and a near-field matrix regenerated for it (temporary device memory of about the
+ * plan's FP64 element tables plus two near-field matrices).  g_beta[nf] or dJ_dbeta[2] may be
+ * NULL; host or device buffers.  No counterpart in the reference, whose triElem.alpha/beta/gamma
+ * (structs.h:75-81) are never used. */
+int fmm_vjp_admittance(fmm_plan *plan, const cuDoubleComplex *x, const double *pts, int npts,
+                       const cuDoubleComplex *pbar, const cuDoubleComplex *lambda, cuDoubleComplex *g_beta,
+                       double *dJ_dbeta);
+
 /* Scattered pressure at npts exterior points y from the surface pressure p:
  * -sum_j p_j int_{T_j} (b G + c dG/dn_x)(x, y) dS(x) with the plan's b and c and regular rule,
  * i.e. M p - L dp/dn for the exterior problem (c = -1, b = (dp/dn)/p; rigid body: M p). */
