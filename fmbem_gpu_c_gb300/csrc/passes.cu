@@ -385,9 +385,10 @@ RcrList *pass32_desc(Plan *P, int l, int which, int nrhs, RcrPass &ps)
 
 int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st)
 {
-    if (which == PASS_M2L && P->lev[l].tc.on) return launch_tc_m2l(P, l, nrhs, st);
     RcrPass ps;
     RcrList *Lst = pass32_desc(P, l, which, nrhs, ps);
+    if (Lst && Lst->t3.on) return launch_tc3_pass(P, l, which, nrhs, st);
+    if (which == PASS_M2L && P->lev[l].tc.on) return launch_tc_m2l(P, l, nrhs, st);
     return Lst ? launch_rcr_pass(*Lst, ps, st) : FMM_OK;
 }
 

@@ -89,7 +89,12 @@ static void free_plan(Plan *P)
         LevelDev &L = P->lev[l];
         F(L.parent); F(L.octant); F(L.child_beg); F(L.child_list); F(L.sr_beg); F(L.sr_src); F(L.sr_dir);
         F(L.Cm64); F(L.Dl64); F(L.Cm32); F(L.Dl32); F(L.Csr64); F(L.Csr32); F(L.Crr64); F(L.Crr32); F(L.Crr32L);
-        for (RcrList *R : {&L.m2l, &L.m2m, &L.l2l}) { F(R->items); F(R->src); F(R->dst); }
+        for (RcrList *R : {&L.m2l, &L.m2m, &L.l2l}) {
+            F(R->items); F(R->src); F(R->dst);
+            Tc3 &t = R->t3;
+            F(t.opsR); F(t.opsC); F(t.blkR); F(t.blkC); F(t.t_dir); F(t.itR1); F(t.itC); F(t.itR2);
+            F(t.listR); F(t.listC); F(t.W); F(t.Z);
+        }
         F(L.tc.B); F(L.tc.items);
     }
     F(P->tc_err); F(P->m2l_part64);
@@ -238,6 +243,7 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
         TRY(build_rcr_lists(P));
         TRY(tune_rcr_tiles(P));
         TRY(tune_tc_m2l(P));
+        TRY(tune_tc3(P));
     }
     CTRY(dev_alloc(P, (void **)&P->xbuf, sizeof(double2) * nf));
     CTRY(dev_alloc(P, (void **)&P->ybuf, sizeof(double2) * nf));
@@ -312,6 +318,8 @@ extern "C" int fmm_plan_info(const fmm_plan *plan, fmm_info *info)
         info->num_m2l[l] = P->lev[l].num_sr;
         info->m2l_columns[l] = P->opt.build_mixed ? (P->lev[l].tc.on ? 128 : P->lev[l].m2l.tc) : 0;
         info->m2l_tensor[l] = P->opt.build_mixed && P->lev[l].tc.on ? 1 : 0;
+        if (P->opt.build_mixed)
+            info->pass_tc3[l] = (P->lev[l].m2m.t3.on ? 1 : 0) | (P->lev[l].m2l.t3.on ? 2 : 0) | (P->lev[l].l2l.t3.on ? 4 : 0);
     }
     info->expansions_scaled = P->opt.build_mixed && P->scaled ? 1 : 0;
     info->num_near = P->num_near;

@@ -12,6 +12,27 @@ constexpr int NDIST = 15;      // distinct squared lengths of those offsets
 constexpr int MAX_TIMERS = 64;
 constexpr int NSIDE = 8;      // side streams for the independent M2L passes (at most)
 
+// Three-stage tensor-core form of one batched pass (tc_rcr3.cu): rotation blocks per
+// polar-angle class and coaxial blocks per length class, split into TF32 hi/lo tiles; chunks,
+// class orders and work items for items_nrhs right-hand sides; the W and Z scratch.
+struct Tc3 {
+    int on = 0, built = 0;
+    int p = 0, pinr = 0, nq = 0, T = 0, nclsR = 0, nclsC = 0;
+    std::vector<int> clsR_of_t, clsC_of_t;   // class of each translation (list order)
+    std::vector<int4> hblkR, hblkC;          // per block: (table offset, K, Npad, valid N)
+    long long strideR = 0, strideC = 0;      // floats per class
+    float *opsR = nullptr, *opsC = nullptr;
+    int4 *blkR = nullptr, *blkC = nullptr;
+    int *t_dir = nullptr;                    // direction of each translation
+    int items_nrhs = 0;
+    std::vector<int> chunk_t0, it_beg;
+    int4 *itR1 = nullptr, *itC = nullptr, *itR2 = nullptr;
+    size_t capR1 = 0, capC = 0, capR2 = 0;
+    int *listR = nullptr, *listC = nullptr;
+    float2 *W = nullptr, *Z = nullptr;
+    size_t scratch_cap = 0;
+};
+
 // Work list of one batched translation pass: translations sorted by direction (src, dst,
 // key_beg per direction, key_w = coaxial block per direction) and the device items
 // (direction, first column, count, coaxial block) for items_nrhs right-hand sides, tc
@@ -25,6 +46,7 @@ struct RcrList {
     int ndst_rank = 0;            // boxes of the destination level
     int n_items = 0, items_nrhs = 0;
     int tc = 8, shc = 0;          // columns per item; rotation/coaxial blocks staged in shared memory
+    Tc3 t3;                       // three-stage tensor-core form (used where t3.on)
 };
 
 // M2L of one level on the tensor cores (tc_m2l.cu): the level's 316 translation operators
@@ -190,6 +212,11 @@ int gen_dense_m2l(Plan *P, int l, double2 *T);   // passes.cu
 int tune_tc_m2l(Plan *P);
 int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st);
 int check_tc_error(Plan *P);
+
+// tc_rcr3.cu
+int build_tc3(Plan *P, int l, int which);
+int launch_tc3_pass(Plan *P, int l, int which, int nrhs, cudaStream_t st);
+int tune_tc3(Plan *P);
 
 // batched.cu
 int build_rcr_lists(Plan *P);

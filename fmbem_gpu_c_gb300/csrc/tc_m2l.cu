@@ -28,6 +28,7 @@
 // copies a direction's operator once per run of its tiles (operator-full barrier), and the MMA
 // warp releases it after the run's last tile (a commit to the operator-empty barrier).
 #include "plan.h"
+#include "tc_common.cuh"
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -84,48 +85,6 @@ static bool tc_geometry(int p, TcM2L &g)
     // stays in shared memory while a CTA's consecutive tiles keep its direction
     g.res = g.nhalf == 1 && tc_smem_bytes(g.Nmma, 1, g.nch) <= TC_SMEM_MAX ? 1 : 0;
     return true;
-}
-
-// byte offset of element (row r, k) in a no-swizzle K-major tile of KC columns: 8-row x 16-byte
-// core matrices, K-adjacent cores 128 B apart (leading byte offset), 8-row groups 32 KC apart
-// (stride byte offset)
-__host__ __device__ __forceinline__ uint32_t core_off(int r, int k, int KC)
-{
-    return (uint32_t)((r >> 3) * 32 * KC + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
-}
-
-__device__ __forceinline__ float tf32_trunc(float x) { return __int_as_float(__float_as_int(x) & (int)0xffffe000); }
-
-__device__ __forceinline__ uint32_t smem_u32(const void *ptr) { return (uint32_t)__cvta_generic_to_shared(ptr); }
-
-// shared-memory matrix descriptor (no swizzle): start, leading and stride byte offsets (>> 4),
-// descriptor version 1 at bits 46-47
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
-{
-    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
-           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
-}
-
-// wait for the phase of the given parity of an mbarrier, at most `limit` SM clock cycles;
-// false when the wait gave up
-__device__ __forceinline__ bool mbar_wait_limit(uint32_t bar, uint32_t parity, long long limit)
-{
-    long long t0 = clock64();
-    while (true) {
-        uint32_t done;
-        asm volatile("{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\tselp.u32 %0, 1, 0, q;\n\t}"
-                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
-        if (done) return true;
-        if (clock64() - t0 > limit) return false;
-    }
-}
-
-// the kernel's waits: at most ~1 s of SM clock
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) { return mbar_wait_limit(bar, parity, 2000000000LL); }
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 // destination / source expansion of row r of tile (it): column e = translation t x nrhs + r,

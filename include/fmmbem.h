@@ -86,6 +86,12 @@ typedef struct {
     int expansions_scaled;               /* mixed path: 1 where the FP32 expansions are kept scaled by degree
                                             (low k t, where the plain coaxial entries would leave the FP32
                                             range): multipoles d_n M_n, locals L_n / d_n per level */
+    int pass_tc3[FMM_MAX_LEVEL + 1];     /* mixed path: passes of level l run as three tensor-core stages
+                                            (tcgen05, split TF32: rotation, coaxial, rotation GEMMs over the
+                                            translations that share each operator) -- bit 0 the M2M from
+                                            level l into l-1, bit 1 the M2L of level l, bit 2 the L2L from
+                                            l-1 into l; chosen at plan creation by timing against the other
+                                            forms (FMMBEM_TC3=0: never, 1: wherever the order allows) */
 } fmm_info;
 
 typedef struct fmm_plan fmm_plan;
