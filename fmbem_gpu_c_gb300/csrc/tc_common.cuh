@@ -15,7 +15,12 @@ __host__ __device__ __forceinline__ uint32_t core_off(int r, int k, int KC)
     return (uint32_t)((r >> 3) * 32 * KC + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
 }
 
-__device__ __forceinline__ float tf32_trunc(float x) { return __int_as_float(__float_as_int(x) & (int)0xffffe000); }
+// x rounded to the nearest TF32 value (10 explicit mantissa bits; halves away from zero) by
+// adding half a TF32 unit to the magnitude bits and clearing the 13 low bits.  As the hi part of
+// a split, x = hi + lo with lo = tf32_round(x - hi) keeps about 24 bits, against about 20 for
+// truncated halves.
+__host__ __device__ __forceinline__ uint32_t tf32_round_bits(uint32_t u) { return (u + 0x1000u) & 0xffffe000u; }
+__device__ __forceinline__ float tf32_round(float x) { return __uint_as_float(tf32_round_bits(__float_as_uint(x))); }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *ptr) { return (uint32_t)__cvta_generic_to_shared(ptr); }
 

@@ -263,10 +263,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
 #pragma unroll
                 for (int j = 0; j < KH; j += 4) {
                     float4 hi, lo;
-                    hi.x = tf32_trunc(x[j]); lo.x = tf32_trunc(x[j] - hi.x);
-                    hi.y = tf32_trunc(x[j + 1]); lo.y = tf32_trunc(x[j + 1] - hi.y);
-                    hi.z = tf32_trunc(x[j + 2]); lo.z = tf32_trunc(x[j + 2] - hi.z);
-                    hi.w = tf32_trunc(x[j + 3]); lo.w = tf32_trunc(x[j + 3] - hi.w);
+                    hi.x = tf32_round(x[j]); lo.x = tf32_round(x[j] - hi.x);
+                    hi.y = tf32_round(x[j + 1]); lo.y = tf32_round(x[j + 1] - hi.y);
+                    hi.z = tf32_round(x[j + 2]); lo.z = tf32_round(x[j + 2] - hi.z);
+                    hi.w = tf32_round(x[j + 3]); lo.w = tf32_round(x[j + 3] - hi.w);
                     const uint32_t o = core_off(r, kh + j, TC_KC);
                     *reinterpret_cast<float4 *>(Ahi + o) = hi;
                     *reinterpret_cast<float4 *>(Alo + o) = lo;
@@ -366,8 +366,8 @@ __global__ void tc_split_kernel(const double2 *__restrict__ T, int p, int KC, in
             v = po == 0 ? (pi == 0 ? t.x : -t.y) : (pi == 0 ? t.y : t.x);
             if (dinv) v *= dinv[(int)sqrtf((float)(h * CH + nr / 2) + 0.5f)] * dinv[(int)sqrtf((float)(k / 2) + 0.5f)];
         }
-        float hi = tf32_trunc((float)v);
-        float lo = tf32_trunc((float)(v - (double)hi));
+        float hi = tf32_round((float)v);
+        float lo = tf32_round((float)(v - (double)hi));
         size_t base = ((((size_t)d * nhalf + h) * nch + c) * 2 + part) * (size_t)Nmma * KC;
         B[base + core_off(nr, kcol, KC) / 4] = part ? lo : hi;
     }

@@ -19,8 +19,9 @@
 // on the MMA's M side, 128 rows = 64 columns x 2 parts (re, im in the rotation stages, the +m and
 // -m orders in the coaxial stage), and one operator block (one degree, or one order) on the N
 // side: D[row][o] = sum_k A[row][k] B[o][k], K and N the block's size padded to 8 and 16, so the
-// block-diagonal structure costs no MMA work.  Operands are split into TF32 hi and lo halves
-// and multiplied as hi*hi + hi*lo + lo*hi with FP32 accumulation in TMEM (FP32-level accuracy).
+// block-diagonal structure costs no MMA work.  Operands are split into TF32 hi and lo halves,
+// each rounded to nearest, and multiplied as hi*hi + hi*lo + lo*hi with FP32 accumulation in
+// TMEM (FP32-level accuracy).
 //
 // A persistent kernel per stage (one CTA per SM, 14 warps) runs over (tile, block range) items:
 //   warp 0     issues the MMAs (one thread) of each block into one of four TMEM accumulators
@@ -86,10 +87,10 @@ struct T3Args {
 __device__ __forceinline__ void t3_store(unsigned char *Ahi, unsigned char *Alo, int row, int k, const float (&v)[4])
 {
     float4 hi, lo;
-    hi.x = tf32_trunc(v[0]); lo.x = tf32_trunc(v[0] - hi.x);
-    hi.y = tf32_trunc(v[1]); lo.y = tf32_trunc(v[1] - hi.y);
-    hi.z = tf32_trunc(v[2]); lo.z = tf32_trunc(v[2] - hi.z);
-    hi.w = tf32_trunc(v[3]); lo.w = tf32_trunc(v[3] - hi.w);
+    hi.x = tf32_round(v[0]); lo.x = tf32_round(v[0] - hi.x);
+    hi.y = tf32_round(v[1]); lo.y = tf32_round(v[1] - hi.y);
+    hi.z = tf32_round(v[2]); lo.z = tf32_round(v[2] - hi.z);
+    hi.w = tf32_round(v[3]); lo.w = tf32_round(v[3] - hi.w);
     const uint32_t o = core_off(row, k, T3_KC);
     *reinterpret_cast<float4 *>(Ahi + o) = hi;
     *reinterpret_cast<float4 *>(Alo + o) = lo;
@@ -374,15 +375,15 @@ static long long t3_layout(std::vector<int4> &blk)
 static inline void t3_put(float *tab, long long base, int Npad, int o, int k, double v)
 {
     const int c = k / T3_KC, kc = k % T3_KC;
+    // TF32 halves rounded to nearest, as the device splits its data
     float hi = (float)v;
-    // TF32 halves (truncation, as the device splits its data)
     uint32_t u;
     memcpy(&u, &hi, 4);
-    u &= 0xffffe000u;
+    u = tf32_round_bits(u);
     memcpy(&hi, &u, 4);
     float lo = (float)((double)(float)v - (double)hi);
     memcpy(&u, &lo, 4);
-    u &= 0xffffe000u;
+    u = tf32_round_bits(u);
     memcpy(&lo, &u, 4);
     const long long t = base + (long long)c * 2 * Npad * T3_KC;
     tab[t + core_off(o, kc, T3_KC) / 4] = hi;

@@ -142,5 +142,10 @@ def test_autograd_function_gradcheck(fm):
         return FarFieldObjective.apply(V, beta)
 
     t = torch.zeros(4, dtype=torch.float64, requires_grad=True)
-    # central differences at eps against the backward; J ~ 1e-2 here
-    assert torch.autograd.gradcheck(f, (t,), eps=1e-6, atol=1e-8, rtol=1e-4, check_undefined_grad=False)
+    f(t).backward()
+    scale = float(t.grad.abs().max())
+    assert scale > 0
+    # central differences at eps against the backward, within 1e-4 of the largest derivative (the
+    # bound of the other gradient tests: the derivative holds the octree's box centres fixed while
+    # the differences move them with the bounding cube)
+    assert torch.autograd.gradcheck(f, (t,), eps=1e-6, atol=1e-4 * scale, rtol=0.0, check_undefined_grad=False)
