@@ -37,12 +37,14 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 __device__ __forceinline__ bool mbar_wait_limit(uint32_t bar, uint32_t parity, long long limit)
 {
     long long t0 = clock64();
-    while (true) {
+    for (int tries = 0;; tries++) {
         uint32_t done;
         asm volatile("{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\tselp.u32 %0, 1, 0, q;\n\t}"
                      : "=r"(done) : "r"(bar), "r"(parity) : "memory");
         if (done) return true;
         if (clock64() - t0 > limit) return false;
+        // a waiting warp leaves its issue slots to the warps that work
+        if (tries >= 4) __nanosleep(64);
     }
 }
 

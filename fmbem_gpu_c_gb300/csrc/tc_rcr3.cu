@@ -50,39 +50,51 @@ namespace fmm {
 constexpr int T3_M = 128;
 constexpr int T3_COLS = 64;
 constexpr int T3_KC = 16;
-constexpr int T3_STAGES = 4;
-constexpr int T3_SLOTS = 4;
+constexpr int T3_SA = 4;            // data stages (A hi / lo)
+constexpr int T3_SBMAX = 8;         // operator stages (B hi / lo) at most
+constexpr int T3_SLOTS = 4;         // TMEM accumulators of 128 columns
 constexpr int T3_NMAX = 128;
 constexpr int T3_THREADS = 448;
 constexpr int T3_GWARPS = 8;
 constexpr int T3_EPI0 = 2 + T3_GWARPS;
 constexpr uint32_t T3_TA = T3_M * T3_KC * 4;
-constexpr uint32_t T3_TBMAX = T3_NMAX * T3_KC * 4;
-constexpr uint32_t T3_STAGE = 2 * T3_TA + 2 * T3_TBMAX;
-constexpr size_t T3_SMEM = T3_STAGES * (size_t)T3_STAGE + (2 * T3_STAGES + 2 * T3_SLOTS) * 8 + 16;
+constexpr size_t T3_SMEM_MAX = 227 * 1024 - 2048;  // dynamic shared memory beside the static tables
+constexpr size_t T3_BAR_BYTES = (2 * T3_SA + 2 * T3_SBMAX + 2 * T3_SLOTS) * 8 + 16;
 constexpr size_t T3_SCRATCH_BYTES = (size_t)32 << 20; // per scratch buffer (W, Z) of one pass
 constexpr int T3_MAXP = 64;
 
 enum { T3_R1 = 0, T3_C = 1, T3_R2 = 2 };
 
 struct T3Args {
-    int p, pinr, nq, nrhs, n_items, t0;
+    int p, pinr, nq, nrhs, n_items, t0, nblk;
+    int sb, s2;              // operator stages; staging row stride (float2) of the epilogue, 0 if none
+    uint32_t bstage;         // bytes of one operator stage
     const int4 *items;       // (class, first column, count, b0 | b1 << 16)
-    const int4 *blk;         // per block: (operator offset in floats, K, Npad, valid N)
+    const int4 *blk;         // per block: (operator offset in floats, K, Npad, valid N); nblk of them
     const int *list;         // stage position -> translation of the chunk (chunk-local)
-    const int *g_src, *g_dst, *t_dir;
+    const int *g_src, *g_dst, *t_dir;  // g_src set for R1 only
     const float2 *PH;
     int phstride, phoff;
     const float *ops;
     long long ops_stride;    // floats per class
     const float2 *src;       // R1: source expansions [box][rhs][src_stride]
     int src_stride;
-    const float2 *in;        // C: W, R2: Z, [column][p^2]
+    const float2 *in;        // C: W, R2: Z, [column][p^2] in the paired order
     float2 *out;             // R1: W, C: Z
     float2 *dst;             // R2: destination expansions [box][rhs][dst_stride]
     int dst_stride, atomic;
     int *err;
 };
+
+// Scratch order within degree n: m = 0 first, then the pairs (m, -m) for m = 1..n, so that the
+// coaxial stage, which reads and writes +m and -m together, touches one sector for both.
+__host__ __device__ __forceinline__ int t3_pm(int m) { return m == 0 ? 0 : (m > 0 ? 2 * m - 1 : -2 * m); }
+
+// dynamic shared memory of a launch: data stages, operator stages, epilogue staging, barriers
+static inline size_t t3_smem(uint32_t bstage, int sb, int s2)
+{
+    return (size_t)T3_SA * 2 * T3_TA + (size_t)sb * bstage + (size_t)4 * 16 * s2 * 8 + T3_BAR_BYTES;
+}
 
 __device__ __forceinline__ void t3_store(unsigned char *Ahi, unsigned char *Alo, int row, int k, const float (&v)[4])
 {
@@ -96,24 +108,147 @@ __device__ __forceinline__ void t3_store(unsigned char *Ahi, unsigned char *Alo,
     *reinterpret_cast<float4 *>(Alo + o) = lo;
 }
 
+// Position (item, block, K chunk) in a CTA's sequence of chunks (q >= n_items past the end),
+// with what the gathering thread of column ci needs of the item, resolved once per item: the
+// scratch column (-1 where the tile has no column ci), and for R1 the source box and the
+// direction's phases.
+struct T3Cursor {
+    int q, b, c, b1, nch;
+    int col, box;
+    const float2 *ph;
+};
+
+__device__ __forceinline__ void t3_cur_item(T3Cursor &u, const T3Args &a, const int4 *blk, int ci)
+{
+    u.c = 0;
+    u.col = -1;
+    if (u.q < a.n_items) {
+        const int4 it = a.items[u.q];
+        u.b = it.w & 0xffff;
+        u.b1 = it.w >> 16;
+        u.nch = (blk[u.b].y + T3_KC - 1) / T3_KC;
+        if (ci < it.z) {
+            const int pos = it.y + ci, tl = a.list[pos / a.nrhs], rr = pos - (pos / a.nrhs) * a.nrhs;
+            u.col = tl * a.nrhs + rr;
+            if (a.g_src) {
+                const int t = a.t0 + tl;
+                u.box = a.g_src[t] * a.nrhs + rr;
+                u.ph = a.PH + (size_t)a.t_dir[t] * a.phstride + a.phoff;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void t3_cur_next(T3Cursor &u, const T3Args &a, const int4 *blk, int ci)
+{
+    if (u.q >= a.n_items) return;
+    if (++u.c < u.nch) return;
+    u.c = 0;
+    if (++u.b < u.b1) {
+        u.nch = (blk[u.b].y + T3_KC - 1) / T3_KC;
+        return;
+    }
+    u.q += gridDim.x;
+    t3_cur_item(u, a, blk, ci);
+}
+
+// one thread's loads for one chunk (valid = 0 past the end of the CTA's sequence): R1 source
+// values and their phases, R2 the Z values, C the W values of order +m (x[0..1]) and -m (x[2..3])
+struct T3Raw {
+    float2 x[4], e[4];
+    int valid;
+};
+
+template <int ST>
+__device__ __forceinline__ void t3_load(const T3Args &a, const T3Cursor &u, const int4 *blk, int qk, T3Raw &r)
+{
+#pragma unroll
+    for (int j = 0; j < 4; j++) r.x[j] = r.e[j] = make_float2(0.f, 0.f);
+    r.valid = u.q < a.n_items;
+    if (!r.valid || u.col < 0) return;
+    const int P2 = a.p * a.p, K = blk[u.b].y, k0 = u.c * T3_KC + 4 * qk;
+    if (ST == T3_C) {
+        // order m = b; K entries (n, part) for n = m + k/2 < pinr
+        const int m = u.b;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (k0 + 2 * h < K) {
+                const int n = m + k0 / 2 + h;
+                const float2 *row = a.in + (size_t)u.col * P2 + n * n;
+                r.x[h] = __ldg(row + t3_pm(m));
+                if (m > 0) r.x[2 + h] = __ldg(row + t3_pm(-m));
+            }
+        }
+    } else {
+        // degree n = b; K entries m + n for |m| <= n, |m| < pinr
+        const int n = u.b;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int k = k0 + j, m = k - n;
+            if (k < K && m < a.pinr && -m < a.pinr) {
+                if (ST == T3_R1) {
+                    r.x[j] = __ldg(a.src + (size_t)u.box * a.src_stride + n * n + k);
+                    r.e[j] = __ldg(u.ph + m);
+                } else {
+                    r.x[j] = __ldg(a.in + (size_t)u.col * P2 + n * n + t3_pm(m));
+                }
+            }
+        }
+    }
+}
+
+// the two data rows of a thread's chunk from its loads
+template <int ST>
+__device__ __forceinline__ void t3_values(const T3Raw &r, float (&v0)[4], float (&v1)[4])
+{
+    if (ST == T3_C) {
+        v0[0] = r.x[0].x; v0[1] = r.x[0].y; v0[2] = r.x[1].x; v0[3] = r.x[1].y;
+        v1[0] = r.x[2].x; v1[1] = r.x[2].y; v1[2] = r.x[3].x; v1[3] = r.x[3].y;
+    } else if (ST == T3_R1) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            v0[j] = r.x[j].x * r.e[j].x - r.x[j].y * r.e[j].y;
+            v1[j] = r.x[j].x * r.e[j].y + r.x[j].y * r.e[j].x;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            v0[j] = r.x[j].x;
+            v1[j] = r.x[j].y;
+        }
+    }
+}
+
 template <int ST>
 __global__ void __launch_bounds__(T3_THREADS, 1) rcr3_kernel(T3Args a)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + T3_STAGES * (size_t)T3_STAGE);
-    uint64_t *full = bars, *empty = bars + T3_STAGES, *accf = bars + 2 * T3_STAGES, *acce = accf + T3_SLOTS;
+    unsigned char *aring = smem;
+    unsigned char *bring = aring + (size_t)T3_SA * 2 * T3_TA;
+    float2 *stg_all = reinterpret_cast<float2 *>(bring + (size_t)a.sb * a.bstage);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(stg_all + (size_t)4 * 16 * a.s2);
+    uint64_t *fulla = bars, *emptya = fulla + T3_SA, *fullb = emptya + T3_SA, *emptyb = fullb + T3_SBMAX;
+    uint64_t *accf = emptyb + T3_SBMAX, *acce = accf + T3_SLOTS;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(acce + T3_SLOTS);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int P2 = a.p * a.p;
+    const int P2 = a.p * a.p, SB = a.sb;
+    __shared__ int4 s_blk[T3_MAXP];
+    __shared__ int4 s_cinfo[4][16];  // epilogue: per warp, its 16 columns (scratch column, box, direction)
+    for (int b = tid; b < a.nblk; b += blockDim.x) s_blk[b] = a.blk[b];
+    const int4 *blk = s_blk;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(512));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 32) {
-        for (int s = 0; s < T3_STAGES; s++) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)), "r"(T3_GWARPS + 1));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)));
+        for (int s = 0; s < T3_SA; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(fulla + s)), "r"(T3_GWARPS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(emptya + s)));
+        }
+        for (int s = 0; s < SB; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(fullb + s)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(emptyb + s)));
         }
         for (int j = 0; j < T3_SLOTS; j++) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(accf + j)));
@@ -135,7 +270,7 @@ __global__ void __launch_bounds__(T3_THREADS, 1) rcr3_kernel(T3Args a)
                 const int4 it = a.items[q];
                 const int b1 = it.w >> 16;
                 for (int b = it.w & 0xffff; b < b1 && ok; b++, i++) {
-                    const int4 bk = a.blk[b];
+                    const int4 bk = blk[b];
                     const int K = bk.y, Npad = bk.z, slot = i % T3_SLOTS;
                     ok = mbar_wait(smem_u32(acce + slot), ((i / T3_SLOTS) & 1) ^ 1);
                     if (!ok) break;
@@ -145,12 +280,13 @@ __global__ void __launch_bounds__(T3_THREADS, 1) rcr3_kernel(T3Args a)
                         (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Npad >> 3) << 17) | ((uint32_t)(T3_M >> 4) << 24);
                     const int nch = (K + T3_KC - 1) / T3_KC;
                     for (int c = 0; c < nch && ok; c++, g++) {
-                        const int s = g % T3_STAGES;
-                        ok = mbar_wait(smem_u32(full + s), (g / T3_STAGES) & 1);
+                        const int sa = g % T3_SA, sbi = g % SB;
+                        ok = mbar_wait(smem_u32(fulla + sa), (g / T3_SA) & 1) &&
+                             mbar_wait(smem_u32(fullb + sbi), (g / SB) & 1);
                         if (!ok) break;
                         asm volatile("tcgen05.fence::after_thread_sync;");
-                        const uint32_t a_hi = smem_u32(smem + (size_t)s * T3_STAGE), a_lo = a_hi + T3_TA;
-                        const uint32_t b_hi = a_hi + 2 * T3_TA, b_lo = b_hi + (uint32_t)Npad * T3_KC * 4;
+                        const uint32_t a_hi = smem_u32(aring + (size_t)sa * 2 * T3_TA), a_lo = a_hi + T3_TA;
+                        const uint32_t b_hi = smem_u32(bring + (size_t)sbi * a.bstage), b_lo = b_hi + (uint32_t)Npad * T3_KC * 4;
                         const int nks = K - c * T3_KC > 8 ? 2 : 1;
                         for (int ks = 0; ks < nks; ks++)
 #pragma unroll
@@ -163,7 +299,10 @@ __global__ void __launch_bounds__(T3_THREADS, 1) rcr3_kernel(T3Args a)
                                              "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
                             }
                         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                         smem_u32(empty + s))
+                                         smem_u32(emptya + sa))
+                                     : "memory");
+                        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                         smem_u32(emptyb + sbi))
                                      : "memory");
                     }
                     if (ok)
@@ -182,14 +321,14 @@ __global__ void __launch_bounds__(T3_THREADS, 1) rcr3_kernel(T3Args a)
                 const int b1 = it.w >> 16;
                 const float *opc = a.ops + (long long)it.x * a.ops_stride;
                 for (int b = it.w & 0xffff; b < b1 && ok; b++) {
-                    const int4 bk = a.blk[b];
+                    const int4 bk = blk[b];
                     const int K = bk.y, Npad = bk.z, nch = (K + T3_KC - 1) / T3_KC;
                     const uint32_t bytes = 2u * (uint32_t)Npad * T3_KC * 4;
                     for (int c = 0; c < nch && ok; c++, g++) {
-                        const int s = g % T3_STAGES;
-                        ok = mbar_wait(smem_u32(empty + s), ((g / T3_STAGES) & 1) ^ 1);
+                        const int s = g % SB;
+                        ok = mbar_wait(smem_u32(emptyb + s), ((g / SB) & 1) ^ 1);
                         if (!ok) break;
-                        const uint32_t bar = smem_u32(full + s), dst = smem_u32(smem + (size_t)s * T3_STAGE + 2 * T3_TA);
+                        const uint32_t bar = smem_u32(fullb + s), dst = smem_u32(bring + (size_t)s * a.bstage);
                         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
                         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
                                      "l"(opc + bk.x + (size_t)c * 2 * Npad * T3_KC), "r"(bytes), "r"(bar)
@@ -200,154 +339,172 @@ __global__ void __launch_bounds__(T3_THREADS, 1) rcr3_kernel(T3Args a)
         }
     } else if (warp < T3_EPI0) {
         // ---------------------------------------------------------------- data gather
-        // thread (column ci, K quarter qk): rows 2 ci and 2 ci + 1, four K entries of every chunk
+        // thread (column ci, K quarter qk): rows 2 ci and 2 ci + 1, four K entries of every chunk.
+        // Four chunks of loads are in flight: a buffer is reloaded right after it is stored.
         const int gt = tid - 64, ci = gt >> 2, qk = gt & 3;
-        int g = 0;
-        for (int q = blockIdx.x; q < a.n_items && ok; q += gridDim.x) {
-            const int4 it = a.items[q];
-            const int b1 = it.w >> 16;
-            const bool valid = ci < it.z;
-            int col = 0, box = 0, dir = 0;
-            if (valid) {
-                const int pos = it.y + ci, tl = a.list[pos / a.nrhs], r = pos - (pos / a.nrhs) * a.nrhs;
-                col = tl * a.nrhs + r;
-                if (ST == T3_R1) {
-                    const int t = a.t0 + tl;
-                    box = a.g_src[t] * a.nrhs + r;
-                    dir = a.t_dir[t];
-                }
-            }
-            const float2 *ph = a.PH + (size_t)dir * a.phstride + a.phoff;
-            for (int b = it.w & 0xffff; b < b1 && ok; b++) {
-                const int K = a.blk[b].y, nch = (K + T3_KC - 1) / T3_KC;
-                for (int c = 0; c < nch && ok; c++, g++) {
-                    const int k0 = c * T3_KC + 4 * qk;
-                    float v0[4], v1[4];
-                    if (ST == T3_C) {
-                        // order m = b; K entries (n, part) for n = m + k/2 < pinr; rows +m, -m
-                        const int m = b;
+        T3Cursor ul;
+        ul.q = blockIdx.x;
+        t3_cur_item(ul, a, blk, ci);
+        T3Raw r[4];
 #pragma unroll
-                        for (int h = 0; h < 2; h++) {
-                            const int n = m + k0 / 2 + h;
-                            float2 xp = make_float2(0.f, 0.f), xm = make_float2(0.f, 0.f);
-                            if (valid && k0 + 2 * h < K) {
-                                const float2 *row = a.in + (size_t)col * P2 + n * n + n;
-                                xp = row[m];
-                                if (m > 0) xm = row[-m];
-                            }
-                            v0[2 * h] = xp.x; v0[2 * h + 1] = xp.y;
-                            v1[2 * h] = xm.x; v1[2 * h + 1] = xm.y;
-                        }
-                    } else {
-                        // degree n = b; K entries m + n for |m| <= n; rows re, im
-                        const int n = b;
+        for (int j = 0; j < 4; j++) {
+            t3_load<ST>(a, ul, blk, qk, r[j]);
+            t3_cur_next(ul, a, blk, ci);
+        }
+        for (int g = 0; ok; g += 4) {
 #pragma unroll
-                        for (int j = 0; j < 4; j++) {
-                            const int k = k0 + j, m = k - n;
-                            float2 x = make_float2(0.f, 0.f);
-                            if (valid && k < K && m < a.pinr && -m < a.pinr) {
-                                if (ST == T3_R1) {
-                                    const float2 s = a.src[(size_t)box * a.src_stride + n * n + k], e = ph[m];
-                                    x = make_float2(s.x * e.x - s.y * e.y, s.x * e.y + s.y * e.x);
-                                } else {
-                                    x = a.in[(size_t)col * P2 + n * n + k];
-                                }
-                            }
-                            v0[j] = x.x;
-                            v1[j] = x.y;
-                        }
-                    }
-                    const int s = g % T3_STAGES;
-                    ok = mbar_wait(smem_u32(empty + s), ((g / T3_STAGES) & 1) ^ 1);
-                    if (!ok) break;
-                    unsigned char *Ahi = smem + (size_t)s * T3_STAGE, *Alo = Ahi + T3_TA;
-                    t3_store(Ahi, Alo, 2 * ci, 4 * qk, v0);
-                    t3_store(Ahi, Alo, 2 * ci + 1, 4 * qk, v1);
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    __syncwarp();
-                    if (lane == 0) mbar_arrive(smem_u32(full + s));
+            for (int j = 0; j < 4; j++) {
+                if (!ok || !r[j].valid) {
+                    ok = false;
+                    break;
                 }
+                float v0[4], v1[4];
+                t3_values<ST>(r[j], v0, v1);
+                const int s = (g + j) % T3_SA;
+                if (!mbar_wait(smem_u32(emptya + s), (((g + j) / T3_SA) & 1) ^ 1)) {
+                    ok = false;
+                    atomicExch(a.err, 1);
+                    break;
+                }
+                unsigned char *Ahi = aring + (size_t)s * 2 * T3_TA, *Alo = Ahi + T3_TA;
+                t3_store(Ahi, Alo, 2 * ci, 4 * qk, v0);
+                t3_store(Ahi, Alo, 2 * ci + 1, 4 * qk, v1);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(fulla + s));
+                t3_load<ST>(a, ul, blk, qk, r[j]);
+                t3_cur_next(ul, a, blk, ci);
             }
         }
+        ok = true; // the end of the sequence is not an error; a failed wait set the flag above
     } else {
         // ---------------------------------------------------------------- epilogue
-        const int wq = warp & 3, row = wq * 32 + lane, ci = row >> 1, part = row & 1;
+        // Warp w reads TMEM lane quarter w & 3: rows of 16 columns, re and im (or +m and -m) in
+        // adjacent lanes.  The rotation stages stage a block's outputs for their 16 columns in
+        // shared memory and write them out with consecutive lanes on consecutive entries of a
+        // column (several columns per pass when a column has fewer than 32 entries); the coaxial
+        // stage writes its +m and -m rows to adjacent scratch entries directly.
+        const int wq = warp & 3, row = wq * 32 + lane, ci = row >> 1, part = row & 1, cl = lane >> 1;
+        const int ew = warp - T3_EPI0;
+        float2 *stg = stg_all + (size_t)ew * 16 * a.s2;
+        float *stgf = reinterpret_cast<float *>(stg);
+        int4 *cinfo = s_cinfo[ew];
         int i = 0;
         for (int q = blockIdx.x; q < a.n_items && ok; q += gridDim.x) {
             const int4 it = a.items[q];
             const int b1 = it.w >> 16;
             const bool valid = ci < it.z;
-            int col = 0, dbox = 0, dir = 0;
+            int col = -1;
+            const float2 *ph = a.PH + a.phoff;
             if (valid) {
                 const int pos = it.y + ci, tl = a.list[pos / a.nrhs], r = pos - (pos / a.nrhs) * a.nrhs;
                 col = tl * a.nrhs + r;
-                if (ST == T3_R2) {
-                    const int t = a.t0 + tl;
-                    dbox = a.g_dst[t] * a.nrhs + r;
-                    dir = a.t_dir[t];
+                if (ST == T3_R2) ph = a.PH + (size_t)a.t_dir[a.t0 + tl] * a.phstride + a.phoff;
+                if (ST != T3_C && part == 0) {
+                    int dbox = 0, dir = 0;
+                    if (ST == T3_R2) {
+                        const int t = a.t0 + tl;
+                        dbox = a.g_dst[t] * a.nrhs + r;
+                        dir = a.t_dir[t];
+                    }
+                    cinfo[cl] = make_int4(col, dbox, dir, 0);
                 }
+            } else if (ST != T3_C && part == 0) {
+                cinfo[cl] = make_int4(-1, 0, 0, 0);
             }
-            const float2 *ph = a.PH + (size_t)dir * a.phstride + a.phoff;
+            __syncwarp();
             for (int b = it.w & 0xffff; b < b1 && ok; b++, i++) {
-                const int4 bk = a.blk[b];
+                const int4 bk = blk[b];
                 const int Npad = bk.z, nout = bk.w, slot = i % T3_SLOTS;
                 ok = mbar_wait(smem_u32(accf + slot), (i / T3_SLOTS) & 1);
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                for (int j0 = 0; j0 < Npad; j0 += 16) {
-                    uint32_t v[16];
+                for (int j0 = 0; j0 < Npad; j0 += 32) {
+                    uint32_t v[32];
                     const uint32_t ta = tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(slot * T3_NMAX + j0);
-                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
                                  : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
                                    "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-                                   "=r"(v[14]), "=r"(v[15])
+                                   "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]),
+                                   "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
+                                   "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                                  : "r"(ta));
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                     if (ST == T3_C) {
                         // row (column ci, sign part): Z_{+-m}(n') = (v[2j'], v[2j'+1]), n' = m + j'
                         const int m = b;
                         if (valid && !(part && m == 0)) {
+                            float2 *zc = a.out + (size_t)col * P2 + t3_pm(part ? -m : m);
 #pragma unroll
-                            for (int j = 0; j < 16; j += 2) {
+                            for (int j = 0; j < 32; j += 2) {
                                 const int jj = j0 + j;
                                 if (jj < nout) {
                                     const int n = m + jj / 2;
-                                    a.out[(size_t)col * P2 + n * n + n + (part ? -m : m)] =
-                                        make_float2(__uint_as_float(v[j]), __uint_as_float(v[j + 1]));
+                                    zc[n * n] = make_float2(__uint_as_float(v[j]), __uint_as_float(v[j + 1]));
                                 }
                             }
                         }
-                    } else {
-                        // rows re (part 0) and im (part 1) of one column sit in adjacent lanes; the
-                        // even lane writes the even outputs, the odd lane the odd ones
+                    } else if (ST == T3_R1) {
+                        // output j of degree n (m' = j - n), staged at its paired position
                         const int n = b;
 #pragma unroll
-                        for (int j = 0; j < 16; j++) {
+                        for (int j = 0; j < 32; j++) {
+                            const int jj = j0 + j;
+                            if (jj < nout) stgf[2 * (cl * a.s2 + t3_pm(jj - n)) + part] = __uint_as_float(v[j]);
+                        }
+                    } else {
+                        // y e^{-i m' phi}: re and im from the lane pair, the column's phases loaded
+                        // together for the piece; staged in natural order
+                        const int n = b;
+                        float2 e[32];
+#pragma unroll
+                        for (int j = 0; j < 32; j++) {
+                            const int m = min(j0 + j, nout - 1) - n;
+                            e[j] = __ldg(ph + m);
+                        }
+#pragma unroll
+                        for (int j = 0; j < 32; j++) {
                             const float mine = __uint_as_float(v[j]);
                             const float other = __shfl_xor_sync(0xffffffffu, mine, 1);
-                            const int jj = j0 + j;
-                            if (!valid || jj >= nout || (jj & 1) != part) continue;
-                            const float2 y = part ? make_float2(other, mine) : make_float2(mine, other);
-                            if (ST == T3_R1) {
-                                a.out[(size_t)col * P2 + n * n + jj] = y;
-                            } else {
-                                const float2 e = ph[jj - n];
-                                const float2 w = make_float2(e.x * y.x + e.y * y.y, e.x * y.y - e.y * y.x);
-                                float2 *d = a.dst + (size_t)dbox * a.dst_stride + n * n + jj;
-                                if (a.atomic) {
-                                    atomicAdd(d, w);
-                                } else {
-                                    const float2 o = *d;
-                                    *d = make_float2(o.x + w.x, o.y + w.y);
-                                }
-                            }
+                            const float yr = part ? other : mine, yi = part ? mine : other;
+                            const float w = part ? e[j].x * yi - e[j].y * yr : e[j].x * yr + e[j].y * yi;
+                            if (j0 + j < nout) stgf[2 * (cl * a.s2 + j0 + j) + part] = w;
                         }
                     }
                 }
                 asm volatile("tcgen05.fence::before_thread_sync;");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(acce + slot));
+                if (ST != T3_C) {
+                    const int n = b;
+                    // columns per pass: 32 / nout when a column's run is shorter than a warp
+                    const int cpp = nout < 32 ? 32 / nout : 1, coff = nout < 32 ? lane / nout : 0;
+                    const int e0 = nout < 32 ? lane - coff * nout : lane;
+                    for (int c0 = 0; c0 < 16; c0 += cpp) {
+                        const int c = c0 + coff;
+                        if (c >= 16 || coff >= cpp) continue;
+                        const int4 inf = cinfo[c];
+                        if (inf.x < 0) continue;
+                        for (int e = e0; e < nout; e += 32) {
+                            const float2 y = stg[c * a.s2 + e];
+                            if (ST == T3_R1) {
+                                a.out[(size_t)inf.x * P2 + n * n + e] = y;
+                            } else {
+                                float2 *d = a.dst + (size_t)inf.y * a.dst_stride + n * n + e;
+                                if (a.atomic) {
+                                    atomicAdd(d, y);
+                                } else {
+                                    const float2 o = *d;
+                                    *d = make_float2(o.x + y.x, o.y + y.y);
+                                }
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
             }
+            __syncwarp();
         }
     }
     if (!ok) atomicExch(a.err, 1);
@@ -611,14 +768,31 @@ static int t3_prepare(Plan *P, Tc3 &t, int nrhs)
     return FMM_OK;
 }
 
+// Ring and staging sizes of a launch from its blocks: the rotation stages stage each block's
+// outputs (up to 2p-1 complex per column, row stride 1 mod 16 float2 so that the 16 columns of a
+// warp hit different banks); the operator stages take what is left, up to eight.
 template <int ST>
-static int t3_launch(T3Args &a, int nsm, cudaStream_t st)
+static int t3_launch(T3Args &a, const std::vector<int4> &hblk, int nsm, cudaStream_t st)
 {
     static size_t attr = 0;
-    int e = raise_smem_limit((const void *)rcr3_kernel<ST>, T3_SMEM, &attr);
+    int npmax = 16, nomax = 1;
+    for (const int4 &b : hblk) {
+        npmax = std::max(npmax, b.z);
+        nomax = std::max(nomax, b.w);
+    }
+    a.bstage = 2u * (uint32_t)npmax * T3_KC * 4;
+    a.s2 = ST == T3_C ? 0 : (nomax + 15) / 16 * 16 + 1;
+    a.sb = T3_SBMAX;
+    while (a.sb > 2 && t3_smem(a.bstage, a.sb, a.s2) > T3_SMEM_MAX) a.sb--;
+    const size_t sm = t3_smem(a.bstage, a.sb, a.s2);
+    if (sm > T3_SMEM_MAX) {
+        fmm_set_error("three-stage tensor-core pass: %zu bytes of shared memory needed", sm);
+        return FMM_ERR_ARG;
+    }
+    int e = raise_smem_limit((const void *)rcr3_kernel<ST>, T3_SMEM_MAX, &attr);
     if (e) return e;
     if (a.n_items <= 0) return FMM_OK;
-    rcr3_kernel<ST><<<std::min(a.n_items, nsm), T3_THREADS, T3_SMEM, st>>>(a);
+    rcr3_kernel<ST><<<std::min(a.n_items, nsm), T3_THREADS, sm, st>>>(a);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
@@ -644,7 +818,6 @@ int launch_tc3_pass(Plan *P, int l, int which, int nrhs, cudaStream_t st)
     a.pinr = t.pinr;
     a.nq = t.nq;
     a.nrhs = nrhs;
-    a.g_src = Lst->src;
     a.g_dst = Lst->dst;
     a.t_dir = t.t_dir;
     a.PH = ps.PH;
@@ -664,31 +837,37 @@ int launch_tc3_pass(Plan *P, int l, int which, int nrhs, cudaStream_t st)
         a.n_items = t.it_beg[3 * (k + 1)] - t.it_beg[3 * k];
         a.list = t.listR + a.t0;
         a.blk = t.blkR;
+        a.nblk = (int)t.hblkR.size();
         a.ops = t.opsR;
         a.ops_stride = t.strideR;
+        a.g_src = Lst->src;
         a.in = nullptr;
         a.out = t.W;
-        if ((e = t3_launch<T3_R1>(a, nsm, st))) return e;
+        if ((e = t3_launch<T3_R1>(a, t.hblkR, nsm, st))) return e;
         // C: W -> Z
         a.items = t.itC + t.it_beg[3 * k + 1];
         a.n_items = t.it_beg[3 * (k + 1) + 1] - t.it_beg[3 * k + 1];
         a.list = t.listC + a.t0;
         a.blk = t.blkC;
+        a.nblk = (int)t.hblkC.size();
         a.ops = t.opsC;
         a.ops_stride = t.strideC;
+        a.g_src = nullptr;
         a.in = t.W;
         a.out = t.Z;
-        if ((e = t3_launch<T3_C>(a, nsm, st))) return e;
+        if ((e = t3_launch<T3_C>(a, t.hblkC, nsm, st))) return e;
         // R2: Z -> destinations
         a.items = t.itR2 + t.it_beg[3 * k + 2];
         a.n_items = t.it_beg[3 * (k + 1) + 2] - t.it_beg[3 * k + 2];
         a.list = t.listR + a.t0;
         a.blk = t.blkR;
+        a.nblk = (int)t.hblkR.size();
         a.ops = t.opsR;
         a.ops_stride = t.strideR;
+        a.g_src = nullptr;
         a.in = t.Z;
         a.out = nullptr;
-        if ((e = t3_launch<T3_R2>(a, nsm, st))) return e;
+        if ((e = t3_launch<T3_R2>(a, t.hblkR, nsm, st))) return e;
     }
     return FMM_OK;
 }
