@@ -570,30 +570,33 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
     return FMM_OK;
 }
 
-// Dense M2L operators of level l for the tensor-core pass: T[d][i][j] (p^2 x p^2, FP64), the
-// RCR translation of direction d applied to the unit multipole e_j.  One CTA per (direction,
-// column).
-__global__ void dense_m2l_kernel(int p, int pmax, const double *__restrict__ Hsr, const double2 *__restrict__ PHsr,
+// Dense M2L operators of level l for the tensor-core pass: T[c][i][j] (p^2 x p^2, FP64), the
+// RCR translation of direction dirs[c] with its azimuthal phases left out (rotation by the
+// polar angle, coaxial translation, rotation back) applied to the unit multipole e_j; the
+// translation of any direction d with the same polar angle and distance is then
+// diag(e^{-i m' phi_d}) T diag(e^{i m phi_d}).  One CTA per (operator, column).
+__global__ void dense_m2l_kernel(int p, int pmax, const int *__restrict__ dirs, const double *__restrict__ Hsr,
                                  const double2 *__restrict__ Csr, double2 *__restrict__ T)
 {
     extern __shared__ unsigned char smraw[];
-    const int P2 = p * p, d = blockIdx.x, j = blockIdx.y, rs = rot_size(pmax), w = 2 * pmax - 1;
-    double2 *sE = (double2 *)smraw, *sX = sE + P2, *sW1 = sX + P2, *sW2 = sW1 + P2, *sY = sW2 + P2;
+    const int P2 = p * p, c = blockIdx.x, d = dirs[c], j = blockIdx.y, rs = rot_size(pmax), w = 2 * pmax - 1;
+    double2 *sE = (double2 *)smraw, *sX = sE + P2, *sW1 = sX + P2, *sW2 = sW1 + P2, *sY = sW2 + P2, *sOne = sY + P2;
     for (int i = threadIdx.x; i < P2; i += blockDim.x) {
         sE[i] = make_double2(i == j ? 1.0 : 0.0, 0.0);
         sY[i] = make_double2(0.0, 0.0);
     }
+    for (int i = threadIdx.x; i < w; i += blockDim.x) sOne[i] = make_double2(1.0, 0.0);
     __syncthreads();
-    rcr_block<double>(p, pmax, Hsr + (size_t)d * rs, PHsr + (size_t)d * w, Csr + (size_t)c_dir_dist[d] * coax_size(p), sE,
-                      p, sX, sW1, sW2, sY, p);
-    for (int i = threadIdx.x; i < P2; i += blockDim.x) T[((size_t)d * P2 + i) * P2 + j] = sY[i];
+    rcr_block<double>(p, pmax, Hsr + (size_t)d * rs, sOne, Csr + (size_t)c_dir_dist[d] * coax_size(p), sE, p, sX, sW1,
+                      sW2, sY, p);
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) T[((size_t)c * P2 + i) * P2 + j] = sY[i];
 }
 
-int gen_dense_m2l(Plan *P, int l, double2 *T)
+int gen_dense_m2l(Plan *P, int l, const int *dirs, int ndirs, double2 *T)
 {
     const int p = P->lev[l].p;
-    size_t sm = (size_t)5 * p * p * sizeof(double2);
-    dense_m2l_kernel<<<dim3(NDIR, p * p), 128, sm, P->stream>>>(p, P->pmax, P->Hsr64, P->PHsr64, P->lev[l].Csr64, T);
+    size_t sm = ((size_t)5 * p * p + 2 * P->pmax) * sizeof(double2);
+    dense_m2l_kernel<<<dim3(ndirs, p * p), 128, sm, P->stream>>>(p, P->pmax, dirs, P->Hsr64, P->lev[l].Csr64, T);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

@@ -95,7 +95,7 @@ static void free_plan(Plan *P)
             F(t.opsR); F(t.opsC); F(t.blkR); F(t.blkC); F(t.t_dir); F(t.itR1); F(t.itC); F(t.itR2);
             F(t.listR); F(t.listC); F(t.W); F(t.Z);
         }
-        F(L.tc.B); F(L.tc.items);
+        F(L.tc.B); F(L.tc.items); F(L.tc.src); F(L.tc.dst); F(L.tc.dir);
     }
     F(P->tc_err); F(P->m2l_part64);
     F(P->Hsr64); F(P->PHsr64); F(P->Hsr32); F(P->PHsr32);

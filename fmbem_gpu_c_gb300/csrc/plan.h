@@ -49,16 +49,21 @@ struct RcrList {
     Tc3 t3;                       // three-stage tensor-core form (used where t3.on)
 };
 
-// M2L of one level on the tensor cores (tc_m2l.cu): the level's 316 translation operators
-// stored densely, real-embedded and split into TF32 hi/lo parts in the layout the MMA reads.
+// M2L of one level on the tensor cores (tc_m2l.cu): one dense operator per class of the 316
+// directions with equal (dz, dx^2 + dy^2) -- equal polar angle and distance, so the class's
+// directions differ only by their azimuthal phases, which the kernel applies to each row --
+// real-embedded and split into TF32 hi/lo parts in the layout the MMA reads.
 struct TcM2L {
     int on = 0;                   // this level's mixed M2L runs on the tensor cores
     int KC = 40, nch = 0, nhalf = 1, CH = 0, Nmma = 0;
-    int res = 0;                  // the whole operator of a direction stays in shared memory (p <= 8)
-    float *B = nullptr;           // [dir][half][chunk][hi, lo][Nmma x KC core-matrix tile]
+    int res = 0;                  // the whole operator of a class stays in shared memory (p <= 8)
+    int ncls = 0;                 // operator classes
+    std::vector<int> cls_of_dir;  // M2L direction -> class
+    float *B = nullptr;           // [class][half][chunk][hi, lo][Nmma x KC core-matrix tile]
     size_t B_bytes = 0;
-    int4 *items = nullptr;        // (direction, first column, count, 0), 128 columns each
+    int4 *items = nullptr;        // (class, first column, count, 0), 128 columns each
     size_t items_cap = 0;
+    int *src = nullptr, *dst = nullptr, *dir = nullptr;  // the level's translations in class order
     int n_items = 0, items_nrhs = 0;
 };
 
@@ -208,7 +213,10 @@ RcrList *pass32_desc(Plan *P, int l, int which, int nrhs, RcrPass &ps);
 void launch_axpby(double a, const double2 *x, double b, double2 *y, size_t n, cudaStream_t st);
 
 // tc_m2l.cu
-int gen_dense_m2l(Plan *P, int l, double2 *T);   // passes.cu
+int gen_dense_m2l(Plan *P, int l, const int *dirs, int ndirs, double2 *T);   // passes.cu
+// Classes of a pass's keys with one rotation: M2L directions of equal (dz, dx^2 + dy^2), M2M /
+// L2L octants of equal z bit.  cls[key] = class, rep[class] = its first key.  (tc_rcr3.cu)
+void direction_classes(const Plan *P, int which, int nkeys, std::vector<int> &cls, std::vector<int> &rep);
 int tune_tc_m2l(Plan *P);
 int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st);
 int check_tc_error(Plan *P);

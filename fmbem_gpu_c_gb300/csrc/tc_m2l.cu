@@ -1,14 +1,17 @@
 // M2L of the mixed path on the 5th-generation tensor cores (tcgen05.mma, kind::tf32) for the
-// levels whose translation operators are small enough to store densely (p <= 16, the levels
+// levels whose translation operators are small enough to store densely (p <= 20, the levels
 // that carry most translations).
 //
-// The translations of one direction share one operator T_d (p^2 x p^2 complex; the RCR
-// product of translation.cu:1864-1961 formed once at plan time).  With the columns of a tile
-// being 128 translations of that direction (times right-hand sides), the pass is the real GEMM
-//     D[t][o] = sum_k A[t][k] B[o][k],   A[t] = source expansion of translation t,
-//                                         B    = T_d embedded as a real 2p^2 x 2p^2 matrix,
-// k and o running over interleaved (re, im) parts, so A is the expansion as it lies in memory.
-// Split TF32 (3 products hi*hi + hi*lo + lo*hi of 11-bit halves) gives FP32-level accuracy.
+// The translation of direction d is T_d = diag(e^{-i m' phi_d}) S_c diag(e^{i m phi_d}) (the RCR
+// product of translation.cu:1864-1961 with its azimuthal phases taken out), where S_c (p^2 x p^2
+// complex, formed once at plan time) depends only on the polar angle and the distance of d:
+// the 316 directions fall into about 60 classes c of equal (dz, dx^2 + dy^2).  With the rows of
+// a tile being 128 translations of one class (times right-hand sides), the pass is the real GEMM
+//     D[t][o] = sum_k A[t][k] B[o][k],   A[t] = source expansion of translation t times e^{i m phi},
+//                                         B    = S_c embedded as a real 2p^2 x 2p^2 matrix,
+// k and o running over interleaved (re, im) parts, and the epilogue multiplies row t's outputs
+// by e^{-i m' phi} of its own direction.  Split TF32 (3 products hi*hi + hi*lo + lo*hi of
+// rounded 11-bit halves) gives FP32-level accuracy.
 //
 // A persistent, warp-specialised kernel (one CTA per SM, 14 warps) runs over the tiles
 // (128 translations x one output half):
@@ -17,15 +20,16 @@
 //              accumulator's "full" barrier;
 //   warp 1     copies the operator's K chunks (hi and lo tiles, contiguous) with cp.async.bulk;
 //   warps 2-9  gather the source expansions, two threads per row (translation), each half of
-//              every 16-wide K chunk, split them into TF32 hi / lo and store them in the
-//              no-swizzle K-major core-matrix layout;
-//   warps 10-13 read a finished accumulator (tcgen05.ld, one TMEM lane quarter per warp), stage
-//              32 columns at a time in shared memory and add them into the destination local
-//              expansions with coalesced FP32 atomics, overlapping the next tile's MMAs.
+//              every 16-wide K chunk, apply the row's phases, split them into TF32 hi / lo and
+//              store them in the no-swizzle K-major core-matrix layout;
+//   warps 10-13 read a finished accumulator (tcgen05.ld, one TMEM lane quarter per warp), apply
+//              each row's phases, stage 32 columns at a time in shared memory and add them into
+//              the destination local expansions with coalesced FP32 atomics, overlapping the
+//              next tile's MMAs.
 // Four shared-memory stages of KC = 16; every wait has a time limit, after which the thread sets
 // the plan's error flag and stops.  Where one output half's whole operator fits beside the A
 // stages (p <= 8), it stays resident instead: each CTA takes a contiguous range of tiles, warp 1
-// copies a direction's operator once per run of its tiles (operator-full barrier), and the MMA
+// copies a class's operator once per run of its tiles (operator-full barrier), and the MMA
 // warp releases it after the run's last tile (a commit to the operator-empty barrier).
 #include "plan.h"
 #include "tc_common.cuh"
@@ -39,16 +43,20 @@ namespace fmm {
 constexpr int TC_M = 128;               // translations per tile (MMA M)
 constexpr int TC_KC = 16;               // K per stage (2 MMA K-steps of 8)
 constexpr int TC_STAGES = 4;
-constexpr int TC_THREADS = 448;         // 14 warps
 constexpr int TC_AWARPS = 8;            // source-gather warps (2..9)
 constexpr int TC_EPI0 = 2 + TC_AWARPS;  // first epilogue warp
-constexpr int TC_MAXP = 16;
+constexpr int TC_EWARPS = 8;            // epilogue warps (10..17), two per TMEM lane quarter
+constexpr int TC_THREADS = 32 * (TC_EPI0 + TC_EWARPS);
+constexpr int TC_MAXP = 20;
+constexpr int TC_MTAB = TC_MAXP * TC_MAXP + 8;  // order m of every coefficient (int8), zero padded
 constexpr int TC_EPI_LD = 33;           // staging row stride (floats) of the epilogue
 constexpr size_t TC_SMEM_MAX = 232448;  // 227 KB of dynamic shared memory per CTA
 
 struct TcPass {
     const int4 *items;
-    const int *g_src, *g_dst;
+    const int *g_src, *g_dst, *g_dir;    // per translation (class order): boxes and direction
+    const float2 *PH;                    // phases e^{i m phi} of direction d at d phstride + phoff + m
+    int phstride, phoff;
     int nrhs, nsrc, ndst;
     int p, K, nch, nhalf, CH, Nmma, ntiles;
     int res;                      // operator resident: one output half, whole operator in shared memory
@@ -64,7 +72,7 @@ static size_t tc_stage_bytes(int Nmma) { return (size_t)8 * TC_KC * (TC_M + Nmma
 static size_t tc_smem_bytes(int Nmma, int res, int nch)
 {
     size_t main = res ? TC_STAGES * (size_t)8 * TC_KC * TC_M + (size_t)nch * 8 * TC_KC * Nmma : TC_STAGES * tc_stage_bytes(Nmma);
-    return main + 4 * 32 * TC_EPI_LD * sizeof(float) + (2 * TC_STAGES + 6) * 8 + 16;
+    return main + TC_EWARPS * 32 * TC_EPI_LD * sizeof(float) + (2 * TC_STAGES + 6) * 8 + 16 + TC_MTAB;
 }
 
 // Output halves and MMA width for order p: each half holds CH coefficients (2 CH real outputs,
@@ -89,6 +97,24 @@ static bool tc_geometry(int p, TcM2L &g)
 
 // destination / source expansion of row r of tile (it): column e = translation t x nrhs + r,
 // expansions stored [box][rhs][p^2]
+// degree n and order m of coefficient i = n^2 + n + m
+__device__ __forceinline__ void tc_nm(int i, int &n, int &m)
+{
+    int q = (int)sqrtf((float)i);
+    while (q * q > i) q--;
+    while ((q + 1) * (q + 1) <= i) q++;
+    n = q;
+    m = i - q * q - q;
+}
+
+// phases e^{i m phi} of the direction of row r of tile (it), indexed by m; null for an empty row
+__device__ __forceinline__ const float2 *tile_phases(const TcPass &ps, int4 it, int r)
+{
+    if (r >= it.z) return nullptr;
+    const int t = (it.y + r) / ps.nrhs;
+    return ps.PH + (size_t)ps.g_dir[t] * ps.phstride + ps.phoff;
+}
+
 __device__ __forceinline__ int tile_box(const TcPass &ps, int4 it, int r, bool source)
 {
     if (r >= it.z) return -1;
@@ -103,13 +129,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
     const uint32_t tA = (uint32_t)TC_M * TC_KC * 4, tB = (uint32_t)Nmma * TC_KC * 4, stage = 2 * tA + (res ? 0 : 2 * tB);
     unsigned char *bres = smem + TC_STAGES * stage;  // resident operator (res)
     float *epi = reinterpret_cast<float *>(bres + (res ? (size_t)nch * 2 * tB : 0));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(epi + 4 * 32 * TC_EPI_LD);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(epi + TC_EWARPS * 32 * TC_EPI_LD);
     uint64_t *full = bars, *empty = bars + TC_STAGES, *accf = bars + 2 * TC_STAGES, *acce = accf + 2;
     uint64_t *bfull = acce + 2, *bempty = bfull + 1;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(bempty + 1);
+    signed char *s_m = reinterpret_cast<signed char *>(tslot + 4);  // m of coefficient i, 0 beyond p^2
+    for (int i = threadIdx.x; i < TC_MTAB; i += blockDim.x) {
+        int n, m;
+        tc_nm(i, n, m);
+        s_m[i] = i < P2 ? (signed char)m : (signed char)0;
+    }
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // tiles of this CTA: strided over the grid, or (res) one contiguous range, so that
-    // consecutive tiles share their direction and its resident operator
+    // consecutive tiles share their class and its resident operator
     const int q_first = res ? (int)((long long)blockIdx.x * ps.ntiles / gridDim.x) : (int)blockIdx.x;
     const int q_end = res ? (int)((long long)(blockIdx.x + 1) * ps.ntiles / gridDim.x) : ps.ntiles;
     const int q_step = res ? 1 : (int)gridDim.x;
@@ -125,7 +157,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
         }
         for (int a = 0; a < 2; a++) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(accf + a)));   // MMA commit
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(smem_u32(acce + a)));   // 4 epilogue warps
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(acce + a)), "r"(TC_EWARPS));  // epilogue warps
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bfull)));   // operator copy (res)
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bempty)));  // MMA commit (res)
@@ -147,7 +179,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                 const int a = i & 1;
                 ok = mbar_wait(smem_u32(acce + a), ((i >> 1) & 1) ^ 1);
                 if (ok && res && ps.items[q].x != cur) {
-                    // this tile's operator: the copy of the next direction run
+                    // this tile's operator: the copy of the next class run
                     ok = mbar_wait(smem_u32(bfull), loads & 1);
                     loads++;
                     cur = ps.items[q].x;
@@ -180,7 +212,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                                      smem_u32(accf + a))
                                  : "memory");
-                // the last tile of a direction run releases the resident operator once its MMAs are done
+                // the last tile of a class run releases the resident operator once its MMAs are done
                 if (ok && res && (q + 1 >= q_end || ps.items[q + 1].x != cur))
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                                      smem_u32(bempty))
@@ -190,7 +222,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
     } else if (warp == 1) {
         // ---------------------------------------------------------------- operator copies
         if (lane == 0 && res) {
-            // one copy of a direction's whole operator per direction run
+            // one copy of a class's whole operator per class run
             const uint32_t bytes = (uint32_t)nch * 2 * tB;
             int loads = 0, cur = -1;
             for (int q = q_first; q < q_end && ok; q += q_step) {
@@ -232,6 +264,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
         // two threads per row (translation), each 8 of every 16-wide K chunk; the loads of the
         // next two chunks are in flight while a chunk waits for its stage and is stored
         constexpr int KH = TC_KC / 2;
+        static_assert(KH == 8, "four complex coefficients per thread and chunk half");
         const int at = tid - 64, r = at & (TC_M - 1), kh = (at >> 7) * KH;
         const float *srcf = reinterpret_cast<const float *>(ps.src);
         const bool vec4 = (K & 3) == 0;
@@ -240,8 +273,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
             const int item = q / ps.nhalf;
             const int sb = tile_box(ps, ps.items[item], r, true);
             const float *row = srcf + (size_t)(sb < 0 ? 0 : sb) * K;
-            auto load = [&](float(&x)[KH], int c) {
+            const float2 *phr = tile_phases(ps, ps.items[item], r);
+            if (!phr) phr = ps.PH + ps.phoff;  // an empty row (its x is zero): any valid phase
+            // the row's source coefficients and their phases e^{i m phi}: KH / 2 = 4 complex
+            // coefficients from i0 = k0 / 2 on (i0 a multiple of 4, so their four orders are
+            // one 32-bit word of the m table)
+            auto load = [&](float(&x)[KH], float2(&f)[KH / 2], int c) {
                 const int k0 = c * TC_KC + kh;
+                {
+                    const uint32_t mm = *reinterpret_cast<const uint32_t *>(s_m + (k0 >> 1));
+#pragma unroll
+                    for (int j = 0; j < KH / 2; j++) f[j] = __ldg(phr + (int)(signed char)(mm >> (8 * j)));
+                }
 #pragma unroll
                 for (int j = 0; j < KH; j += 4) {
                     const int k = k0 + j;
@@ -256,8 +299,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                     }
                 }
             };
-            auto store = [&](const float(&x)[KH], int gg) -> bool {
+            auto store = [&](float(&x)[KH], const float2(&f)[KH / 2], int gg) -> bool {
                 const int s = gg % TC_STAGES;
+#pragma unroll
+                for (int j = 0; j < KH / 2; j++) {
+                    const float xr = x[2 * j], xi = x[2 * j + 1];
+                    x[2 * j] = xr * f[j].x - xi * f[j].y;
+                    x[2 * j + 1] = xr * f[j].y + xi * f[j].x;
+                }
                 if (!mbar_wait(smem_u32(empty + s), ((gg / TC_STAGES) & 1) ^ 1)) return false;
                 unsigned char *Ahi = smem + s * stage, *Alo = Ahi + tA;
 #pragma unroll
@@ -277,33 +326,46 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                 return true;
             };
             float xa[KH], xb[KH], xc[KH];
-            load(xa, 0);
-            if (nch > 1) load(xb, 1);
+            float2 fa[KH / 2], fb[KH / 2], fc[KH / 2];
+            load(xa, fa, 0);
+            if (nch > 1) load(xb, fb, 1);
             for (int c = 0; c < nch && ok; c += 3) {
-                if (c + 2 < nch) load(xc, c + 2);
-                ok = store(xa, g + c);
+                if (c + 2 < nch) load(xc, fc, c + 2);
+                ok = store(xa, fa, g + c);
                 if (!ok || c + 1 >= nch) break;
-                if (c + 3 < nch) load(xa, c + 3);
-                ok = store(xb, g + c + 1);
+                if (c + 3 < nch) load(xa, fa, c + 3);
+                ok = store(xb, fb, g + c + 1);
                 if (!ok || c + 2 >= nch) break;
-                if (c + 4 < nch) load(xb, c + 4);
-                ok = store(xc, g + c + 2);
+                if (c + 4 < nch) load(xb, fb, c + 4);
+                ok = store(xc, fc, g + c + 2);
             }
             g += nch;
         }
     } else {
         // ---------------------------------------------------------------- epilogue
-        const int wq = warp & 3;  // TMEM lane quarter of this warp
+        // warp w reads TMEM lane quarter w % 4; the two warps of a quarter take alternate
+        // 32-column blocks
+        const int wq = warp & 3, eh = (warp - TC_EPI0) >> 2;
         float *st = epi + (warp - TC_EPI0) * 32 * TC_EPI_LD;
+        // destinations of coefficient pairs 16-byte aligned: p^2 and the half width even
+        const bool pairs = (P2 % 2 == 0) && (ps.CH % 2 == 0);
         int i = 0;
         for (int q = q_first; q < q_end && ok; q += q_step, i++) {
             const int a = i & 1, item = q / ps.nhalf, h = q - item * ps.nhalf;
-            const int dbox = tile_box(ps, ps.items[item], wq * 32 + lane, false);
+            const int4 it = ps.items[item];
+            const int row = wq * 32 + lane;
+            const int dbox = tile_box(ps, it, row, false);
+            const int drow = row < it.z ? ps.g_dir[(it.y + row) / ps.nrhs] : 0;
+            // rows of one class run hold each direction's translations contiguously, so a tile
+            // whose first and last rows share a direction has one direction (one set of phases)
+            const int d0 = ps.g_dir[it.y / ps.nrhs];
+            const bool uni = d0 == ps.g_dir[(it.y + it.z - 1) / ps.nrhs];
+            const float2 *ph0 = ps.PH + (size_t)d0 * ps.phstride + ps.phoff;
             const int co0 = h * ps.CH, nco = min(ps.CH, P2 - co0);
             ok = mbar_wait(smem_u32(accf + a), (i >> 1) & 1);
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            for (int cb = 0; cb < Nmma; cb += 32) {
+            for (int cb = 32 * eh; cb < Nmma; cb += 64) {
                 uint32_t v[32];
                 const uint32_t ta = tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(a * 256 + cb);
                 asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -318,15 +380,44 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
 #pragma unroll
                 for (int j = 0; j < 32; j++) st[lane * TC_EPI_LD + j] = __uint_as_float(v[j]);
                 __syncwarp();
-                // two rows per step, 16 coefficients (32 columns) per row
-                const int jc = lane & 15, c2 = cb + 2 * jc;
+                if (pairs) {
+                    // four rows per step, 8 pairs of coefficients per row, each pair added with one
+                    // 16-byte atomic; coefficient co of row rr times e^{-i m' phi} of its direction
+                    const int jq = lane & 7, co = co0 + cb / 2 + 2 * jq;
+                    const bool cv = cb + 4 * jq < 2 * nco;
+                    const int m0 = s_m[cv ? co : 0], m1 = s_m[cv ? co + 1 : 0];
+                    const float2 u0 = __ldg(ph0 + m0), u1 = __ldg(ph0 + m1);
 #pragma unroll 4
-                for (int rp = 0; rp < 16; rp++) {
-                    const int rr = 2 * rp + (lane >> 4);
-                    const int d = __shfl_sync(0xffffffffu, dbox, rr);
-                    if (d >= 0 && c2 < 2 * nco)
-                        atomicAdd(ps.dst + (size_t)d * P2 + co0 + c2 / 2,
-                                  make_float2(st[rr * TC_EPI_LD + 2 * jc], st[rr * TC_EPI_LD + 2 * jc + 1]));
+                    for (int rq = 0; rq < 8; rq++) {
+                        const int rr = 4 * rq + (lane >> 3);
+                        const int d = __shfl_sync(0xffffffffu, dbox, rr);
+                        const int dr = __shfl_sync(0xffffffffu, drow, rr);
+                        if (d >= 0 && cv) {
+                            const float2 *pr = ps.PH + (size_t)dr * ps.phstride + ps.phoff;
+                            const float2 e0 = uni ? u0 : __ldg(pr + m0), e1 = uni ? u1 : __ldg(pr + m1);
+                            const float *y = st + rr * TC_EPI_LD + 4 * jq;
+                            const float4 w = make_float4(y[0] * e0.x + y[1] * e0.y, y[1] * e0.x - y[0] * e0.y,
+                                                         y[2] * e1.x + y[3] * e1.y, y[3] * e1.x - y[2] * e1.y);
+                            atomicAdd(reinterpret_cast<float4 *>(ps.dst + (size_t)d * P2 + co), w);
+                        }
+                    }
+                } else {
+                    // two rows per step, 16 coefficients (32 columns) per row
+                    const int jc = lane & 15, c2 = cb + 2 * jc, co = co0 + c2 / 2;
+                    const bool cv = c2 < 2 * nco;
+                    const int mo = s_m[cv ? co : 0];
+                    const float2 fu = __ldg(ph0 + mo);
+#pragma unroll 4
+                    for (int rp = 0; rp < 16; rp++) {
+                        const int rr = 2 * rp + (lane >> 4);
+                        const int d = __shfl_sync(0xffffffffu, dbox, rr);
+                        const int dr = __shfl_sync(0xffffffffu, drow, rr);
+                        if (d >= 0 && cv) {
+                            const float2 e = uni ? fu : __ldg(ps.PH + (size_t)dr * ps.phstride + ps.phoff + mo);
+                            const float yr = st[rr * TC_EPI_LD + 2 * jc], yi = st[rr * TC_EPI_LD + 2 * jc + 1];
+                            atomicAdd(ps.dst + (size_t)d * P2 + co, make_float2(yr * e.x + yi * e.y, yi * e.x - yr * e.y));
+                        }
+                    }
                 }
                 __syncwarp();
             }
@@ -341,7 +432,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
-// The real-embedded operators of one level, split into TF32 hi/lo, in the tile layout:
+// The real-embedded class operators of one level, split into TF32 hi/lo, in the tile layout:
 // element (o, k) of half h, chunk c holds  Re T (o, k even-even / odd-odd), -Im T (o even, k
 // odd) or Im T (o odd, k even) of coefficient (h CH + o/2, (c KC + k)/2).
 // dinv (plans with scaled FP32 expansions, else null): 1/d_n per degree; the operator maps
@@ -379,10 +470,24 @@ static int build_tc_level(Plan *P, int l)
     TcM2L &g = L.tc;
     if (!tc_geometry(L.p, g)) return FMM_OK;
     const int P2 = L.p * L.p;
-    size_t total = (size_t)NDIR * g.nhalf * g.nch * 2 * g.Nmma * g.KC;
+    std::vector<int> rep;
+    direction_classes(P, PASS_M2L, NDIR, g.cls_of_dir, rep);
+    g.ncls = (int)rep.size();
+    size_t total = (size_t)g.ncls * g.nhalf * g.nch * 2 * g.Nmma * g.KC;
     double2 *T = nullptr;
-    FMM_CUDA_TRY(cudaMalloc(&T, sizeof(double2) * (size_t)NDIR * P2 * P2));
-    int st = gen_dense_m2l(P, l, T);
+    int *rep_dev = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&T, sizeof(double2) * (size_t)g.ncls * P2 * P2));
+    cudaError_t e0 = cudaMalloc(&rep_dev, sizeof(int) * rep.size());
+    if (e0 == cudaSuccess) e0 = cudaMemcpy(rep_dev, rep.data(), sizeof(int) * rep.size(), cudaMemcpyHostToDevice);
+    if (e0 != cudaSuccess) {
+        cudaFree(T);
+        cudaFree(rep_dev);
+        fmm_set_error("tensor-core M2L tables: %s", cudaGetErrorString(e0));
+        return FMM_ERR_CUDA;
+    }
+    int st = gen_dense_m2l(P, l, rep_dev, g.ncls, T);
+    if (st == FMM_OK && cudaStreamSynchronize(P->stream) != cudaSuccess) st = FMM_ERR_CUDA;
+    cudaFree(rep_dev);
     if (st) { cudaFree(T); return st; }
     cudaError_t e = dev_alloc(P, (void **)&g.B, sizeof(float) * total);
     if (e != cudaSuccess) { cudaFree(T); fmm_set_error("tensor-core M2L tables: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
@@ -404,12 +509,78 @@ static int build_tc_level(Plan *P, int l)
     return FMM_OK;
 }
 
-static int ensure_tc_items(LevelDev &L, int nrhs)
+__global__ void tc_permute_kernel(int n, const int *__restrict__ perm, const int *__restrict__ src,
+                                  const int *__restrict__ dst, int *__restrict__ psrc, int *__restrict__ pdst)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int t = perm[i];
+        psrc[i] = src[t];
+        pdst[i] = dst[t];
+    }
+}
+
+// The level's translations in class order and the tiles over them, rebuilt when nrhs
+// changes: where the expansions of nrhs columns are more than L2 keeps, the destination boxes
+// are cut into Morton ranges first (as for the SIMT tiles); within a range, class by class,
+// the runs of the class's directions one after another (each run sorted by destination).
+// Tiles are (class, first column, count) of at most 128 columns e = t nrhs + r.
+static int ensure_tc_items(LevelDev &L, int nrhs, cudaStream_t st)
 {
     TcM2L &g = L.tc;
     if (g.items_nrhs == nrhs) return FMM_OK;
+    const RcrList &Lst = L.m2l;
+    const int nkeys = (int)Lst.key_beg.size() - 1, T = Lst.key_beg.back(), nd = std::max(Lst.ndst_rank, 1);
+    const size_t ws = 2 * (size_t)L.nb * L.p * L.p * sizeof(float2) * nrhs, budget = 48u << 20;
+    const long long nblk = std::min<long long>(nd, std::max<long long>(1, (long long)((ws + budget - 1) / budget)));
+    std::vector<std::vector<int>> dirs(g.ncls);
+    for (int d = 0; d < nkeys; d++) dirs[g.cls_of_dir[d]].push_back(d);
+    std::vector<int> perm, pdir;
     std::vector<int4> items;
-    build_items(L.m2l, nrhs, TC_M, 2 * (size_t)L.nb * L.p * L.p * sizeof(float2) * nrhs, false, items);
+    perm.reserve(T);
+    pdir.reserve(T);
+    const int *rk = Lst.dst_rank.data();
+    for (long long k = 0; k < nblk; k++) {
+        const int lo = (int)(k * nd / nblk), hi = (int)((k + 1) * nd / nblk);
+        for (int c = 0; c < g.ncls; c++) {
+            const long long r0 = (long long)perm.size();
+            for (int d : dirs[c]) {
+                int a0 = Lst.key_beg[d], a1 = Lst.key_beg[d + 1];
+                if (nblk > 1) {
+                    a0 = (int)(std::lower_bound(rk + Lst.key_beg[d], rk + Lst.key_beg[d + 1], lo) - rk);
+                    a1 = (int)(std::lower_bound(rk + Lst.key_beg[d], rk + Lst.key_beg[d + 1], hi) - rk);
+                }
+                for (int a = a0; a < a1; a++) {
+                    perm.push_back(a);
+                    pdir.push_back(d);
+                }
+            }
+            const long long e0 = r0 * nrhs, e1 = (long long)perm.size() * nrhs;
+            for (long long a = e0; a < e1; a += TC_M)
+                items.push_back(make_int4(c, (int)a, (int)std::min<long long>(TC_M, e1 - a), 0));
+        }
+    }
+    if ((int)perm.size() != T) {
+        fmm_set_error("tensor-core M2L: the class order covers %d of %d translations", (int)perm.size(), T);
+        return FMM_ERR_ARG;
+    }
+    if (!g.src && T > 0) {
+        FMM_CUDA_TRY(cudaMalloc(&g.src, sizeof(int) * T));
+        FMM_CUDA_TRY(cudaMalloc(&g.dst, sizeof(int) * T));
+        FMM_CUDA_TRY(cudaMalloc(&g.dir, sizeof(int) * T));
+    }
+    if (T > 0) {
+        int *perm_dev = nullptr;
+        FMM_CUDA_TRY(cudaMalloc(&perm_dev, sizeof(int) * T));
+        cudaError_t e = cudaMemcpy(perm_dev, perm.data(), sizeof(int) * T, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(g.dir, pdir.data(), sizeof(int) * T, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            tc_permute_kernel<<<(T + 255) / 256, 256, 0, st>>>(T, perm_dev, Lst.src, Lst.dst, g.src, g.dst);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        cudaFree(perm_dev);
+        if (e != cudaSuccess) { fmm_set_error("tensor-core M2L lists: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
+    }
     if (items.size() > g.items_cap) {
         if (g.items) cudaFree(g.items);
         g.items = nullptr;
@@ -427,12 +598,16 @@ int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st)
     LevelDev &L = P->lev[l];
     TcM2L &g = L.tc;
     if (L.m2l.key_beg.empty() || L.m2l.key_beg.back() == 0) return FMM_OK;
-    int e = ensure_tc_items(L, nrhs);
+    int e = ensure_tc_items(L, nrhs, st);
     if (e) return e;
     TcPass ps;
     ps.items = g.items;
-    ps.g_src = L.m2l.src;
-    ps.g_dst = L.m2l.dst;
+    ps.g_src = g.src;
+    ps.g_dst = g.dst;
+    ps.g_dir = g.dir;
+    ps.PH = P->PHsr32;
+    ps.phstride = 2 * P->pmax - 1;
+    ps.phoff = P->pmax - 1;
     ps.nrhs = nrhs;
     ps.nsrc = L.nb;
     ps.ndst = L.nb;
@@ -512,7 +687,7 @@ int check_tc_error(Plan *P)
     return FMM_OK;
 }
 
-// For every level with p <= 16: build the dense split operators and keep the tensor-core
+// For every level with p <= 20: build the dense split operators and keep the tensor-core
 // pass where it beats the SIMT tiles on this plan (4 timed runs each), else free its tables.
 // FMMBEM_TENSOR_M2L=0 keeps the SIMT tiles, =1 takes the tensor cores wherever they apply.
 int tune_tc_m2l(Plan *P)

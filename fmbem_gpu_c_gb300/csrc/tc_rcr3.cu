@@ -548,7 +548,7 @@ static inline void t3_put(float *tab, long long base, int Npad, int o, int k, do
 }
 
 // polar-angle class of every key (direction or octant) of a pass
-static void t3_classes(const Plan *P, int which, int nkeys, std::vector<int> &cls, std::vector<int> &rep)
+void direction_classes(const Plan *P, int which, int nkeys, std::vector<int> &cls, std::vector<int> &rep)
 {
     cls.assign(nkeys, -1);
     rep.clear();
@@ -595,7 +595,7 @@ int build_tc3(Plan *P, int l, int which)
     for (int d = 0; d < nkeys; d++)
         for (int q = Lst->key_beg[d]; q < Lst->key_beg[d + 1]; q++) tdir[q] = d;
     std::vector<int> clsR, rep;
-    t3_classes(P, which, nkeys, clsR, rep);
+    direction_classes(P, which, nkeys, clsR, rep);
     t.nclsR = (int)rep.size();
     int nclsC = 0;
     for (int d = 0; d < nkeys; d++) nclsC = std::max(nclsC, Lst->key_w[d] + 1);

@@ -80,8 +80,8 @@ typedef struct {
     double setup_seconds;
     int m2l_columns[FMM_MAX_LEVEL + 1];  /* mixed path: M2L translations per CTA tile (0 without mixed tables) */
     int m2l_tensor[FMM_MAX_LEVEL + 1];   /* mixed path: 1 where the level's M2L runs on the tensor cores
-                                            (tcgen05, split TF32, dense per-direction operators; levels with
-                                            p <= 16 where plan-time timing found it faster, or all of them
+                                            (tcgen05, split TF32, dense operators per class of directions; levels with
+                                            p <= 20 where plan-time timing found it faster, or all of them
                                             with FMMBEM_TENSOR_M2L=1; none with FMMBEM_TENSOR_M2L=0) */
     int expansions_scaled;               /* mixed path: 1 where the FP32 expansions are kept scaled by degree
                                             (low k t, where the plain coaxial entries would leave the FP32

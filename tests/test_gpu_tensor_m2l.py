@@ -1,4 +1,5 @@
-"""The tensor-core M2L (tcgen05, split TF32, dense per-direction operators) of the mixed path:
+"""The tensor-core M2L (tcgen05, split TF32, dense operators per class of directions with equal
+polar angle and distance, azimuthal phases applied per row) of the mixed path:
 forced on with FMMBEM_TENSOR_M2L=1, against the FP64 matvec, the SIMT tiles and the oracle,
 for even and odd orders, one and several right-hand sides, and the Burton-Miller operator."""
 import os
@@ -28,7 +29,7 @@ def make_plan(fm, mode, *args, **kw):
 
 
 # (p = 16 at 1 kHz would leave the FP32 range in the coaxial tables: no mixed path there)
-@pytest.mark.parametrize("p,k", [(8, K1), (9, K1), (13, K1), (16, K2)])
+@pytest.mark.parametrize("p,k", [(8, K1), (9, K1), (13, K1), (16, K2), (20, K2)])
 def test_tensor_m2l_matches_fp64_and_oracle(fm, oracle, p, k):
     V, F = fm.icosphere(3, 0.1)
     kw = dict(k=k, depth=3, p_levels={2: p, 3: p}, rule=1, a=0.5, b=0.0, c=-1.0)
@@ -55,11 +56,11 @@ def test_tensor_m2l_matches_fp64_and_oracle(fm, oracle, p, k):
 
 
 def test_tensor_m2l_on_the_81920_triangle_workload(fm):
-    """cfg2 orders 40/30/20/14/10: the levels with p <= 16 (14 and 10) on the tensor cores."""
+    """Orders 40/30/20/14/10: the levels with p <= 20 (20, 14 and 10) on the tensor cores."""
     V, F = fm.icosphere(6, 0.3)
     P2 = {2: 40, 3: 30, 4: 20, 5: 14, 6: 10}
     plan = make_plan(fm, "1", V, F, k=K2, depth=6, p_levels=P2, rule=0, a=0.5, b=0.0, c=-1.0)
-    assert [plan.info.m2l_tensor[l] for l in range(2, 7)] == [0, 0, 0, 1, 1]
+    assert [plan.info.m2l_tensor[l] for l in range(2, 7)] == [0, 0, 1, 1, 1]
     rng = np.random.default_rng(0)
     x = rng.standard_normal(plan.nf) + 1j * rng.standard_normal(plan.nf)
     y64 = plan.matvec(x, fm.FMM_FP64)
