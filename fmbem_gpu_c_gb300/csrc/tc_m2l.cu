@@ -268,78 +268,115 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
         const int at = tid - 64, r = at & (TC_M - 1), kh = (at >> 7) * KH;
         const float *srcf = reinterpret_cast<const float *>(ps.src);
         const bool vec4 = (K & 3) == 0;
-        int g = 0;
-        for (int q = q_first; q < q_end && ok; q += q_step) {
-            const int item = q / ps.nhalf;
-            const int sb = tile_box(ps, ps.items[item], r, true);
-            const float *row = srcf + (size_t)(sb < 0 ? 0 : sb) * K;
-            const float2 *phr = tile_phases(ps, ps.items[item], r);
-            if (!phr) phr = ps.PH + ps.phoff;  // an empty row (its x is zero): any valid phase
-            // the row's source coefficients and their phases e^{i m phi}: KH / 2 = 4 complex
-            // coefficients from i0 = k0 / 2 on (i0 a multiple of 4, so their four orders are
-            // one 32-bit word of the m table)
-            auto load = [&](float(&x)[KH], float2(&f)[KH / 2], int c) {
-                const int k0 = c * TC_KC + kh;
-                {
-                    const uint32_t mm = *reinterpret_cast<const uint32_t *>(s_m + (k0 >> 1));
-#pragma unroll
-                    for (int j = 0; j < KH / 2; j++) f[j] = __ldg(phr + (int)(signed char)(mm >> (8 * j)));
-                }
-#pragma unroll
-                for (int j = 0; j < KH; j += 4) {
-                    const int k = k0 + j;
-                    if (sb >= 0 && vec4 && k + 3 < K) {
-                        float4 v = __ldg(reinterpret_cast<const float4 *>(row + k));
-                        x[j] = v.x; x[j + 1] = v.y; x[j + 2] = v.z; x[j + 3] = v.w;
-                    } else {
-                        float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
-                        if (sb >= 0 && k + 1 < K) v0 = __ldg(reinterpret_cast<const float2 *>(row + k));
-                        if (sb >= 0 && k + 3 < K) v1 = __ldg(reinterpret_cast<const float2 *>(row + k + 2));
-                        x[j] = v0.x; x[j + 1] = v0.y; x[j + 2] = v1.x; x[j + 3] = v1.y;
-                    }
-                }
-            };
-            auto store = [&](float(&x)[KH], const float2(&f)[KH / 2], int gg) -> bool {
-                const int s = gg % TC_STAGES;
-#pragma unroll
-                for (int j = 0; j < KH / 2; j++) {
-                    const float xr = x[2 * j], xi = x[2 * j + 1];
-                    x[2 * j] = xr * f[j].x - xi * f[j].y;
-                    x[2 * j + 1] = xr * f[j].y + xi * f[j].x;
-                }
-                if (!mbar_wait(smem_u32(empty + s), ((gg / TC_STAGES) & 1) ^ 1)) return false;
-                unsigned char *Ahi = smem + s * stage, *Alo = Ahi + tA;
-#pragma unroll
-                for (int j = 0; j < KH; j += 4) {
-                    float4 hi, lo;
-                    hi.x = tf32_round(x[j]); lo.x = tf32_round(x[j] - hi.x);
-                    hi.y = tf32_round(x[j + 1]); lo.y = tf32_round(x[j + 1] - hi.y);
-                    hi.z = tf32_round(x[j + 2]); lo.z = tf32_round(x[j + 2] - hi.z);
-                    hi.w = tf32_round(x[j + 3]); lo.w = tf32_round(x[j + 3] - hi.w);
-                    const uint32_t o = core_off(r, kh + j, TC_KC);
-                    *reinterpret_cast<float4 *>(Ahi + o) = hi;
-                    *reinterpret_cast<float4 *>(Alo + o) = lo;
-                }
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(full + s));
-                return true;
-            };
-            float xa[KH], xb[KH], xc[KH];
-            float2 fa[KH / 2], fb[KH / 2], fc[KH / 2];
-            load(xa, fa, 0);
-            if (nch > 1) load(xb, fb, 1);
-            for (int c = 0; c < nch && ok; c += 3) {
-                if (c + 2 < nch) load(xc, fc, c + 2);
-                ok = store(xa, fa, g + c);
-                if (!ok || c + 1 >= nch) break;
-                if (c + 3 < nch) load(xa, fa, c + 3);
-                ok = store(xb, fb, g + c + 1);
-                if (!ok || c + 2 >= nch) break;
-                if (c + 4 < nch) load(xb, fb, c + 4);
-                ok = store(xc, fc, g + c + 2);
+        // The CTA's tiles as one stream of chunks u = (tile, chunk); the loads run two chunks
+        // ahead of the stores, also across tile boundaries.  The row of the tile after the one
+        // being loaded is looked up in two steps while the loads cross the current tile: its
+        // work item when they enter it, its translation's source box and direction half way
+        // through, so that neither lookup stalls the stream.
+        const int ntile = q_first < q_end ? (q_end - q_first + q_step - 1) / q_step : 0;
+        const int U = ntile * nch, cmid = nch / 2;
+        struct RowSrc {
+            const float *row;
+            const float2 *ph;
+            bool v;
+        };
+        auto tile_item = [&](int i) -> int4 {
+            return i < ntile ? ps.items[(q_first + i * q_step) / ps.nhalf] : make_int4(0, 0, 0, 0);
+        };
+        // row r of a tile from its translation's raw source box / direction (box < 0: empty row)
+        auto row_src = [&](int box, int rr, int dir) -> RowSrc {
+            RowSrc o{srcf, ps.PH + ps.phoff, false};
+            if (box < 0) return o;
+            o.row = srcf + (size_t)(box * ps.nrhs + rr) * K;
+            o.ph = ps.PH + (size_t)dir * ps.phstride + ps.phoff;
+            o.v = true;
+            return o;
+        };
+        int lt = 0, lc = 0;          // tile and chunk of the next load
+        int nbox = -1, nrr = 0, ndir = 0;
+        auto lookup = [&](int4 it) {  // the translation of row r of item it
+            nbox = -1;
+            if (r < it.z) {
+                const int e = it.y + r, t = e / ps.nrhs;
+                nrr = e - t * ps.nrhs;
+                nbox = ps.g_src[t];
+                ndir = ps.g_dir[t];
             }
-            g += nch;
+        };
+        lookup(tile_item(0));
+        RowSrc cur = row_src(nbox, nrr, ndir);
+        int4 itn = tile_item(1);
+        // the row's source coefficients of chunk u and their phases e^{i m phi}: KH / 2 = 4
+        // complex coefficients from i0 = k0 / 2 on (i0 a multiple of 4, so their four orders
+        // are one 32-bit word of the m table)
+        auto load = [&](float(&x)[KH], float2(&f)[KH / 2]) {
+            if (lc == nch) {
+                lc = 0;
+                lt++;
+                cur = row_src(nbox, nrr, ndir);
+                itn = tile_item(lt + 1);
+            }
+            if (lc == cmid) lookup(itn);
+            const int k0 = lc * TC_KC + kh;
+            lc++;
+            {
+                const uint32_t mm = *reinterpret_cast<const uint32_t *>(s_m + (k0 >> 1));
+#pragma unroll
+                for (int j = 0; j < KH / 2; j++) f[j] = __ldg(cur.ph + (int)(signed char)(mm >> (8 * j)));
+            }
+#pragma unroll
+            for (int j = 0; j < KH; j += 4) {
+                const int k = k0 + j;
+                if (cur.v && vec4 && k + 3 < K) {
+                    float4 v = __ldg(reinterpret_cast<const float4 *>(cur.row + k));
+                    x[j] = v.x; x[j + 1] = v.y; x[j + 2] = v.z; x[j + 3] = v.w;
+                } else {
+                    float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
+                    if (cur.v && k + 1 < K) v0 = __ldg(reinterpret_cast<const float2 *>(cur.row + k));
+                    if (cur.v && k + 3 < K) v1 = __ldg(reinterpret_cast<const float2 *>(cur.row + k + 2));
+                    x[j] = v0.x; x[j + 1] = v0.y; x[j + 2] = v1.x; x[j + 3] = v1.y;
+                }
+            }
+        };
+        auto store = [&](float(&x)[KH], const float2(&f)[KH / 2], int u) -> bool {
+            const int s = u % TC_STAGES;
+#pragma unroll
+            for (int j = 0; j < KH / 2; j++) {
+                const float xr = x[2 * j], xi = x[2 * j + 1];
+                x[2 * j] = xr * f[j].x - xi * f[j].y;
+                x[2 * j + 1] = xr * f[j].y + xi * f[j].x;
+            }
+            if (!mbar_wait(smem_u32(empty + s), ((u / TC_STAGES) & 1) ^ 1)) return false;
+            unsigned char *Ahi = smem + s * stage, *Alo = Ahi + tA;
+#pragma unroll
+            for (int j = 0; j < KH; j += 4) {
+                float4 hi, lo;
+                hi.x = tf32_round(x[j]); lo.x = tf32_round(x[j] - hi.x);
+                hi.y = tf32_round(x[j + 1]); lo.y = tf32_round(x[j + 1] - hi.y);
+                hi.z = tf32_round(x[j + 2]); lo.z = tf32_round(x[j + 2] - hi.z);
+                hi.w = tf32_round(x[j + 3]); lo.w = tf32_round(x[j + 3] - hi.w);
+                const uint32_t o = core_off(r, kh + j, TC_KC);
+                *reinterpret_cast<float4 *>(Ahi + o) = hi;
+                *reinterpret_cast<float4 *>(Alo + o) = lo;
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(full + s));
+            return true;
+        };
+        float xa[KH], xb[KH], xc[KH];
+        float2 fa[KH / 2], fb[KH / 2], fc[KH / 2];
+        if (U > 0) load(xa, fa);
+        if (U > 1) load(xb, fb);
+        for (int u = 0; u < U && ok; u += 3) {
+            if (u + 2 < U) load(xc, fc);
+            ok = store(xa, fa, u);
+            if (!ok || u + 1 >= U) break;
+            if (u + 3 < U) load(xa, fa);
+            ok = store(xb, fb, u + 1);
+            if (!ok || u + 2 >= U) break;
+            if (u + 4 < U) load(xb, fb);
+            ok = store(xc, fc, u + 2);
         }
     } else {
         // ---------------------------------------------------------------- epilogue
