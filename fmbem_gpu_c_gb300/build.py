@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                   "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + SRC]
 
-SOURCES = ["plan.cu", "tables.cu", "passes.cu", "octree_gpu.cu", "octree_host.cpp", "legacy.cu", "noalloc.cu", "batched.cu", "vjp.cu", "mesh.cpp", "tc_m2l.cu", "scene.cu", "tc_rcr3.cu"]
+SOURCES = ["plan.cu", "tables.cu", "passes.cu", "octree_gpu.cu", "octree_host.cpp", "legacy.cu", "noalloc.cu", "batched.cu", "vjp.cu", "mesh.cpp", "tc_dense.cu", "scene.cu", "tc_rcr3.cu"]
 
 
 def _sources():

@@ -388,7 +388,7 @@ int launch_pass32(Plan *P, int l, int which, int nrhs, cudaStream_t st)
     RcrPass ps;
     RcrList *Lst = pass32_desc(P, l, which, nrhs, ps);
     if (Lst && Lst->t3.on) return launch_tc3_pass(P, l, which, nrhs, st);
-    if (which == PASS_M2L && P->lev[l].tc.on) return launch_tc_m2l(P, l, nrhs, st);
+    if (Lst && Lst->td.on) return launch_tc_dense(P, l, which, nrhs, st);
     return Lst ? launch_rcr_pass(*Lst, ps, st) : FMM_OK;
 }
 
@@ -570,16 +570,19 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
     return FMM_OK;
 }
 
-// Dense M2L operators of level l for the tensor-core pass: T[c][i][j] (p^2 x p^2, FP64), the
-// RCR translation of direction dirs[c] with its azimuthal phases left out (rotation by the
-// polar angle, coaxial translation, rotation back) applied to the unit multipole e_j; the
-// translation of any direction d with the same polar angle and distance is then
-// diag(e^{-i m' phi_d}) T diag(e^{i m phi_d}).  One CTA per (operator, column).
-__global__ void dense_m2l_kernel(int p, int pmax, const int *__restrict__ dirs, const double *__restrict__ Hsr,
-                                 const double2 *__restrict__ Csr, double2 *__restrict__ T)
+// Dense operators for the tensor-core passes: T[c][i][j] (pout^2 x pin^2, FP64), the RCR
+// translation of key keys[c] applied to the unit source e_j.  M2L (ph = null): direction
+// keys[c] with its azimuthal phases left out (rotation by the polar angle, coaxial
+// translation, rotation back); the translation of any direction d with the same polar angle
+// and distance is then diag(e^{-i m' phi_d}) T diag(e^{i m phi_d}).  M2M / L2L: octant keys[c]
+// with its phases.  One CTA per (operator, column).
+__global__ void dense_rcr_kernel(int p, int pmax, int pin, int pout, const int *__restrict__ keys,
+                                 const double *__restrict__ H, const double2 *__restrict__ PH,
+                                 const double2 *__restrict__ Cc, int coax_per_dir, double2 *__restrict__ T)
 {
     extern __shared__ unsigned char smraw[];
-    const int P2 = p * p, c = blockIdx.x, d = dirs[c], j = blockIdx.y, rs = rot_size(pmax), w = 2 * pmax - 1;
+    const int P2 = p * p, c = blockIdx.x, d = keys[c], j = blockIdx.y, rs = rot_size(pmax), w = 2 * pmax - 1;
+    const int pi2 = pin * pin, po2 = pout * pout;
     double2 *sE = (double2 *)smraw, *sX = sE + P2, *sW1 = sX + P2, *sW2 = sW1 + P2, *sY = sW2 + P2, *sOne = sY + P2;
     for (int i = threadIdx.x; i < P2; i += blockDim.x) {
         sE[i] = make_double2(i == j ? 1.0 : 0.0, 0.0);
@@ -587,16 +590,35 @@ __global__ void dense_m2l_kernel(int p, int pmax, const int *__restrict__ dirs, 
     }
     for (int i = threadIdx.x; i < w; i += blockDim.x) sOne[i] = make_double2(1.0, 0.0);
     __syncthreads();
-    rcr_block<double>(p, pmax, Hsr + (size_t)d * rs, sOne, Csr + (size_t)c_dir_dist[d] * coax_size(p), sE, p, sX, sW1,
-                      sW2, sY, p);
-    for (int i = threadIdx.x; i < P2; i += blockDim.x) T[((size_t)c * P2 + i) * P2 + j] = sY[i];
+    const double2 *cb = Cc + (coax_per_dir ? (size_t)c_dir_dist[d] * coax_size(p) : 0);
+    rcr_block<double>(p, pmax, H + (size_t)d * rs, PH ? PH + (size_t)d * w : sOne, cb, sE, pin, sX, sW1, sW2, sY, pout);
+    for (int i = threadIdx.x; i < po2; i += blockDim.x) T[((size_t)c * po2 + i) * pi2 + j] = sY[i];
 }
 
-int gen_dense_m2l(Plan *P, int l, const int *dirs, int ndirs, double2 *T)
+int gen_dense_rcr(Plan *P, int l, int which, const int *keys, int nkeys, double2 *T)
 {
-    const int p = P->lev[l].p;
+    const LevelDev &L = P->lev[l];
+    int p, pin, pout;
+    const double *H;
+    const double2 *PH, *Cc;
+    if (which == PASS_M2L) {
+        p = pin = pout = L.p;
+        H = P->Hsr64;
+        PH = nullptr;
+        Cc = L.Csr64;
+    } else {
+        const int pp = P->lev[l - 1].p;  // the RCR order of M2M / L2L is the parent's
+        p = pp;
+        pin = which == PASS_M2M ? L.p : pp;
+        pout = which == PASS_M2M ? pp : L.p;
+        H = which == PASS_M2M ? P->Hss64 : P->Hrr64;
+        PH = which == PASS_M2M ? P->PHss64 : P->PHrr64;
+        Cc = L.Crr64;
+    }
     size_t sm = ((size_t)5 * p * p + 2 * P->pmax) * sizeof(double2);
-    dense_m2l_kernel<<<dim3(ndirs, p * p), 128, sm, P->stream>>>(p, P->pmax, dirs, P->Hsr64, P->lev[l].Csr64, T);
+    if (sm > 48 * 1024) FMM_CUDA_TRY(cudaFuncSetAttribute(dense_rcr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    dense_rcr_kernel<<<dim3(nkeys, pin * pin), 128, sm, P->stream>>>(p, P->pmax, pin, pout, keys, H, PH, Cc,
+                                                                   which == PASS_M2L ? 1 : 0, T);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }

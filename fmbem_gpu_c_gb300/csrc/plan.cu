@@ -94,10 +94,10 @@ static void free_plan(Plan *P)
             Tc3 &t = R->t3;
             F(t.opsR); F(t.opsC); F(t.blkR); F(t.blkC); F(t.t_dir); F(t.itR1); F(t.itC); F(t.itR2);
             F(t.listR); F(t.listC); F(t.W); F(t.Z);
+            F(R->td.B); F(R->td.items); F(R->td.src); F(R->td.dst); F(R->td.dir);
         }
-        F(L.tc.B); F(L.tc.items); F(L.tc.src); F(L.tc.dst); F(L.tc.dir);
     }
-    F(P->tc_err); F(P->m2l_part64);
+    F(P->tc_err); F(P->tc_ones); F(P->m2l_part64);
     F(P->Hsr64); F(P->PHsr64); F(P->Hsr32); F(P->PHsr32);
     F(P->V_dev); F(P->F_dev); F(P->elem_leaf); F(P->leaf_beg); F(P->leaf_elem);
     F(P->U64); F(P->Rv64); F(P->U32); F(P->Rv32); F(P->near_beg); F(P->near_col); F(P->near64); F(P->near32);
@@ -242,7 +242,7 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
     if (P->opt.build_mixed) {
         TRY(build_rcr_lists(P));
         TRY(tune_rcr_tiles(P));
-        TRY(tune_tc_m2l(P));
+        TRY(tune_tc_dense(P));
         TRY(tune_tc3(P));
     }
     CTRY(dev_alloc(P, (void **)&P->xbuf, sizeof(double2) * nf));
@@ -316,8 +316,13 @@ extern "C" int fmm_plan_info(const fmm_plan *plan, fmm_info *info)
         info->p_level[l] = P->lev[l].p;
         info->num_box[l] = P->lev[l].nb;
         info->num_m2l[l] = P->lev[l].num_sr;
-        info->m2l_columns[l] = P->opt.build_mixed ? (P->lev[l].tc.on ? 128 : P->lev[l].m2l.tc) : 0;
-        info->m2l_tensor[l] = P->opt.build_mixed && P->lev[l].tc.on ? 1 : 0;
+        // the form a pass runs in: three-stage, else dense tensor-core, else SIMT tiles
+        auto dense = [](const RcrList &R) { return R.td.on && !R.t3.on; };
+        const LevelDev &L = P->lev[l];
+        info->m2l_columns[l] = P->opt.build_mixed ? (dense(L.m2l) ? 128 : L.m2l.tc) : 0;
+        info->m2l_tensor[l] = P->opt.build_mixed && dense(L.m2l) ? 1 : 0;
+        info->pass_dense[l] =
+            P->opt.build_mixed ? (dense(L.m2m) ? 1 : 0) | (dense(L.m2l) ? 2 : 0) | (dense(L.l2l) ? 4 : 0) : 0;
         if (P->opt.build_mixed)
             info->pass_tc3[l] = (P->lev[l].m2m.t3.on ? 1 : 0) | (P->lev[l].m2l.t3.on ? 2 : 0) | (P->lev[l].l2l.t3.on ? 4 : 0);
     }

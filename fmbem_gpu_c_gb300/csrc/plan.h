@@ -33,6 +33,27 @@ struct Tc3 {
     size_t scratch_cap = 0;
 };
 
+// A batched pass on the tensor cores as dense operators (tc_dense.cu).  M2L: one operator per
+// class of the 316 directions with equal (dz, dx^2 + dy^2) -- equal polar angle and distance,
+// so the class's directions differ only by their azimuthal phases, which the kernel applies
+// to each row.  M2M / L2L: one operator per octant.  Real-embedded and split into TF32 hi/lo
+// parts in the layout the MMA reads.
+struct TcDense {
+    int on = 0;                   // the pass runs on the tensor cores
+    int pin = 0, pout = 0;        // source and destination orders
+    int phased = 0;               // M2L: operators per class, phases per row
+    int KC = 40, nch = 0, nhalf = 1, CH = 0, Nmma = 0;
+    int res = 0;                  // the whole operator of a class stays in shared memory (small p)
+    int ncls = 0;                 // operators
+    std::vector<int> cls_of_dir;  // key (direction or octant) -> operator
+    float *B = nullptr;           // [class][half][chunk][hi, lo][Nmma x KC core-matrix tile]
+    size_t B_bytes = 0;
+    int4 *items = nullptr;        // (class, first column, count, 0), 128 columns each
+    size_t items_cap = 0;
+    int *src = nullptr, *dst = nullptr, *dir = nullptr;  // the pass's translations in class order
+    int n_items = 0, items_nrhs = 0;
+};
+
 // Work list of one batched translation pass: translations sorted by direction (src, dst,
 // key_beg per direction, key_w = coaxial block per direction) and the device items
 // (direction, first column, count, coaxial block) for items_nrhs right-hand sides, tc
@@ -47,24 +68,7 @@ struct RcrList {
     int n_items = 0, items_nrhs = 0;
     int tc = 8, shc = 0;          // columns per item; rotation/coaxial blocks staged in shared memory
     Tc3 t3;                       // three-stage tensor-core form (used where t3.on)
-};
-
-// M2L of one level on the tensor cores (tc_m2l.cu): one dense operator per class of the 316
-// directions with equal (dz, dx^2 + dy^2) -- equal polar angle and distance, so the class's
-// directions differ only by their azimuthal phases, which the kernel applies to each row --
-// real-embedded and split into TF32 hi/lo parts in the layout the MMA reads.
-struct TcM2L {
-    int on = 0;                   // this level's mixed M2L runs on the tensor cores
-    int KC = 40, nch = 0, nhalf = 1, CH = 0, Nmma = 0;
-    int res = 0;                  // the whole operator of a class stays in shared memory (p <= 8)
-    int ncls = 0;                 // operator classes
-    std::vector<int> cls_of_dir;  // M2L direction -> class
-    float *B = nullptr;           // [class][half][chunk][hi, lo][Nmma x KC core-matrix tile]
-    size_t B_bytes = 0;
-    int4 *items = nullptr;        // (class, first column, count, 0), 128 columns each
-    size_t items_cap = 0;
-    int *src = nullptr, *dst = nullptr, *dir = nullptr;  // the level's translations in class order
-    int n_items = 0, items_nrhs = 0;
+    TcDense td;                   // dense tensor-core form (used where td.on)
 };
 
 // One batched FP32 translation pass as the tile kernels read it.
@@ -101,7 +105,6 @@ struct LevelDev {
     // batched passes of the mixed path: M2L of this level, M2M (this level -> parents),
     // L2L (parents -> this level)
     RcrList m2l, m2m, l2l;
-    TcM2L tc;
     int m2l_split = 1;            // FP64 M2L: CTAs per box (source runs), > 1 on levels with few boxes
 };
 
@@ -152,7 +155,8 @@ struct Plan {
     int nside = 2;                // side streams in use (FMMBEM_M2L_STREAMS, 1..NSIDE)
     cudaGraphExec_t graph_exec = nullptr; // captured mixed translation passes for graph_nrhs columns
     int graph_nrhs = 0, graph_seen = 0;
-    int *tc_err = nullptr;        // set by the tensor-core M2L when one of its waits gives up
+    int *tc_err = nullptr;        // set by a tensor-core pass when one of its waits gives up
+    float2 *tc_ones = nullptr;    // phases of the tensor-core passes without phases (all 1)
     double2 *m2l_part64 = nullptr; // FP64 M2L partial sums of split levels [run][box][p^2]
     size_t device_bytes = 0;
     char mixed_note[160] = "plan was created without build_mixed";
@@ -212,13 +216,15 @@ RcrList *pass32_desc(Plan *P, int l, int which, int nrhs, RcrPass &ps);
 // plan.cu: y = a x + b y over n entries
 void launch_axpby(double a, const double2 *x, double b, double2 *y, size_t n, cudaStream_t st);
 
-// tc_m2l.cu
-int gen_dense_m2l(Plan *P, int l, const int *dirs, int ndirs, double2 *T);   // passes.cu
+// tc_dense.cu
+// Dense FP64 operators of a pass (passes.cu): T[c][i][j] (pout^2 x pin^2), the RCR translation
+// of key keys[c] applied to the unit source e_j; M2L without its azimuthal phases.
+int gen_dense_rcr(Plan *P, int l, int which, const int *keys, int nkeys, double2 *T);
 // Classes of a pass's keys with one rotation: M2L directions of equal (dz, dx^2 + dy^2), M2M /
 // L2L octants of equal z bit.  cls[key] = class, rep[class] = its first key.  (tc_rcr3.cu)
 void direction_classes(const Plan *P, int which, int nkeys, std::vector<int> &cls, std::vector<int> &rep);
-int tune_tc_m2l(Plan *P);
-int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st);
+int tune_tc_dense(Plan *P);
+int launch_tc_dense(Plan *P, int l, int which, int nrhs, cudaStream_t st);
 int check_tc_error(Plan *P);
 
 // tc_rcr3.cu

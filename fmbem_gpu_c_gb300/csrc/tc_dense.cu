@@ -57,8 +57,10 @@ struct TcPass {
     const int *g_src, *g_dst, *g_dir;    // per translation (class order): boxes and direction
     const float2 *PH;                    // phases e^{i m phi} of direction d at d phstride + phoff + m
     int phstride, phoff;
+    int phased;                          // M2L: phases per row (pin = pout); M2M / L2L: none (PH a
+                                         // table of ones, phstride 0)
     int nrhs, nsrc, ndst;
-    int p, K, nch, nhalf, CH, Nmma, ntiles;
+    int pin, P2o, K, nch, nhalf, CH, Nmma, ntiles;  // K = 2 pin^2 inputs, P2o = pout^2 outputs
     int res;                      // operator resident: one output half, whole operator in shared memory
     const float *B;
     const float2 *src;
@@ -75,12 +77,13 @@ static size_t tc_smem_bytes(int Nmma, int res, int nch)
     return main + TC_EWARPS * 32 * TC_EPI_LD * sizeof(float) + (2 * TC_STAGES + 6) * 8 + 16 + TC_MTAB;
 }
 
-// Output halves and MMA width for order p: each half holds CH coefficients (2 CH real outputs,
-// Nmma = that rounded up to 16, <= 256); K = 2p^2 in chunks of 16.
-static bool tc_geometry(int p, TcM2L &g)
+// Output halves and MMA width for source order pin and destination order pout: each half holds
+// CH coefficients (2 CH real outputs, Nmma = that rounded up to 16, <= 256); K = 2 pin^2 in
+// chunks of 16.
+static bool tc_geometry(int pin, int pout, TcDense &g)
 {
-    if (p < 4 || p > TC_MAXP) return false;
-    const int P2 = p * p, K = 2 * P2;
+    if (pin < 4 || pin > TC_MAXP || pout < 4 || pout > TC_MAXP) return false;
+    const int P2 = pout * pout, K = 2 * pin * pin;
     for (g.nhalf = 1;; g.nhalf++) {
         g.CH = (P2 + g.nhalf - 1) / g.nhalf;
         g.Nmma = (2 * g.CH + 15) / 16 * 16;
@@ -90,13 +93,11 @@ static bool tc_geometry(int p, TcM2L &g)
     g.nch = (K + TC_KC - 1) / TC_KC;
     if (tc_smem_bytes(g.Nmma, 0, g.nch) > TC_SMEM_MAX) return false;
     // one output half whose whole operator fits beside the A stages (p <= 8): the operator
-    // stays in shared memory while a CTA's consecutive tiles keep its direction
+    // stays in shared memory while a CTA's consecutive tiles keep its class
     g.res = g.nhalf == 1 && tc_smem_bytes(g.Nmma, 1, g.nch) <= TC_SMEM_MAX ? 1 : 0;
     return true;
 }
 
-// destination / source expansion of row r of tile (it): column e = translation t x nrhs + r,
-// expansions stored [box][rhs][p^2]
 // degree n and order m of coefficient i = n^2 + n + m
 __device__ __forceinline__ void tc_nm(int i, int &n, int &m)
 {
@@ -107,14 +108,8 @@ __device__ __forceinline__ void tc_nm(int i, int &n, int &m)
     m = i - q * q - q;
 }
 
-// phases e^{i m phi} of the direction of row r of tile (it), indexed by m; null for an empty row
-__device__ __forceinline__ const float2 *tile_phases(const TcPass &ps, int4 it, int r)
-{
-    if (r >= it.z) return nullptr;
-    const int t = (it.y + r) / ps.nrhs;
-    return ps.PH + (size_t)ps.g_dir[t] * ps.phstride + ps.phoff;
-}
-
+// destination / source expansion of row r of tile (it): column e = translation t x nrhs + r,
+// expansions stored [box][rhs][p^2]
 __device__ __forceinline__ int tile_box(const TcPass &ps, int4 it, int r, bool source)
 {
     if (r >= it.z) return -1;
@@ -122,10 +117,10 @@ __device__ __forceinline__ int tile_box(const TcPass &ps, int4 it, int r, bool s
     return (source ? ps.g_src[t] : ps.g_dst[t]) * ps.nrhs + rr;
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_dense_kernel(TcPass ps)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const int Nmma = ps.Nmma, K = ps.K, P2 = ps.p * ps.p, nch = ps.nch, res = ps.res;
+    const int Nmma = ps.Nmma, K = ps.K, P2 = ps.pin * ps.pin, P2o = ps.P2o, nch = ps.nch, res = ps.res;
     const uint32_t tA = (uint32_t)TC_M * TC_KC * 4, tB = (uint32_t)Nmma * TC_KC * 4, stage = 2 * tA + (res ? 0 : 2 * tB);
     unsigned char *bres = smem + TC_STAGES * stage;  // resident operator (res)
     float *epi = reinterpret_cast<float *>(bres + (res ? (size_t)nch * 2 * tB : 0));
@@ -385,7 +380,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
         const int wq = warp & 3, eh = (warp - TC_EPI0) >> 2;
         float *st = epi + (warp - TC_EPI0) * 32 * TC_EPI_LD;
         // destinations of coefficient pairs 16-byte aligned: p^2 and the half width even
-        const bool pairs = (P2 % 2 == 0) && (ps.CH % 2 == 0);
+        const bool pairs = (P2o % 2 == 0) && (ps.CH % 2 == 0);
         int i = 0;
         for (int q = q_first; q < q_end && ok; q += q_step, i++) {
             const int a = i & 1, item = q / ps.nhalf, h = q - item * ps.nhalf;
@@ -394,11 +389,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
             const int dbox = tile_box(ps, it, row, false);
             const int drow = row < it.z ? ps.g_dir[(it.y + row) / ps.nrhs] : 0;
             // rows of one class run hold each direction's translations contiguously, so a tile
-            // whose first and last rows share a direction has one direction (one set of phases)
+            // whose first and last rows share a direction has one direction (one set of phases);
+            // passes without phases read a table of ones (phstride 0)
             const int d0 = ps.g_dir[it.y / ps.nrhs];
-            const bool uni = d0 == ps.g_dir[(it.y + it.z - 1) / ps.nrhs];
+            const bool uni = !ps.phased || d0 == ps.g_dir[(it.y + it.z - 1) / ps.nrhs];
             const float2 *ph0 = ps.PH + (size_t)d0 * ps.phstride + ps.phoff;
-            const int co0 = h * ps.CH, nco = min(ps.CH, P2 - co0);
+            const int co0 = h * ps.CH, nco = min(ps.CH, P2o - co0);
             ok = mbar_wait(smem_u32(accf + a), (i >> 1) & 1);
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
@@ -435,7 +431,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                             const float *y = st + rr * TC_EPI_LD + 4 * jq;
                             const float4 w = make_float4(y[0] * e0.x + y[1] * e0.y, y[1] * e0.x - y[0] * e0.y,
                                                          y[2] * e1.x + y[3] * e1.y, y[3] * e1.x - y[2] * e1.y);
-                            atomicAdd(reinterpret_cast<float4 *>(ps.dst + (size_t)d * P2 + co), w);
+                            atomicAdd(reinterpret_cast<float4 *>(ps.dst + (size_t)d * P2o + co), w);
                         }
                     }
                 } else {
@@ -452,7 +448,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
                         if (d >= 0 && cv) {
                             const float2 e = uni ? fu : __ldg(ps.PH + (size_t)dr * ps.phstride + ps.phoff + mo);
                             const float yr = st[rr * TC_EPI_LD + 2 * jc], yi = st[rr * TC_EPI_LD + 2 * jc + 1];
-                            atomicAdd(ps.dst + (size_t)d * P2 + co, make_float2(yr * e.x + yi * e.y, yi * e.x - yr * e.y));
+                            atomicAdd(ps.dst + (size_t)d * P2o + co, make_float2(yr * e.x + yi * e.y, yi * e.x - yr * e.y));
                         }
                     }
                 }
@@ -469,15 +465,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) m2l_tc_kernel(TcPass ps)
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
-// The real-embedded class operators of one level, split into TF32 hi/lo, in the tile layout:
-// element (o, k) of half h, chunk c holds  Re T (o, k even-even / odd-odd), -Im T (o even, k
-// odd) or Im T (o odd, k even) of coefficient (h CH + o/2, (c KC + k)/2).
-// dinv (plans with scaled FP32 expansions, else null): 1/d_n per degree; the operator maps
-// scaled multipoles to scaled locals, T_ij / (d_n(i) d_n(j)).
-__global__ void tc_split_kernel(const double2 *__restrict__ T, int p, int KC, int nch, int nhalf, int CH, int Nmma,
-                                const double *__restrict__ dinv, float *__restrict__ B, size_t total)
+// The real-embedded operators of a pass, split into TF32 hi/lo, in the tile layout: element
+// (o, k) of half h, chunk c holds  Re T (o, k even-even / odd-odd), -Im T (o even, k odd) or
+// Im T (o odd, k even) of coefficient (h CH + o/2, (c KC + k)/2).
+// fout / fin (plans with scaled FP32 expansions, else null): per-degree factors of the
+// destination and source coefficients, so that the operator maps the scaled expansions
+// (multipoles d_n M_n, locals L_n / d_n of their own levels).
+__global__ void tc_split_kernel(const double2 *__restrict__ T, int pin, int pout, int KC, int nch, int nhalf, int CH,
+                                int Nmma, const double *__restrict__ fout, const double *__restrict__ fin,
+                                float *__restrict__ B, size_t total)
 {
-    const int P2 = p * p, K = 2 * P2;
+    const int P2i = pin * pin, P2o = pout * pout, K = 2 * P2i;
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
         size_t z = q;
         int kcol = (int)(z % KC); z /= KC;
@@ -486,13 +484,14 @@ __global__ void tc_split_kernel(const double2 *__restrict__ T, int p, int KC, in
         int c = (int)(z % nch); z /= nch;
         int h = (int)(z % nhalf);
         int d = (int)(z / nhalf);
-        int k = c * KC + kcol, nco = min(CH, P2 - h * CH);
+        int k = c * KC + kcol, nco = min(CH, P2o - h * CH);
         double v = 0.0;
         if (nr < 2 * nco && k < K) {
-            double2 t = T[((size_t)d * P2 + h * CH + nr / 2) * P2 + k / 2];
+            const int io = h * CH + nr / 2, ii = k / 2;
+            double2 t = T[((size_t)d * P2o + io) * P2i + ii];
             int po = nr & 1, pi = k & 1;
             v = po == 0 ? (pi == 0 ? t.x : -t.y) : (pi == 0 ? t.y : t.x);
-            if (dinv) v *= dinv[(int)sqrtf((float)(h * CH + nr / 2) + 0.5f)] * dinv[(int)sqrtf((float)(k / 2) + 0.5f)];
+            if (fout) v *= fout[(int)sqrtf((float)io + 0.5f)] * fin[(int)sqrtf((float)ii + 0.5f)];
         }
         float hi = tf32_round((float)v);
         float lo = tf32_round((float)(v - (double)hi));
@@ -501,48 +500,94 @@ __global__ void tc_split_kernel(const double2 *__restrict__ T, int p, int KC, in
     }
 }
 
-static int build_tc_level(Plan *P, int l)
+// The list of a pass and its orders: M2L of level l, M2M of level l into its parents, L2L of
+// the parents into level l.
+static RcrList *dense_list(Plan *P, int l, int which, int &pin, int &pout)
 {
     LevelDev &L = P->lev[l];
-    TcM2L &g = L.tc;
-    if (!tc_geometry(L.p, g)) return FMM_OK;
-    const int P2 = L.p * L.p;
+    if (which == PASS_M2L) {
+        pin = pout = L.p;
+        return &L.m2l;
+    }
+    if (l <= P->lmin) return nullptr;
+    const int pp = P->lev[l - 1].p;
+    pin = which == PASS_M2M ? L.p : pp;
+    pout = which == PASS_M2M ? pp : L.p;
+    return which == PASS_M2M ? &L.m2m : &L.l2l;
+}
+
+static int build_tc_dense(Plan *P, int l, int which)
+{
+    int pin = 0, pout = 0;
+    RcrList *Lst = dense_list(P, l, which, pin, pout);
+    if (!Lst || Lst->key_beg.empty() || Lst->key_beg.back() == 0) return FMM_OK;
+    TcDense &g = Lst->td;
+    if (!tc_geometry(pin, pout, g)) return FMM_OK;
+    g.pin = pin;
+    g.pout = pout;
+    const int nkeys = (int)Lst->key_beg.size() - 1, P2i = pin * pin, P2o = pout * pout;
     std::vector<int> rep;
-    direction_classes(P, PASS_M2L, NDIR, g.cls_of_dir, rep);
+    if (which == PASS_M2L) {
+        g.phased = 1;
+        direction_classes(P, PASS_M2L, nkeys, g.cls_of_dir, rep);
+    } else {
+        g.phased = 0;  // eight octant operators, phases included
+        g.cls_of_dir.resize(nkeys);
+        for (int d = 0; d < nkeys; d++) g.cls_of_dir[d] = d;
+        rep = g.cls_of_dir;
+    }
     g.ncls = (int)rep.size();
     size_t total = (size_t)g.ncls * g.nhalf * g.nch * 2 * g.Nmma * g.KC;
     double2 *T = nullptr;
     int *rep_dev = nullptr;
-    FMM_CUDA_TRY(cudaMalloc(&T, sizeof(double2) * (size_t)g.ncls * P2 * P2));
-    cudaError_t e0 = cudaMalloc(&rep_dev, sizeof(int) * rep.size());
-    if (e0 == cudaSuccess) e0 = cudaMemcpy(rep_dev, rep.data(), sizeof(int) * rep.size(), cudaMemcpyHostToDevice);
-    if (e0 != cudaSuccess) {
+    double *fdev = nullptr;
+    auto fail = [&](cudaError_t e) {
         cudaFree(T);
         cudaFree(rep_dev);
-        fmm_set_error("tensor-core M2L tables: %s", cudaGetErrorString(e0));
+        cudaFree(fdev);
+        fmm_set_error("tensor-core pass tables: %s", cudaGetErrorString(e));
         return FMM_ERR_CUDA;
+    };
+    cudaError_t e = cudaMalloc(&T, sizeof(double2) * (size_t)g.ncls * P2o * P2i);
+    if (e == cudaSuccess) e = cudaMalloc(&rep_dev, sizeof(int) * rep.size());
+    if (e == cudaSuccess) e = cudaMemcpy(rep_dev, rep.data(), sizeof(int) * rep.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(e);
+    int st = gen_dense_rcr(P, l, which, rep_dev, g.ncls, T);
+    if (st) {
+        cudaFree(T);
+        cudaFree(rep_dev);
+        return st;
     }
-    int st = gen_dense_m2l(P, l, rep_dev, g.ncls, T);
-    if (st == FMM_OK && cudaStreamSynchronize(P->stream) != cudaSuccess) st = FMM_ERR_CUDA;
-    cudaFree(rep_dev);
-    if (st) { cudaFree(T); return st; }
-    cudaError_t e = dev_alloc(P, (void **)&g.B, sizeof(float) * total);
-    if (e != cudaSuccess) { cudaFree(T); fmm_set_error("tensor-core M2L tables: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
-    g.B_bytes = sizeof(float) * total;
-    double *dinv = nullptr;
+    // degree factors of the scaled expansions: M2L 1/d^l both sides; M2M d^{l-1} out, 1/d^l
+    // in; L2L 1/d^l out, d^{l-1} in
+    const double *fo = nullptr, *fi = nullptr;
     if (P->scaled) {
-        std::vector<double> h(L.p);
-        for (int n = 0; n < L.p; n++) h[n] = 1.0 / P->dsc[l][n];
-        e = cudaMalloc(&dinv, sizeof(double) * L.p);
-        if (e == cudaSuccess) e = cudaMemcpy(dinv, h.data(), sizeof(double) * L.p, cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) { cudaFree(T); cudaFree(dinv); fmm_set_error("tensor-core M2L tables: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
+        const int pm = std::max(pin, pout);
+        std::vector<double> h(2 * pm, 1.0);
+        for (int n = 0; n < pm; n++) {
+            const double inv = 1.0 / P->dsc[l][n], par = which == PASS_M2L ? 1.0 : P->dsc[l - 1][n];
+            h[n] = which == PASS_M2M ? par : inv;           // out
+            h[pm + n] = which == PASS_L2L ? par : inv;      // in
+        }
+        e = cudaMalloc(&fdev, sizeof(double) * h.size());
+        if (e == cudaSuccess) e = cudaMemcpy(fdev, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(e);
+        fo = fdev;
+        fi = fdev + pm;
     }
-    tc_split_kernel<<<152 * 16, 256, 0, P->stream>>>(T, L.p, g.KC, g.nch, g.nhalf, g.CH, g.Nmma, dinv, g.B, total);
+    e = dev_alloc(P, (void **)&g.B, sizeof(float) * total);
+    if (e != cudaSuccess) return fail(e);
+    g.B_bytes = sizeof(float) * total;
+    tc_split_kernel<<<152 * 16, 256, 0, P->stream>>>(T, pin, pout, g.KC, g.nch, g.nhalf, g.CH, g.Nmma, fo, fi, g.B, total);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
     cudaFree(T);
-    cudaFree(dinv);
-    if (e != cudaSuccess) { fmm_set_error("tensor-core M2L tables: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
+    cudaFree(rep_dev);
+    cudaFree(fdev);
+    T = nullptr;
+    rep_dev = nullptr;
+    fdev = nullptr;
+    if (e != cudaSuccess) return fail(e);
     return FMM_OK;
 }
 
@@ -556,18 +601,17 @@ __global__ void tc_permute_kernel(int n, const int *__restrict__ perm, const int
     }
 }
 
-// The level's translations in class order and the tiles over them, rebuilt when nrhs
-// changes: where the expansions of nrhs columns are more than L2 keeps, the destination boxes
-// are cut into Morton ranges first (as for the SIMT tiles); within a range, class by class,
-// the runs of the class's directions one after another (each run sorted by destination).
-// Tiles are (class, first column, count) of at most 128 columns e = t nrhs + r.
-static int ensure_tc_items(LevelDev &L, int nrhs, cudaStream_t st)
+// The pass's translations in class order and the tiles over them, rebuilt when nrhs changes:
+// where the expansions of nrhs columns are more than L2 keeps, the destination boxes are cut
+// into Morton ranges first (as for the SIMT tiles); within a range, class by class, the runs
+// of the class's keys one after another (each run sorted by destination).  Tiles are (class,
+// first column, count) of at most 128 columns e = t nrhs + r.
+static int ensure_td_items(RcrList &Lst, size_t ws, int nrhs, cudaStream_t st)
 {
-    TcM2L &g = L.tc;
+    TcDense &g = Lst.td;
     if (g.items_nrhs == nrhs) return FMM_OK;
-    const RcrList &Lst = L.m2l;
     const int nkeys = (int)Lst.key_beg.size() - 1, T = Lst.key_beg.back(), nd = std::max(Lst.ndst_rank, 1);
-    const size_t ws = 2 * (size_t)L.nb * L.p * L.p * sizeof(float2) * nrhs, budget = 48u << 20;
+    const size_t budget = 48u << 20;
     const long long nblk = std::min<long long>(nd, std::max<long long>(1, (long long)((ws + budget - 1) / budget)));
     std::vector<std::vector<int>> dirs(g.ncls);
     for (int d = 0; d < nkeys; d++) dirs[g.cls_of_dir[d]].push_back(d);
@@ -597,7 +641,7 @@ static int ensure_tc_items(LevelDev &L, int nrhs, cudaStream_t st)
         }
     }
     if ((int)perm.size() != T) {
-        fmm_set_error("tensor-core M2L: the class order covers %d of %d translations", (int)perm.size(), T);
+        fmm_set_error("tensor-core pass: the class order covers %d of %d translations", (int)perm.size(), T);
         return FMM_ERR_ARG;
     }
     if (!g.src && T > 0) {
@@ -616,7 +660,7 @@ static int ensure_tc_items(LevelDev &L, int nrhs, cudaStream_t st)
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         cudaFree(perm_dev);
-        if (e != cudaSuccess) { fmm_set_error("tensor-core M2L lists: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
+        if (e != cudaSuccess) { fmm_set_error("tensor-core pass lists: %s", cudaGetErrorString(e)); return FMM_ERR_CUDA; }
     }
     if (items.size() > g.items_cap) {
         if (g.items) cudaFree(g.items);
@@ -630,26 +674,37 @@ static int ensure_tc_items(LevelDev &L, int nrhs, cudaStream_t st)
     return FMM_OK;
 }
 
-int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st)
+int launch_tc_dense(Plan *P, int l, int which, int nrhs, cudaStream_t st)
 {
-    LevelDev &L = P->lev[l];
-    TcM2L &g = L.tc;
-    if (L.m2l.key_beg.empty() || L.m2l.key_beg.back() == 0) return FMM_OK;
-    int e = ensure_tc_items(L, nrhs, st);
+    int pin = 0, pout = 0;
+    RcrList *Lst = dense_list(P, l, which, pin, pout);
+    if (!Lst || Lst->key_beg.empty() || Lst->key_beg.back() == 0) return FMM_OK;
+    TcDense &g = Lst->td;
+    RcrPass rp;
+    pass32_desc(P, l, which, nrhs, rp);
+    const size_t ws = ((size_t)rp.nsrc * pin * pin + (size_t)rp.ndst * pout * pout) * sizeof(float2) * nrhs;
+    int e = ensure_td_items(*Lst, ws, nrhs, st);
     if (e) return e;
+    if (!P->tc_ones) {
+        std::vector<float2> ones(2 * TC_MAXP + 1, make_float2(1.f, 0.f));
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&P->tc_ones, sizeof(float2) * ones.size()));
+        FMM_CUDA_TRY(cudaMemcpy(P->tc_ones, ones.data(), sizeof(float2) * ones.size(), cudaMemcpyHostToDevice));
+    }
     TcPass ps;
     ps.items = g.items;
     ps.g_src = g.src;
     ps.g_dst = g.dst;
     ps.g_dir = g.dir;
-    ps.PH = P->PHsr32;
-    ps.phstride = 2 * P->pmax - 1;
-    ps.phoff = P->pmax - 1;
+    ps.phased = g.phased;
+    ps.PH = g.phased ? P->PHsr32 : P->tc_ones;
+    ps.phstride = g.phased ? 2 * P->pmax - 1 : 0;
+    ps.phoff = g.phased ? P->pmax - 1 : TC_MAXP;
     ps.nrhs = nrhs;
-    ps.nsrc = L.nb;
-    ps.ndst = L.nb;
-    ps.p = L.p;
-    ps.K = 2 * L.p * L.p;
+    ps.nsrc = rp.nsrc;
+    ps.ndst = rp.ndst;
+    ps.pin = pin;
+    ps.P2o = pout * pout;
+    ps.K = 2 * pin * pin;
     ps.nch = g.nch;
     ps.nhalf = g.nhalf;
     ps.CH = g.CH;
@@ -657,12 +712,12 @@ int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st)
     ps.ntiles = g.n_items * g.nhalf;
     ps.res = g.res;
     ps.B = g.B;
-    ps.src = L.Cm32;
-    ps.dst = L.Dl32;
+    ps.src = rp.src;
+    ps.dst = rp.dst;
     ps.err = P->tc_err;
     size_t sm = tc_smem_bytes(g.Nmma, g.res, g.nch);
     static size_t attr = 0;
-    e = raise_smem_limit((const void *)m2l_tc_kernel, sm, &attr);
+    e = raise_smem_limit((const void *)tc_dense_kernel, sm, &attr);
     if (e) return e;
     // persistent: one CTA per SM (its shared memory and 512 TMEM columns take the SM)
     static int nsm = 0;
@@ -672,7 +727,7 @@ int launch_tc_m2l(Plan *P, int l, int nrhs, cudaStream_t st)
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         if (nsm <= 0) nsm = 152;
     }
-    m2l_tc_kernel<<<std::min(ps.ntiles, nsm), TC_THREADS, sm, st>>>(ps);
+    tc_dense_kernel<<<std::min(ps.ntiles, nsm), TC_THREADS, sm, st>>>(ps);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
@@ -724,14 +779,27 @@ int check_tc_error(Plan *P)
     return FMM_OK;
 }
 
-// For every level with p <= 20: build the dense split operators and keep the tensor-core
-// pass where it beats the SIMT tiles on this plan (4 timed runs each), else free its tables.
-// FMMBEM_TENSOR_M2L=0 keeps the SIMT tiles, =1 takes the tensor cores wherever they apply.
-int tune_tc_m2l(Plan *P)
+static void td_free(Plan *P, TcDense &g)
 {
-    const char *env = getenv("FMMBEM_TENSOR_M2L");
-    int mode = env ? atoi(env) : -1;
-    if (mode == 0) return FMM_OK;
+    cudaFree(g.B);
+    P->device_bytes -= g.B_bytes;
+    cudaFree(g.items);
+    cudaFree(g.src);
+    cudaFree(g.dst);
+    cudaFree(g.dir);
+    g = TcDense();
+}
+
+// For every pass whose source and destination orders are both <= 20 (M2L of a level, M2M
+// into and L2L out of its parent level): build the dense split operators and keep the
+// tensor-core pass where it beats the SIMT tiles on this plan (4 timed runs each), else free
+// its tables.  FMMBEM_TENSOR_M2L (M2L) and FMMBEM_TENSOR_M2M (M2M and L2L) = 0 keep the SIMT
+// tiles, = 1 take the tensor cores wherever they apply.
+int tune_tc_dense(Plan *P)
+{
+    const char *env_l = getenv("FMMBEM_TENSOR_M2L"), *env_m = getenv("FMMBEM_TENSOR_M2M");
+    const int mode_l = env_l ? atoi(env_l) : -1, mode_m = env_m ? atoi(env_m) : -1;
+    if (mode_l == 0 && mode_m == 0) return FMM_OK;
     if (!P->tc_err) {
         FMM_CUDA_TRY(dev_alloc(P, (void **)&P->tc_err, sizeof(int)));
         FMM_CUDA_TRY(cudaMemset(P->tc_err, 0, sizeof(int)));
@@ -741,36 +809,37 @@ int tune_tc_m2l(Plan *P)
     FMM_CUDA_TRY(cudaEventCreate(&b));
     int rc = FMM_OK;
     for (int l = P->lmin; l <= P->lmax && rc == FMM_OK; l++) {
-        LevelDev &L = P->lev[l];
-        if (L.num_sr == 0 || L.p > TC_MAXP) continue;
-        rc = build_tc_level(P, l);
-        if (rc || !L.tc.B) break;
-        float ms[2] = {0.f, 0.f};
-        for (int on = 0; on < 2 && rc == FMM_OK && mode != 1; on++) {
-            L.tc.on = on;
-            for (int rep = 0; rep < 4 && rc == FMM_OK; rep++) {
-                if (cudaEventRecord(a, P->stream) != cudaSuccess) rc = FMM_ERR_CUDA;
-                if (rc == FMM_OK) rc = launch_pass32(P, l, PASS_M2L, 1, P->stream);
-                if (rc == FMM_OK && cudaEventRecord(b, P->stream) != cudaSuccess) rc = FMM_ERR_CUDA;
-                if (rc == FMM_OK && cudaEventSynchronize(b) != cudaSuccess) rc = FMM_ERR_CUDA;
-                float t = 0.f;
-                cudaEventElapsedTime(&t, a, b);
-                if (rep > 0) ms[on] += t;
+        for (int which = PASS_M2M; which <= PASS_L2L && rc == FMM_OK; which++) {
+            const int mode = which == PASS_M2L ? mode_l : mode_m;
+            if (mode == 0) continue;
+            int pin = 0, pout = 0;
+            RcrList *Lst = dense_list(P, l, which, pin, pout);
+            if (!Lst || Lst->key_beg.empty() || Lst->key_beg.back() == 0) continue;
+            rc = build_tc_dense(P, l, which);
+            if (rc) break;
+            if (!Lst->td.B) continue;  // orders beyond the dense form
+            float ms[2] = {0.f, 0.f};
+            for (int on = 0; on < 2 && rc == FMM_OK && mode != 1; on++) {
+                Lst->td.on = on;
+                for (int rep = 0; rep < 4 && rc == FMM_OK; rep++) {
+                    if (cudaEventRecord(a, P->stream) != cudaSuccess) rc = FMM_ERR_CUDA;
+                    if (rc == FMM_OK) rc = launch_pass32(P, l, which, 1, P->stream);
+                    if (rc == FMM_OK && cudaEventRecord(b, P->stream) != cudaSuccess) rc = FMM_ERR_CUDA;
+                    if (rc == FMM_OK && cudaEventSynchronize(b) != cudaSuccess) rc = FMM_ERR_CUDA;
+                    float t = 0.f;
+                    cudaEventElapsedTime(&t, a, b);
+                    if (rep > 0) ms[on] += t;
+                }
             }
-        }
-        if (rc == FMM_OK) rc = check_tc_error(P);
-        if (rc) break;
-        L.tc.on = (mode == 1 || ms[1] < ms[0]) ? 1 : 0;
-        if (!L.tc.on) {
-            cudaFree(L.tc.B);
-            P->device_bytes -= L.tc.B_bytes;
-            L.tc.B = nullptr;
-            L.tc.B_bytes = 0;
+            if (rc == FMM_OK) rc = check_tc_error(P);
+            if (rc) break;
+            Lst->td.on = (mode == 1 || ms[1] < ms[0]) ? 1 : 0;
+            if (!Lst->td.on) td_free(P, Lst->td);
         }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    if (rc == FMM_ERR_CUDA && !fmm_last_error()[0]) fmm_set_error("tensor-core M2L tuning: %s", cudaGetErrorString(cudaGetLastError()));
+    if (rc == FMM_ERR_CUDA && !fmm_last_error()[0]) fmm_set_error("tensor-core pass tuning: %s", cudaGetErrorString(cudaGetLastError()));
     return rc;
 }
 

@@ -92,6 +92,12 @@ typedef struct {
                                             level l into l-1, bit 1 the M2L of level l, bit 2 the L2L from
                                             l-1 into l; chosen at plan creation by timing against the other
                                             forms (FMMBEM_TC3=0: never, 1: wherever the order allows) */
+    int pass_dense[FMM_MAX_LEVEL + 1];   /* mixed path: passes of level l run as one dense tensor-core GEMM
+                                            per operator (tcgen05, split TF32; source and destination
+                                            orders <= 20), same bits as pass_tc3 (bit 1 = m2l_tensor);
+                                            chosen at plan creation by timing (FMMBEM_TENSOR_M2L for M2L,
+                                            FMMBEM_TENSOR_M2M for M2M and L2L: 0 never, 1 wherever the
+                                            orders allow) */
 } fmm_info;
 
 typedef struct fmm_plan fmm_plan;

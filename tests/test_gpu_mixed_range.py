@@ -15,15 +15,19 @@ def rel(a, b):
 
 
 def make_plan(fm, mode, *args, **kw):
-    old = os.environ.get("FMMBEM_TENSOR_M2L")
-    os.environ["FMMBEM_TENSOR_M2L"] = mode
+    """The dense tensor-core passes (M2L, M2M and L2L) forced off ("0") or on ("1"), the
+    three-stage form off."""
+    env = {"FMMBEM_TENSOR_M2L": mode, "FMMBEM_TENSOR_M2M": mode, "FMMBEM_TC3": "0"}
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
     try:
         return fm.Plan(*args, **kw)
     finally:
-        if old is None:
-            del os.environ["FMMBEM_TENSOR_M2L"]
-        else:
-            os.environ["FMMBEM_TENSOR_M2L"] = old
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
 
 
 @pytest.mark.parametrize("tensor", ["0", "1"])

@@ -1,6 +1,7 @@
-"""The tensor-core M2L (tcgen05, split TF32, dense operators per class of directions with equal
-polar angle and distance, azimuthal phases applied per row) of the mixed path:
-forced on with FMMBEM_TENSOR_M2L=1, against the FP64 matvec, the SIMT tiles and the oracle,
+"""The dense tensor-core passes (tcgen05, split TF32) of the mixed path: the M2L with one operator
+per class of directions with equal polar angle and distance (azimuthal phases applied per row),
+and the M2M / L2L with one operator per octant, forced on (FMMBEM_TENSOR_M2L=1,
+FMMBEM_TENSOR_M2M=1), against the FP64 matvec, the SIMT tiles and the oracle,
 for even and odd orders, one and several right-hand sides, and the Burton-Miller operator."""
 import os
 
@@ -17,15 +18,19 @@ def rel(a, b):
 
 
 def make_plan(fm, mode, *args, **kw):
-    old = os.environ.get("FMMBEM_TENSOR_M2L")
-    os.environ["FMMBEM_TENSOR_M2L"] = mode
+    """The dense tensor-core passes (M2L, M2M and L2L) forced off ("0") or on ("1"), the
+    three-stage form off."""
+    env = {"FMMBEM_TENSOR_M2L": mode, "FMMBEM_TENSOR_M2M": mode, "FMMBEM_TC3": "0"}
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
     try:
         return fm.Plan(*args, **kw)
     finally:
-        if old is None:
-            del os.environ["FMMBEM_TENSOR_M2L"]
-        else:
-            os.environ["FMMBEM_TENSOR_M2L"] = old
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
 
 
 # (p = 16 at 1 kHz would leave the FP32 range in the coaxial tables: no mixed path there)
@@ -35,8 +40,10 @@ def test_tensor_m2l_matches_fp64_and_oracle(fm, oracle, p, k):
     kw = dict(k=k, depth=3, p_levels={2: p, 3: p}, rule=1, a=0.5, b=0.0, c=-1.0)
     plan = make_plan(fm, "1", V, F, **kw)
     assert all(plan.info.m2l_tensor[l] == 1 for l in (2, 3))
+    assert [plan.info.pass_dense[l] for l in (2, 3)] == [2, 7]
     simt = make_plan(fm, "0", V, F, **kw)
     assert not any(simt.info.m2l_tensor[l] for l in range(13))
+    assert not any(simt.info.pass_dense[l] for l in range(13))
     rng = np.random.default_rng(p)
     x = rng.standard_normal(plan.nf) + 1j * rng.standard_normal(plan.nf)
     y64 = plan.matvec(x, fm.FMM_FP64)
@@ -61,6 +68,9 @@ def test_tensor_m2l_on_the_81920_triangle_workload(fm):
     P2 = {2: 40, 3: 30, 4: 20, 5: 14, 6: 10}
     plan = make_plan(fm, "1", V, F, k=K2, depth=6, p_levels=P2, rule=0, a=0.5, b=0.0, c=-1.0)
     assert [plan.info.m2l_tensor[l] for l in range(2, 7)] == [0, 0, 1, 1, 1]
+    # M2M out of / L2L into levels 5 and 6 (orders 14 and 10 below 20 and 14) run dense too;
+    # level 4's parent has p = 30
+    assert [plan.info.pass_dense[l] for l in range(2, 7)] == [0, 0, 2, 7, 7]
     rng = np.random.default_rng(0)
     x = rng.standard_normal(plan.nf) + 1j * rng.standard_normal(plan.nf)
     y64 = plan.matvec(x, fm.FMM_FP64)
