@@ -1,5 +1,5 @@
 // M2L of the mixed path on the 5th-generation tensor cores (tcgen05.mma, kind::tf32) for the
-// levels whose translation operators are small enough to store densely (p <= 20, the levels
+// levels whose translation operators are small enough to store densely (p <= 16, the levels
 // that carry most translations).
 //
 // The translation of direction d is T_d = diag(e^{-i m' phi_d}) S_c diag(e^{i m phi_d}) (the RCR
@@ -47,7 +47,10 @@ constexpr int TC_AWARPS = 8;            // source-gather warps (2..9)
 constexpr int TC_EPI0 = 2 + TC_AWARPS;  // first epilogue warp
 constexpr int TC_EWARPS = 8;            // epilogue warps (10..17), two per TMEM lane quarter
 constexpr int TC_THREADS = 32 * (TC_EPI0 + TC_EWARPS);
-constexpr int TC_MAXP = 20;
+// orders up to 16: at p = 20 (K = 800) the dense form's rounding (FP32 accumulation of 300
+// split products per output) raised the iterations of the refined 64-column solve on the
+// 200,000-triangle head-like body from 48 to 56, which cost more than its faster M2L saved
+constexpr int TC_MAXP = 16;
 constexpr int TC_MTAB = TC_MAXP * TC_MAXP + 8;  // order m of every coefficient (int8), zero padded
 constexpr int TC_EPI_LD = 33;           // staging row stride (floats) of the epilogue
 constexpr size_t TC_SMEM_MAX = 232448;  // 227 KB of dynamic shared memory per CTA
@@ -790,15 +793,18 @@ static void td_free(Plan *P, TcDense &g)
     g = TcDense();
 }
 
-// For every pass whose source and destination orders are both <= 20 (M2L of a level, M2M
+// For every pass whose source and destination orders are both <= 16 (M2L of a level, M2M
 // into and L2L out of its parent level): build the dense split operators and keep the
 // tensor-core pass where it beats the SIMT tiles on this plan (4 timed runs each), else free
 // its tables.  FMMBEM_TENSOR_M2L (M2L) and FMMBEM_TENSOR_M2M (M2M and L2L) = 0 keep the SIMT
-// tiles, = 1 take the tensor cores wherever they apply.
+// tiles, = 1 take the tensor cores wherever they apply.  M2M and L2L stay on the SIMT tiles
+// unless FMMBEM_TENSOR_M2M is set: their dense form is twice as fast but about ten times
+// less accurate on the 81,920-triangle sphere (mixed against FP64 8.9e-7 against 7.7e-8),
+// which costs the refined solves more iterations than it saves.
 int tune_tc_dense(Plan *P)
 {
     const char *env_l = getenv("FMMBEM_TENSOR_M2L"), *env_m = getenv("FMMBEM_TENSOR_M2M");
-    const int mode_l = env_l ? atoi(env_l) : -1, mode_m = env_m ? atoi(env_m) : -1;
+    const int mode_l = env_l ? atoi(env_l) : -1, mode_m = env_m ? atoi(env_m) : 0;
     if (mode_l == 0 && mode_m == 0) return FMM_OK;
     if (!P->tc_err) {
         FMM_CUDA_TRY(dev_alloc(P, (void **)&P->tc_err, sizeof(int)));

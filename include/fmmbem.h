@@ -81,7 +81,7 @@ typedef struct {
     int m2l_columns[FMM_MAX_LEVEL + 1];  /* mixed path: M2L translations per CTA tile (0 without mixed tables) */
     int m2l_tensor[FMM_MAX_LEVEL + 1];   /* mixed path: 1 where the level's M2L runs on the tensor cores
                                             (tcgen05, split TF32, dense operators per class of directions; levels with
-                                            p <= 20 where plan-time timing found it faster, or all of them
+                                            p <= 16 where plan-time timing found it faster, or all of them
                                             with FMMBEM_TENSOR_M2L=1; none with FMMBEM_TENSOR_M2L=0) */
     int expansions_scaled;               /* mixed path: 1 where the FP32 expansions are kept scaled by degree
                                             (low k t, where the plain coaxial entries would leave the FP32
@@ -94,10 +94,11 @@ typedef struct {
                                             forms (FMMBEM_TC3=0: never, 1: wherever the order allows) */
     int pass_dense[FMM_MAX_LEVEL + 1];   /* mixed path: passes of level l run as one dense tensor-core GEMM
                                             per operator (tcgen05, split TF32; source and destination
-                                            orders <= 20), same bits as pass_tc3 (bit 1 = m2l_tensor);
-                                            chosen at plan creation by timing (FMMBEM_TENSOR_M2L for M2L,
-                                            FMMBEM_TENSOR_M2M for M2M and L2L: 0 never, 1 wherever the
-                                            orders allow) */
+                                            orders <= 16), same bits as pass_tc3 (bit 1 = m2l_tensor);
+                                            M2L chosen at plan creation by timing (FMMBEM_TENSOR_M2L=0:
+                                            never, 1: wherever the orders allow); M2M and L2L only with
+                                            FMMBEM_TENSOR_M2M=1 (about ten times the rounding error of
+                                            the SIMT form) */
 } fmm_info;
 
 typedef struct fmm_plan fmm_plan;
