@@ -155,7 +155,7 @@ def peaks():
 
 def ncu_traffic():
     """DRAM bytes of the translation passes per matvec (all launches of rcr_tile_kernel and
-    m2l_tc_kernel) from the committed ncu summary."""
+    tc_dense_kernel) from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "translation_passes_traffic_cfg2.md")
     if not os.path.exists(path):
         return None
@@ -328,7 +328,7 @@ def gpu_arm(args, world, rank, local):
     rcr_ms = float(np.mean(kernel_ms["translations"]))  # the M2M/M2L/L2L phase as a whole
     bf16_peak, hbm_peak, peak_kind = peaks()
     achieved_tflops = rcr_flops / (rcr_ms / 1e3) / 1e12
-    # the M2L levels on the tensor cores (m2l_tc_kernel): split-TF32 GEMMs over dense operators,
+    # the M2L levels on the tensor cores (tc_dense_kernel): split-TF32 GEMMs over dense operators,
     # 3 MMAs of 128 x Nmma x 8 per 8 of K for every 128 translations and output half
     tc_levels = [l for l in range(info.lmin, info.lmax + 1) if info.m2l_tensor[l]]
     tc = None
@@ -347,7 +347,7 @@ def gpu_arm(args, world, rank, local):
             ex += info.num_m2l[l] * nhalf * nch * 16 * 6 * nmma
         tc_ms = sum(float(np.mean(kernel_ms["m2l_l%d" % l])) for l in tc_levels)
         tc_alg = sum(info.num_m2l[l] * f_rcr(info.p_level[l]) for l in tc_levels)
-        tc = {"kernel": "m2l_tc_kernel (tcgen05.mma kind::tf32, split TF32, TMEM accumulators)", "levels": tc_levels,
+        tc = {"kernel": "tc_dense_kernel (tcgen05.mma kind::tf32, split TF32, TMEM accumulators)", "levels": tc_levels,
               "ms_per_matvec": tc_ms, "executed_tf32_flops": ex, "executed_tflops": ex / (tc_ms / 1e3) / 1e12,
               "tf32_peak_from_measured_bf16": bf16_peak / 2,
               "executed_frac_of_tf32": ex / (tc_ms / 1e3) / 1e12 / (bf16_peak / 2),
@@ -447,7 +447,7 @@ def gpu_arm(args, world, rank, local):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nf * 16, "d2h_bytes_per_step": nf * 16},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "tensor",
-                     "kernel": "translation passes: rcr_tile_kernel (M2M, L2L, M2L) + m2l_tc_kernel (M2L at levels %s)"
+                     "kernel": "translation passes: rcr_tile_kernel (M2M, L2L, M2L) + tc_dense_kernel (M2L at levels %s)"
                                % tc_levels,
                      "achieved": achieved_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
                      "frac": achieved_tflops / bf16_peak, "peak_source": peak_kind + " bf16 burst",
