@@ -1,6 +1,7 @@
-// M2L of the mixed path on the 5th-generation tensor cores (tcgen05.mma, kind::tf32) for the
-// levels whose translation operators are small enough to store densely (p <= 16, the levels
-// that carry most translations).
+// Batched translation passes of the mixed path on the 5th-generation tensor cores
+// (tcgen05.mma, kind::tf32) as dense operators: the M2L of the levels whose operators are small
+// enough to store densely (p <= 16, the levels that carry most translations) and, on request,
+// the M2M and L2L of those levels (one operator per octant).
 //
 // The translation of direction d is T_d = diag(e^{-i m' phi_d}) S_c diag(e^{i m phi_d}) (the RCR
 // product of translation.cu:1864-1961 with its azimuthal phases taken out), where S_c (p^2 x p^2
@@ -11,9 +12,9 @@
 //                                         B    = S_c embedded as a real 2p^2 x 2p^2 matrix,
 // k and o running over interleaved (re, im) parts, and the epilogue multiplies row t's outputs
 // by e^{-i m' phi} of its own direction.  Split TF32 (3 products hi*hi + hi*lo + lo*hi of
-// rounded 11-bit halves) gives FP32-level accuracy.
+// rounded 11-bit halves) gives close to FP32 accuracy.
 //
-// A persistent, warp-specialised kernel (one CTA per SM, 14 warps) runs over the tiles
+// A persistent, warp-specialised kernel (one CTA per SM, 18 warps) runs over the tiles
 // (128 translations x one output half):
 //   warp 0     issues the MMAs (one thread) into one of two TMEM accumulators (2 x 256 columns)
 //              and commits each K chunk to its stage's "empty" barrier, each tile to its
@@ -22,10 +23,10 @@
 //   warps 2-9  gather the source expansions, two threads per row (translation), each half of
 //              every 16-wide K chunk, apply the row's phases, split them into TF32 hi / lo and
 //              store them in the no-swizzle K-major core-matrix layout;
-//   warps 10-13 read a finished accumulator (tcgen05.ld, one TMEM lane quarter per warp), apply
-//              each row's phases, stage 32 columns at a time in shared memory and add them into
-//              the destination local expansions with coalesced FP32 atomics, overlapping the
-//              next tile's MMAs.
+//   warps 10-17 read a finished accumulator (tcgen05.ld; two warps per TMEM lane quarter, on
+//              alternate 32-column blocks), stage 32 columns at a time in shared memory, apply
+//              each row's phases and add them into the destination expansions with 16-byte FP32
+//              atomics, overlapping the next tile's MMAs.
 // Four shared-memory stages of KC = 16; every wait has a time limit, after which the thread sets
 // the plan's error flag and stops.  Where one output half's whole operator fits beside the A
 // stages (p <= 8), it stays resident instead: each CTA takes a contiguous range of tiles, warp 1
