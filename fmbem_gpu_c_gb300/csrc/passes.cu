@@ -118,10 +118,22 @@ __global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *
                            typename Cx<T>::t *__restrict__ Cm, int flip, int nf, int nb)
 {
     typedef typename Cx<T>::t C;
+    // the box's elements and their i k x_e, loaded once for the whole CTA, so that the loads of
+    // U below depend on shared memory only and can all be in flight together
+    constexpr int MAXE = 64;
+    __shared__ int s_e[MAXE];
+    __shared__ C s_x[MAXE];
     int b = blockIdx.x, ppl = pl * pl;
     x += (size_t)blockIdx.y * nf; // right-hand side blockIdx.y
     typename Cx<T>::t *out = Cm + ((size_t)b * gridDim.y + blockIdx.y) * ppl; // [box][rhs][p^2]
-    int s0 = leaf_beg[b], s1 = leaf_beg[b + 1];
+    const int s0 = leaf_beg[b], ne = leaf_beg[b + 1] - s0;
+    for (int j = threadIdx.x; j < ne && j < MAXE; j += blockDim.x) {
+        const int e = leaf_elem[s0 + j];
+        const double2 xe = x[e];
+        s_e[j] = e;
+        s_x[j] = mk2((T)(-k * xe.y), (T)(k * xe.x));  // i k x_e
+    }
+    __syncthreads();
     for (int i = threadIdx.x; i < ppl; i += blockDim.x) {
         int q = i;
         if (flip) {
@@ -130,11 +142,18 @@ __global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *
             q = n * n + n - m;
         }
         T ar = 0, ai = 0;
-        for (int s = s0; s < s1; s++) {
-            int e = leaf_elem[s];
-            double2 xe = x[e];
-            T xr = (T)(-k * xe.y), xi = (T)(k * xe.x); // i k x_e
-            C u = U[(size_t)e * ppl + q];
+#pragma unroll 4
+        for (int j = 0; j < ne && j < MAXE; j++) {
+            const C xe = s_x[j], u = U[(size_t)s_e[j] * ppl + q];
+            ar += xe.x * u.x - xe.y * u.y;
+            ai += xe.x * u.y + xe.y * u.x;
+        }
+        // boxes with more than MAXE elements (none at the usual leaf occupancy): the rest directly
+        for (int j = MAXE; j < ne; j++) {
+            const int e = leaf_elem[s0 + j];
+            const double2 xd = x[e];
+            const T xr = (T)(-k * xd.y), xi = (T)(k * xd.x);
+            const C u = U[(size_t)e * ppl + q];
             ar += xr * u.x - xi * u.y;
             ai += xr * u.y + xi * u.x;
         }
