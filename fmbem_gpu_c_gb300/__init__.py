@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libfmmbem.so")
 
 FMM_FP64 = 0
 FMM_MIXED = 1
+FMM_FLOAT2 = 2  # FP64 matvec with the M2L in float-float (the mixed solvers' residuals)
 RULE_GAUSS3 = 0
 RULE_DUNAVANT7 = 1
 MAX_LEVEL = 12

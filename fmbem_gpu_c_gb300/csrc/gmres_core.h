@@ -22,6 +22,7 @@
 #include "plan.h"
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 namespace fmm {
@@ -159,9 +160,18 @@ int gmres_core(Ops &o, const double2 *B, double2 *X, int R, const std::vector<do
     return FMM_OK;
 }
 
+// The precision of the refinement's residuals: the FP64 matvec with its M2L in float-float
+// (FMM_FLOAT2: about 48 bits, several times faster than FP64 on GB300; plain FP64 where a plan's
+// tables leave the FP32 exponent range), or plain FP64 with FMMBEM_FF_RESIDUAL=0.
+inline int residual_precision()
+{
+    const char *e = getenv("FMMBEM_FF_RESIDUAL");
+    return (e && atoi(e) == 0) ? FMM_FP64 : FMM_FLOAT2;
+}
+
 // Solve A X = B (o.b() -> o.x(), X holding the initial guess) for R columns at `precision`.
-// FMM_MIXED runs iterative refinement: FP64 residual B - A X, inner lockstep GMRES on the
-// mixed-precision matvec for the correction, X += D.
+// FMM_MIXED runs iterative refinement: residual B - A X in FP64 quality (residual_precision),
+// inner lockstep GMRES on the mixed-precision matvec for the correction, X += D.
 template <class Ops>
 int solve_core(Ops &o, int R, double tol, int maxit, int restart, int precision, std::vector<int> &iters,
                std::vector<double> &relres)
@@ -197,7 +207,7 @@ int solve_core(Ops &o, int R, double tol, int maxit, int restart, int precision,
             if ((st = o.copy(o.w(), o.b()))) return st;
         } else {
             o.active(need);
-            if ((st = o.matvec(o.x(), o.w(), FMM_FP64))) return st;
+            if ((st = o.matvec(o.x(), o.w(), residual_precision()))) return st;
             o.axpby(1.0, o.b(), -1.0, o.w());
         }
         o.active(std::vector<int>(R, 1));

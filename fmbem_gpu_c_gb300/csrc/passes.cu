@@ -1,5 +1,6 @@
 // The FMM matvec: P2M, M2M, M2L (+ fused L2L), L2P + near field.  Templated on the
-// arithmetic type: double for the plain path, float for the mixed-precision path.
+// arithmetic type: double for the plain path, float for the mixed-precision path, float-float
+// (ff.cuh) for the M2L of the FMM_FLOAT2 path.
 //
 // Every translation is rotation - coaxial - rotation (RCR) as in the reference
 // (transMatsVecsMul_SR_rcr, translation.cu:1864-1961): rotate by (phi, theta, 0), apply the
@@ -13,6 +14,7 @@
 // The mixed path runs the batched direction-grouped tiles of batched.cu, which add into the
 // expansions with FP32 atomics, so mixed results vary in the last bits from run to run.
 #include "plan.h"
+#include "ff.cuh"
 #include <algorithm>
 #include <vector>
 
@@ -23,6 +25,7 @@ __constant__ int c_dir_dist[NDIR];
 template <typename T> struct Cx;
 template <> struct Cx<double> { typedef double2 t; };
 template <> struct Cx<float> { typedef float2 t; };
+template <> struct Cx<ff> { typedef ff2 t; };
 
 __device__ __forceinline__ void decode_nm(int i, int &n, int &m)
 {
@@ -355,6 +358,120 @@ static int launch_m2l_level(Plan *P, int l, const char *tname)
     return FMM_OK;
 }
 
+// ---------------------------------------------------------------- float-float M2L (FMM_FLOAT2)
+__global__ void ff_from_real_kernel(const double *__restrict__ in, float2 *__restrict__ out, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const ff a = ff_from(in[i]);
+        out[i] = make_float2(a.hi, a.lo);
+    }
+}
+__global__ void ff_from_cplx_kernel(const double2 *__restrict__ in, float4 *__restrict__ out, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const ff a = ff_from(in[i].x), b = ff_from(in[i].y);
+        out[i] = make_float4(a.hi, a.lo, b.hi, b.lo);
+    }
+}
+__global__ void ff_to_cplx_kernel(const float4 *__restrict__ in, double2 *__restrict__ out, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 v = in[i];
+        out[i] = make_double2(ff_to(ff(v.x, v.y)), ff_to(ff(v.z, v.w)));
+    }
+}
+static unsigned ew_grid(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16); }
+
+// The float-float copies of the translation tables (rotations, phases, coaxial blocks) and
+// the expansions, made on first use.  Only where the FP32 exponent range
+// holds the plain tables (the mixed tables are built and not scaled by degree); elsewhere
+// FMM_FLOAT2 runs FMM_FP64.
+static int ensure_ff(Plan *P)
+{
+    if (P->ff_ready) return FMM_OK;
+    if (!P->opt.build_mixed || P->scaled || !P->U32) {
+        P->ff_ready = -1;
+        return FMM_OK;
+    }
+    const int pmax = P->pmax, rs = rot_size(pmax), w = 2 * pmax - 1;
+    const size_t nh = (size_t)(NDIR + 16) * rs, nph = (size_t)(NDIR + 16) * w;
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->Hall_ff, sizeof(float2) * nh));
+    FMM_CUDA_TRY(dev_alloc(P, (void **)&P->PHall_ff, sizeof(float4) * nph));
+    ff_from_real_kernel<<<ew_grid(nh), 256, 0, P->stream>>>(P->Hsr64, P->Hall_ff, nh);
+    ff_from_cplx_kernel<<<ew_grid(nph), 256, 0, P->stream>>>(P->PHsr64, P->PHall_ff, nph);
+    for (int l = P->lmin; l <= P->lmax; l++) {
+        LevelDev &L = P->lev[l];
+        const size_t ncs = (size_t)NDIST * coax_size(L.p), ne = (size_t)L.nb * L.p * L.p;
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Csr_ff, sizeof(float4) * ncs));
+        ff_from_cplx_kernel<<<ew_grid(ncs), 256, 0, P->stream>>>(L.Csr64, L.Csr_ff, ncs);
+        if (l > P->lmin) {
+            const size_t nrr = (size_t)coax_size(P->lev[l - 1].p);
+            FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Crr_ff, sizeof(float4) * nrr));
+            ff_from_cplx_kernel<<<ew_grid(nrr), 256, 0, P->stream>>>(L.Crr64, L.Crr_ff, nrr);
+        }
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Cm_ff, sizeof(float4) * ne));
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Dl_ff, sizeof(float4) * ne));
+    }
+    FMM_CUDA_TRY(cudaGetLastError());
+    P->ff_ready = 1;
+    return FMM_OK;
+}
+
+// The M2M of level l into level l - 1 in float-float (the parent-owned m2m_kernel).
+static int launch_m2m_level_ff(Plan *P, int l, const char *tname)
+{
+    static size_t m2m_set = 0;
+    const int pmax = P->pmax, rs = rot_size(pmax), w = 2 * pmax - 1;
+    int e = raise_smem_limit((const void *)m2m_kernel<ff>, 4 * (size_t)pmax * pmax * sizeof(ff2), &m2m_set);
+    if (e) return e;
+    LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
+    const ff *Hss = reinterpret_cast<const ff *>(P->Hall_ff) + (size_t)NDIR * rs;
+    const ff2 *PHss = reinterpret_cast<const ff2 *>(P->PHall_ff) + (size_t)NDIR * w;
+    const size_t sm = 4 * (size_t)PL.p * PL.p * sizeof(ff2);
+    timer_begin(P, tname);
+    m2m_kernel<ff><<<PL.nb, block_for(PL.p), sm, P->stream>>>(
+        PL.p, L.p, pmax, PL.child_beg, PL.child_list, L.octant, Hss, PHss, reinterpret_cast<const ff2 *>(L.Crr_ff),
+        reinterpret_cast<const ff2 *>(L.Cm_ff), reinterpret_cast<ff2 *>(PL.Cm_ff));
+    timer_end(P);
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
+// The M2L (+ fused L2L) of level l in float-float: the owner-computes m2l_kernel on the
+// float-float tables and expansions.
+static int launch_m2l_level_ff(Plan *P, int l, const char *tname)
+{
+    static size_t m2l_set = 0;
+    const int lmin = P->lmin, pmax = P->pmax, rs = rot_size(pmax), w = 2 * pmax - 1;
+    int e = raise_smem_limit((const void *)m2l_kernel<ff>, 4 * (size_t)pmax * pmax * sizeof(ff2), &m2l_set);
+    if (e) return e;
+    cudaStream_t st = P->stream;
+    LevelDev &L = P->lev[l];
+    const ff *Hall = reinterpret_cast<const ff *>(P->Hall_ff);
+    const ff2 *PHall = reinterpret_cast<const ff2 *>(P->PHall_ff);
+    const ff *Hsr = Hall, *Hrr = Hall + (size_t)(NDIR + 8) * rs;
+    const ff2 *PHsr = PHall, *PHrr = PHall + (size_t)(NDIR + 8) * w;
+    const ff2 *Csr = reinterpret_cast<const ff2 *>(L.Csr_ff);
+    const ff2 *Crr = l > lmin ? reinterpret_cast<const ff2 *>(L.Crr_ff) : nullptr;
+    const ff2 *Cm = reinterpret_cast<const ff2 *>(L.Cm_ff);
+    ff2 *Dl = reinterpret_cast<ff2 *>(L.Dl_ff);
+    const ff2 *Dpar = l > lmin ? reinterpret_cast<const ff2 *>(P->lev[l - 1].Dl_ff) : nullptr;
+    const int pp = l > lmin ? P->lev[l - 1].p : 0, pe = pp > L.p ? pp : L.p;
+    const size_t sm = 4 * (size_t)pe * pe * sizeof(ff2);
+    timer_begin(P, tname);
+    const int S = std::max(1, L.m2l_split);
+    ff2 *part = S > 1 ? reinterpret_cast<ff2 *>(P->m2l_part64) : nullptr;
+    m2l_kernel<ff><<<dim3(L.nb, S), block_for(pe), sm, st>>>(L.p, pmax, pp, L.sr_beg, L.sr_src, L.sr_dir, Hsr, PHsr, Csr,
+                                                               Cm, L.parent, L.octant, Hrr, PHrr, Crr, Dpar, Dl, part);
+    if (S > 1) {
+        const size_t n = (size_t)L.nb * L.p * L.p;
+        m2l_reduce_kernel<ff><<<(int)std::min<size_t>((n + 255) / 256, 152 * 8), 256, 0, st>>>(S, n, part, Dl);
+    }
+    timer_end(P);
+    FMM_CUDA_TRY(cudaGetLastError());
+    return FMM_OK;
+}
+
 static RcrPass make_pass(int p, int pin, int pout, int atomic, const float *H, int hstride, const float2 *PH,
                          int phstride, int phoff, const float2 *Cc, const float2 *src, float2 *dst, int nrhs, int nsrc,
                          int ndst)
@@ -518,8 +635,9 @@ static int translate32(Plan *P, int nrhs)
     return FMM_OK;
 }
 
+// ffm2l (T = double only): the M2L and its fused L2L in float-float (FMM_FLOAT2)
 template <typename T>
-static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, int nrhs)
+static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, int nrhs, bool ffm2l = false)
 {
     typedef typename Cx<T>::t C;
     const bool f64 = sizeof(T) == 8;
@@ -562,7 +680,7 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
         int e = translate32(P, nrhs);
         if (e) return e;
     }
-    for (int l = lmax; l > lmin && f64; l--) {
+    for (int l = lmax; l > lmin && f64 && !ffm2l; l--) {
         LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
         size_t sm = 4 * (size_t)PL.p * PL.p * sizeof(C);
         timer_begin(P, m2m_names[l]);
@@ -570,7 +688,25 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
                                                            PHss, Crr(l), Cm(l), Cm(l - 1));
         timer_end(P);
     }
-    for (int l = lmin; l <= lmax && f64; l++) {
+    if (f64 && ffm2l) {
+        // the leaf multipoles into float-float; M2M, M2L and L2L in float-float; the leaf locals
+        // back to FP64 for L2P
+        {
+            const size_t n = (size_t)LL.nb * LL.p * LL.p;
+            ff_from_cplx_kernel<<<ew_grid(n), 256, 0, st>>>(LL.Cm64, LL.Cm_ff, n);
+        }
+        for (int l = lmax; l > lmin; l--) {
+            int st = launch_m2m_level_ff(P, l, m2m_names[l]);
+            if (st) return st;
+        }
+        for (int l = lmin; l <= lmax; l++) {
+            int st = launch_m2l_level_ff(P, l, m2l_names[l]);
+            if (st) return st;
+        }
+        const size_t n = (size_t)LL.nb * LL.p * LL.p;
+        ff_to_cplx_kernel<<<ew_grid(n), 256, 0, st>>>(LL.Dl_ff, LL.Dl64, n);
+    }
+    for (int l = lmin; l <= lmax && f64 && !ffm2l; l++) {
         int st = launch_m2l_level<T>(P, l, m2l_names[l]);
         if (st) return st;
     }
@@ -684,8 +820,14 @@ int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpo
         if (st) return st;
         return run_matvec_t<float>(P, x, y, transpose, nrhs);
     }
+    bool ffm2l = false;
+    if (precision == FMM_FLOAT2) {
+        int st = ensure_ff(P);
+        if (st) return st;
+        ffm2l = P->ff_ready > 0;
+    }
     for (int r = 0; r < nrhs; r++) {
-        int st = run_matvec_t<double>(P, x + (size_t)r * P->nf, y + (size_t)r * P->nf, transpose, 1);
+        int st = run_matvec_t<double>(P, x + (size_t)r * P->nf, y + (size_t)r * P->nf, transpose, 1, ffm2l);
         if (st) return st;
     }
     return FMM_OK;

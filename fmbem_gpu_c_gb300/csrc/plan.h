@@ -96,6 +96,9 @@ struct LevelDev {
     short *sr_dir = nullptr;      // direction index 0..315
     long long num_sr = 0;
     double2 *Cm64 = nullptr, *Dl64 = nullptr;
+    // float-float M2L of the FP64 path (FMM_FLOAT2): coaxial tables and expansions, each
+    // complex entry as (re hi, re lo, im hi, im lo)
+    float4 *Csr_ff = nullptr, *Crr_ff = nullptr, *Cm_ff = nullptr, *Dl_ff = nullptr;
     float2 *Cm32 = nullptr, *Dl32 = nullptr;
     double2 *Csr64 = nullptr;     // NDIST coaxial (S|R) blocks at order p
     float2 *Csr32 = nullptr;
@@ -157,6 +160,9 @@ struct Plan {
     int graph_nrhs = 0, graph_seen = 0;
     int *tc_err = nullptr;        // set by a tensor-core pass when one of its waits gives up
     float2 *tc_ones = nullptr;    // phases of the tensor-core passes without phases (all 1)
+    float2 *Hall_ff = nullptr;    // float-float rotation tables (as the FP64 ones, (hi, lo) each)
+    float4 *PHall_ff = nullptr;   // float-float phases
+    int ff_ready = 0;             // 1 once the float-float tables exist, -1 where they cannot
     double2 *m2l_part64 = nullptr; // FP64 M2L partial sums of split levels [run][box][p^2]
     size_t device_bytes = 0;
     char mixed_note[160] = "plan was created without build_mixed";

@@ -606,7 +606,7 @@ static int scene_matvec_dev(Scene *S, const double2 *x, double2 *y, int precisio
             continue;
         }
         FMM_CUDA_TRY(cudaStreamWaitEvent(P->stream, fork, 0));
-        int e = run_matvec(P, x + S->off[i], y + S->off[i], FMM_FP64, 0, 1);
+        int e = run_matvec(P, x + S->off[i], y + S->off[i], precision == FMM_FLOAT2 ? FMM_FLOAT2 : FMM_FP64, 0, 1);
         if (e) return e;
         cudaEvent_t join = S->events[S->events.size() - 2 - i];
         FMM_CUDA_TRY(cudaEventRecord(join, P->stream));
