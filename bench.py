@@ -370,6 +370,21 @@ def gpu_arm(args, world, rank, local):
     torch.cuda.synchronize()
     rel_err = float((torch.linalg.norm(y - y64) / torch.linalg.norm(y64)).item())
     fp64_rate = 1.0 / float(np.median(t64))
+    # the FP64-quality matvec the refined solvers use for residuals (translations in float-float)
+    yff = torch.empty_like(x)
+    plan.matvec(x, fm.FMM_FLOAT2, out=yff)
+    torch.cuda.synchronize()
+    tff = []
+    for _ in range(3):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        plan.matvec(x, fm.FMM_FLOAT2, out=yff)
+        torch.cuda.synchronize()
+        tff.append(time.perf_counter() - a)
+    float2 = {"value": 1.0 / float(np.median(tff)), "unit": UNIT,
+              "rel_err_vs_fp64": float((torch.linalg.norm(yff - y64) / torch.linalg.norm(y64)).item()),
+              "note": "FMM_FLOAT2: M2M, M2L and L2L in float-float on the FP32 pipes, the rest FP64"}
 
     # batching path: NB columns in one mixed pass (device buffers), columns per second
     NB = 16
@@ -457,7 +472,7 @@ def gpu_arm(args, world, rank, local):
         "kernels_ms": {n: float(np.mean(v)) for n, v in kernel_ms.items()},
         "batched": batched,
         "fp64_plain": {"value": fp64_rate, "unit": UNIT, "mixed_speedup": value / world / fp64_rate,
-                       "mixed_vs_fp64_rel_err": rel_err},
+                       "mixed_vs_fp64_rel_err": rel_err, "float2": float2},
         "solve": solve,
         "head64": head64,
         "clocks": clk.summary(),
