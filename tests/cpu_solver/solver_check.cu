@@ -1,8 +1,9 @@
 // Host-only check of the lockstep GMRES and iterative refinement of gmres_core.h (no kernels,
 // no GPU): the solver runs over a column layout whose operator is a dense complex matrix per
-// column, applied on the host.  FMM_FP64 applies it in double precision; FMM_MIXED applies
-// the matrix rounded to float with float accumulation, so the refinement has the same kind
-// of noise floor as the mixed FMM.  One JSON line per case goes to stdout.
+// column, applied on the host.  FMM_FP64 and FMM_FLOAT2 (the FP64-quality matvec the
+// refinement's residuals use) apply it in double precision; FMM_MIXED applies the matrix
+// rounded to float with float accumulation, so the refinement has the same kind of noise
+// floor as the mixed FMM.  One JSON line per case goes to stdout.
 #include "../../fmbem_gpu_c_gb300/csrc/gmres_core.h"
 #include <complex>
 #include <cstdarg>
@@ -50,7 +51,7 @@ struct HostOps {
             }
             col_matvecs++;
             for (int i = 0; i < m; i++) {
-                if (precision == FMM_FP64) {
+                if (precision != FMM_MIXED) {
                     cd acc = 0;
                     for (int j = 0; j < m; j++) acc += A[c][(size_t)i * m + j] * cd(xv[o + j].x, xv[o + j].y);
                     yv[o + i] = make_double2(acc.real(), acc.imag());
