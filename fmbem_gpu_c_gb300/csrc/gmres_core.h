@@ -181,8 +181,9 @@ int solve_core(Ops &o, int R, double tol, int maxit, int restart, int precision,
     if ((st = o.norms(o.b(), bnorm))) return st;
     for (auto &b : bnorm) if (b == 0.0) b = 1.0;
     std::vector<double> tolv(R, tol);
-    if (precision == FMM_FP64)
-        return gmres_core(o, o.b(), o.x(), R, tolv, maxit, restart, FMM_FP64, bnorm, iters, relres);
+    // plain GMRES: FP64, or (FMM_FLOAT2) on the FP64-quality matvec with float-float translations
+    if (precision == FMM_FP64 || precision == FMM_FLOAT2)
+        return gmres_core(o, o.b(), o.x(), R, tolv, maxit, restart, precision, bnorm, iters, relres);
     iters.assign(R, 0);
     relres.assign(R, 0.0);
     std::vector<double> rn, itol(R);

@@ -718,7 +718,10 @@ static int solve_entry(Plan *P, const cuDoubleComplex *b, cuDoubleComplex *x, in
                        int precision, int *iters, double *relres)
 {
     if (!P || !b || !x || R < 1 || !(tol > 0) || maxit < 1 || restart < 1 || restart > 500) { fmm_set_error("invalid argument"); return FMM_ERR_ARG; }
-    if (precision != FMM_FP64 && precision != FMM_MIXED) { fmm_set_error("unknown precision"); return FMM_ERR_ARG; }
+    if (precision != FMM_FP64 && precision != FMM_MIXED && precision != FMM_FLOAT2) {
+        fmm_set_error("unknown precision");
+        return FMM_ERR_ARG;
+    }
     int st = ensure_gmres(P, restart, R);
     if (st) return st;
     size_t n = (size_t)P->nf * R;

@@ -852,7 +852,10 @@ extern "C" int fmm_scene_matvec(fmm_scene *scene, const cuDoubleComplex *x, cuDo
 {
     Scene *S = (Scene *)scene;
     if (!S || !x || !y) { fmm_set_error("fmm_scene_matvec: null argument"); return FMM_ERR_ARG; }
-    if (precision != FMM_FP64 && precision != FMM_MIXED) { fmm_set_error("unknown precision"); return FMM_ERR_ARG; }
+    if (precision != FMM_FP64 && precision != FMM_MIXED && precision != FMM_FLOAT2) {
+        fmm_set_error("unknown precision");
+        return FMM_ERR_ARG;
+    }
     FMM_CUDA_TRY(cudaSetDevice(S->device));
     bool xd = is_dev(x), yd = is_dev(y);
     const size_t bytes = sizeof(double2) * S->N;
@@ -879,7 +882,10 @@ extern "C" int fmm_scene_solve(fmm_scene *scene, const cuDoubleComplex *b, cuDou
         fmm_set_error("fmm_scene_solve: invalid argument");
         return FMM_ERR_ARG;
     }
-    if (precision != FMM_FP64 && precision != FMM_MIXED) { fmm_set_error("unknown precision"); return FMM_ERR_ARG; }
+    if (precision != FMM_FP64 && precision != FMM_MIXED && precision != FMM_FLOAT2) {
+        fmm_set_error("unknown precision");
+        return FMM_ERR_ARG;
+    }
     FMM_CUDA_TRY(cudaSetDevice(S->device));
     int st = ensure_scene_solver(S, restart);
     if (st) return st;

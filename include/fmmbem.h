@@ -49,7 +49,8 @@ typedef enum {
 /* FMM_FLOAT2: the FP64 matvec with its M2L translations (the bulk of its work) in float-float
  * arithmetic on the FP32 pipes (about 48 bits; GB300's FP64 rate is a 64th of its FP32 rate);
  * plans whose tables leave the FP32 exponent range run FMM_FP64 instead.  The mixed solvers'
- * residuals use it. */
+ * residuals use it; fmm_gmres / fmm_solve_batched / fmm_scene_solve with FMM_FLOAT2 run plain
+ * GMRES on it. */
 typedef enum { FMM_FP64 = 0, FMM_MIXED = 1, FMM_FLOAT2 = 2 } fmm_precision;
 typedef enum { FMM_RULE_GAUSS3 = 0, FMM_RULE_DUNAVANT7 = 1 } fmm_rule;
 

@@ -88,3 +88,19 @@ def test_refined_solve_with_float_float_residuals(fm):
     r = b - plan.matvec(x_ff, fm.FMM_FP64)
     assert np.linalg.norm(r) / np.linalg.norm(b) < 1.01e-9
     plan.close()
+
+
+def test_plain_gmres_on_the_float_float_matvec(fm):
+    """fmm_gmres with FMM_FLOAT2: plain GMRES on the FP64-quality matvec reaches the plain FP64
+    solution, and its reported residual is the true one."""
+    V, F = fm.icosphere(4, 0.1)
+    plan = fm.Plan(V, F, k=K2, depth=4, p_levels={2: 16, 3: 14, 4: 10}, rule=1, a=0.5, b=0.0, c=-1.0)
+    b = plan.plane_wave()
+    x2, it2, rr2, ok2 = plan.gmres(b, tol=1e-10, maxit=800, restart=60, precision=fm.FMM_FLOAT2)
+    x64, it64, rr64, ok64 = plan.gmres(b, tol=1e-10, maxit=800, restart=60, precision=fm.FMM_FP64)
+    assert ok2 and ok64
+    assert abs(it2 - it64) <= 2
+    assert rel(x2, x64) < 1e-9
+    r = b - plan.matvec(x2, fm.FMM_FP64)
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 1.01e-10
+    plan.close()
