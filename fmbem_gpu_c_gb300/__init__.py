@@ -37,7 +37,7 @@ class Options(ctypes.Structure):
                 ("a_re", ctypes.c_double), ("a_im", ctypes.c_double), ("b_re", ctypes.c_double),
                 ("b_im", ctypes.c_double), ("c_re", ctypes.c_double), ("c_im", ctypes.c_double),
                 ("build_mixed", ctypes.c_int), ("device", ctypes.c_int), ("alpha_re", ctypes.c_double),
-                ("alpha_im", ctypes.c_double)]
+                ("alpha_im", ctypes.c_double), ("deterministic", ctypes.c_int)]
 
 
 class Info(ctypes.Structure):
@@ -271,13 +271,14 @@ class Plan:
     """A solver plan for one mesh and wavenumber (``fmm_plan_create``)."""
 
     def __init__(self, V=None, F=None, k=1.0, depth=0, s=5, p_levels=None, eps=0.05, rule=RULE_GAUSS3,
-                 a=0.0, b=1.0, c=0.0, build_mixed=True, obj=None, device=0, alpha=0.0):
+                 a=0.0, b=1.0, c=0.0, build_mixed=True, obj=None, device=0, alpha=0.0, deterministic=False):
         o = default_options()
         o.k, o.depth, o.s, o.eps, o.rule = k, depth, s, eps, rule
         a, b, c, alpha = complex(a), complex(b), complex(c), complex(alpha)
         o.a_re, o.a_im, o.b_re, o.b_im, o.c_re, o.c_im = a.real, a.imag, b.real, b.imag, c.real, c.imag
         o.alpha_re, o.alpha_im = alpha.real, alpha.imag
         o.build_mixed = 1 if build_mixed else 0
+        o.deterministic = 1 if deterministic else 0
         o.device = device
         if p_levels is not None:
             for l, p in p_levels.items() if isinstance(p_levels, dict) else enumerate(p_levels):

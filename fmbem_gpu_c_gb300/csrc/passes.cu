@@ -334,7 +334,8 @@ static int launch_m2l_level(Plan *P, int l, const char *tname)
     const C *PHsr = f64 ? (const C *)P->PHsr64 : (const C *)P->PHsr32;
     const C *PHrr = f64 ? (const C *)P->PHrr64 : (const C *)P->PHrr32;
     const C *Csr = f64 ? (const C *)L.Csr64 : (const C *)L.Csr32;
-    const C *Crr = l > lmin ? (f64 ? (const C *)L.Crr64 : (const C *)L.Crr32) : nullptr;
+    // the fused L2L: FP64, or the FP32 table scaled for L2L (plans with scaled expansions)
+    const C *Crr = l > lmin ? (f64 ? (const C *)L.Crr64 : (const C *)(L.Crr32L ? L.Crr32L : L.Crr32)) : nullptr;
     const C *Cm = f64 ? (const C *)L.Cm64 : (const C *)L.Cm32;
     C *Dl = f64 ? (C *)L.Dl64 : (C *)L.Dl32;
     const C *Dpar = l > lmin ? (f64 ? (const C *)P->lev[l - 1].Dl64 : (const C *)P->lev[l - 1].Dl32) : nullptr;
@@ -342,9 +343,9 @@ static int launch_m2l_level(Plan *P, int l, const char *tname)
     int pe = pp > L.p ? pp : L.p;
     size_t sm = 4 * (size_t)pe * pe * sizeof(C);
     timer_begin(P, tname);
-    // FP64 levels with few boxes split each box's sources over S CTAs (P->m2l_split, sized at
-    // plan creation so that the level fills the GPU) and add the runs in a second pass
-    const int S = f64 ? std::max(1, L.m2l_split) : 1;
+    // levels with few boxes split each box's sources over S CTAs (P->m2l_split, sized at plan
+    // creation so that the level fills the GPU) and add the runs in a second pass
+    const int S = std::max(1, L.m2l_split);
     C *part = S > 1 ? (C *)P->m2l_part64 : nullptr;
     m2l_kernel<T><<<dim3(L.nb, S), block_for(pe), sm, st>>>(L.p, pmax, pp, L.sr_beg, L.sr_src, L.sr_dir, Hsr, PHsr, Csr,
                                                               Cm, L.parent, L.octant, Hrr, PHrr, Crr, Dpar, Dl, part);
@@ -641,6 +642,8 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
 {
     typedef typename Cx<T>::t C;
     const bool f64 = sizeof(T) == 8;
+    // owner-computes translations: the FP64 path, and the mixed path of deterministic plans
+    const bool owner = f64 || P->opt.deterministic;
     int lmin = P->lmin, lmax = P->lmax, pmax = P->pmax;
     cudaStream_t st = P->stream;
     {
@@ -676,11 +679,11 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
     p2m_kernel<T><<<dim3(LL.nb, nrhs), 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, transpose ? Rv : U, x, P->opt.k,
                                                      Cm(lmax), transpose, P->nf, LL.nb);
     timer_end(P);
-    if (!f64) {
+    if (!owner) {
         int e = translate32(P, nrhs);
         if (e) return e;
     }
-    for (int l = lmax; l > lmin && f64 && !ffm2l; l--) {
+    for (int l = lmax; l > lmin && owner && !ffm2l; l--) {
         LevelDev &L = P->lev[l], &PL = P->lev[l - 1];
         size_t sm = 4 * (size_t)PL.p * PL.p * sizeof(C);
         timer_begin(P, m2m_names[l]);
@@ -706,7 +709,7 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
         const size_t n = (size_t)LL.nb * LL.p * LL.p;
         ff_to_cplx_kernel<<<ew_grid(n), 256, 0, st>>>(LL.Dl_ff, LL.Dl64, n);
     }
-    for (int l = lmin; l <= lmax && f64 && !ffm2l; l++) {
+    for (int l = lmin; l <= lmax && owner && !ffm2l; l++) {
         int st = launch_m2l_level<T>(P, l, m2l_names[l]);
         if (st) return st;
     }
@@ -818,7 +821,13 @@ int run_matvec(Plan *P, const double2 *x, double2 *y, int precision, int transpo
         }
         int st = ensure_rhs32(P, nrhs);
         if (st) return st;
-        return run_matvec_t<float>(P, x, y, transpose, nrhs);
+        if (!P->opt.deterministic) return run_matvec_t<float>(P, x, y, transpose, nrhs);
+        // the owner-computes kernels take one right-hand side
+        for (int r = 0; r < nrhs; r++) {
+            st = run_matvec_t<float>(P, x + (size_t)r * P->nf, y + (size_t)r * P->nf, transpose, 1);
+            if (st) return st;
+        }
+        return FMM_OK;
     }
     bool ffm2l = false;
     if (precision == FMM_FLOAT2) {

@@ -103,7 +103,7 @@ static void free_plan(Plan *P)
     F(P->U64); F(P->Rv64); F(P->U32); F(P->Rv32); F(P->near_beg); F(P->near_col); F(P->near64); F(P->near32);
     F(P->nearT_beg); F(P->nearT_col); F(P->nearT64); F(P->nearT32);
     F(P->xbuf); F(P->ybuf);
-    F(P->gm_V); F(P->gm_w); F(P->gm_r); F(P->gm_x); F(P->gm_b); F(P->gm_d); F(P->gm_dev_h); F(P->gm_alpha);
+    F(P->gm_V); F(P->gm_w); F(P->gm_r); F(P->gm_x); F(P->gm_b); F(P->gm_d); F(P->gm_dev_h); F(P->gm_part); F(P->gm_alpha);
     if (P->timers_created)
         for (int i = 0; i < MAX_TIMERS; i++) { cudaEventDestroy(P->timers[i].beg); cudaEventDestroy(P->timers[i].end); }
     if (P->timers_created) {
@@ -492,9 +492,11 @@ extern "C" int fmm_last_timings(const fmm_plan *plan, const char **names, double
 // ---------------------------------------------------------------------------- batched BLAS-1
 // Column r of a batch of R vectors of length n; V holds Krylov vectors as [j][r][n].
 namespace fmm {
-// out[r * nvec + j] += conj(V_j,r) . W_r   (grid: x over n, y = j, z = r)
+// part[(r * nvec + j) * gridDim.x + block] = block's share of conj(V_j,r) . W_r   (grid: x over
+// n, y = j, z = r); bdot_sum_kernel adds the shares in block order, so that the dots (and
+// the solves built on them) do not depend on the schedule
 __global__ void bdot_kernel(const double2 *V, size_t vj, size_t vr, const double2 *W, size_t wr, int n, int nvec,
-                            double2 *out)
+                            double2 *part)
 {
     int j = blockIdx.y, r = blockIdx.z;
     const double2 *v = V + (size_t)j * vj + (size_t)r * vr, *w = W + (size_t)r * wr;
@@ -512,9 +514,19 @@ __global__ void bdot_kernel(const double2 *V, size_t vj, size_t vr, const double
         if (threadIdx.x < s) { sr[threadIdx.x] += sr[threadIdx.x + s]; si[threadIdx.x] += si[threadIdx.x + s]; }
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        atomicAdd(&out[(size_t)r * nvec + j].x, sr[0]);
-        atomicAdd(&out[(size_t)r * nvec + j].y, si[0]);
+    if (threadIdx.x == 0) part[((size_t)r * nvec + j) * gridDim.x + blockIdx.x] = make_double2(sr[0], si[0]);
+}
+
+__global__ void bdot_sum_kernel(const double2 *part, int nb, int m, double2 *out)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+        double ar = 0, ai = 0;
+        for (int b = 0; b < nb; b++) {
+            const double2 v = part[(size_t)q * nb + b];
+            ar += v.x;
+            ai += v.y;
+        }
+        out[q] = make_double2(ar, ai);
     }
 }
 
@@ -581,6 +593,9 @@ static int ensure_gmres(Plan *P, int restart, int R)
     FMM_CUDA_TRY(cudaMalloc(&P->gm_b, sizeof(double2) * n));
     FMM_CUDA_TRY(cudaMalloc(&P->gm_d, sizeof(double2) * n));
     FMM_CUDA_TRY(cudaMalloc(&P->gm_dev_h, sizeof(double2) * (size_t)R * (restart + 1)));
+    cudaFree(P->gm_part);
+    P->gm_part = nullptr;
+    FMM_CUDA_TRY(cudaMalloc(&P->gm_part, sizeof(double2) * (size_t)R * (restart + 1) * (BLAS_BLOCKS / 2)));
     FMM_CUDA_TRY(cudaMalloc(&P->gm_alpha, sizeof(double) * R));
     P->gm_restart = restart;
     P->gm_cols = R;
@@ -591,9 +606,10 @@ static int ensure_gmres(Plan *P, int restart, int R)
 static int bdots(Plan *P, const double2 *V, size_t vj, size_t vr, const double2 *W, size_t wr, int nvec, int R,
                  std::vector<double2> &out)
 {
-    FMM_CUDA_TRY(cudaMemsetAsync(P->gm_dev_h, 0, sizeof(double2) * (size_t)R * nvec, P->stream));
     dim3 grid(std::min(BLAS_BLOCKS / 2, (P->nf + 255) / 256), nvec, R);
-    bdot_kernel<<<grid, 256, 0, P->stream>>>(V, vj, vr, W, wr, P->nf, nvec, P->gm_dev_h);
+    bdot_kernel<<<grid, 256, 0, P->stream>>>(V, vj, vr, W, wr, P->nf, nvec, P->gm_part);
+    const int m = R * nvec;
+    bdot_sum_kernel<<<(m + 255) / 256, 256, 0, P->stream>>>(P->gm_part, (int)grid.x, m, P->gm_dev_h);
     out.resize((size_t)R * nvec);
     FMM_CUDA_TRY(cudaMemcpyAsync(out.data(), P->gm_dev_h, sizeof(double2) * out.size(), cudaMemcpyDeviceToHost, P->stream));
     FMM_CUDA_TRY(cudaStreamSynchronize(P->stream));

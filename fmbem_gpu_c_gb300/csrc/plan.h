@@ -180,6 +180,7 @@ struct Plan {
     // GMRES workspace
     double2 *gm_V = nullptr, *gm_w = nullptr, *gm_r = nullptr, *gm_x = nullptr, *gm_b = nullptr, *gm_d = nullptr;
     double2 *gm_dev_h = nullptr;
+    double2 *gm_part = nullptr;    // per-block shares of the solver's dot products
     double *gm_alpha = nullptr;
     int gm_restart = 0, gm_cols = 0; // workspace for restart length and right-hand sides
 };

@@ -72,6 +72,10 @@ typedef struct {
                                  degree-scaled coaxial entries exceed the FP32 range) */
     int device;               /* CUDA device ordinal */
     double alpha_re, alpha_im;/* Burton-Miller coupling alpha (0: the conventional operator) */
+    int deterministic;        /* FMM_MIXED without atomics: each destination box accumulates its
+                                 FP32 translations in one CTA (owner-computes, as the FP64 path),
+                                 one right-hand side after another, so that mixed results are
+                                 reproducible bit for bit; slower than the batched tiles */
 } fmm_options;
 
 typedef struct {
