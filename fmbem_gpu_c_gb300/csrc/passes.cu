@@ -115,26 +115,30 @@ __device__ void rcr_block(int p, int pmax, const T *__restrict__ H, const typena
 // flip = 0: C_b[n,m] = ik sum_e x_e U_e[n,m] (element moments of R_n^{-m}).
 // flip = 1 (transposed operator): the same with the table read at (n,-m); with U = Rv this
 // is the multipole expansion ik sum_i y_i R_n^{-m}(y_i - c) of point sources at centroids.
-template <typename T>
+// P2M of one leaf box (CTA) for a group of up to G right-hand sides (blockIdx.y): thread i takes
+// coefficient i; the box's elements and their i k x_e are staged in shared memory once, so that
+// the loads of U depend on shared memory only and can all be in flight together, and each U
+// entry serves the whole group.  Each column's sum runs in the same order whatever the group.
+template <typename T, int G>
 __global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *__restrict__ leaf_elem,
                            const typename Cx<T>::t *__restrict__ U, const double2 *__restrict__ x, double k,
-                           typename Cx<T>::t *__restrict__ Cm, int flip, int nf, int nb)
+                           typename Cx<T>::t *__restrict__ Cm, int flip, int nf, int nb, int nrhs)
 {
     typedef typename Cx<T>::t C;
-    // the box's elements and their i k x_e, loaded once for the whole CTA, so that the loads of
-    // U below depend on shared memory only and can all be in flight together
     constexpr int MAXE = 64;
     __shared__ int s_e[MAXE];
-    __shared__ C s_x[MAXE];
-    int b = blockIdx.x, ppl = pl * pl;
-    x += (size_t)blockIdx.y * nf; // right-hand side blockIdx.y
-    typename Cx<T>::t *out = Cm + ((size_t)b * gridDim.y + blockIdx.y) * ppl; // [box][rhs][p^2]
+    __shared__ C s_x[MAXE][G];
+    const int b = blockIdx.x, ppl = pl * pl, r0 = blockIdx.y * G, ng = min(G, nrhs - r0);
     const int s0 = leaf_beg[b], ne = leaf_beg[b + 1] - s0;
     for (int j = threadIdx.x; j < ne && j < MAXE; j += blockDim.x) {
         const int e = leaf_elem[s0 + j];
-        const double2 xe = x[e];
         s_e[j] = e;
-        s_x[j] = mk2((T)(-k * xe.y), (T)(k * xe.x));  // i k x_e
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            if (g >= ng) break;
+            const double2 xe = x[(size_t)(r0 + g) * nf + e];
+            s_x[j][g] = mk2((T)(-k * xe.y), (T)(k * xe.x));  // i k x_e
+        }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < ppl; i += blockDim.x) {
@@ -144,23 +148,38 @@ __global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *
             decode_nm(i, n, m);
             q = n * n + n - m;
         }
-        T ar = 0, ai = 0;
+        T ar[G], ai[G];
+#pragma unroll
+        for (int g = 0; g < G; g++) ar[g] = ai[g] = 0;
 #pragma unroll 4
         for (int j = 0; j < ne && j < MAXE; j++) {
-            const C xe = s_x[j], u = U[(size_t)s_e[j] * ppl + q];
-            ar += xe.x * u.x - xe.y * u.y;
-            ai += xe.x * u.y + xe.y * u.x;
+            const C u = U[(size_t)s_e[j] * ppl + q];
+#pragma unroll
+            for (int g = 0; g < G; g++) {
+                if (g >= ng) break;
+                const C xe = s_x[j][g];
+                ar[g] += xe.x * u.x - xe.y * u.y;
+                ai[g] += xe.x * u.y + xe.y * u.x;
+            }
         }
         // boxes with more than MAXE elements (none at the usual leaf occupancy): the rest directly
         for (int j = MAXE; j < ne; j++) {
             const int e = leaf_elem[s0 + j];
-            const double2 xd = x[e];
-            const T xr = (T)(-k * xd.y), xi = (T)(k * xd.x);
             const C u = U[(size_t)e * ppl + q];
-            ar += xr * u.x - xi * u.y;
-            ai += xr * u.y + xi * u.x;
+#pragma unroll
+            for (int g = 0; g < G; g++) {
+                if (g >= ng) break;
+                const double2 xd = x[(size_t)(r0 + g) * nf + e];
+                const T xr = (T)(-k * xd.y), xi = (T)(k * xd.x);
+                ar[g] += xr * u.x - xi * u.y;
+                ai[g] += xr * u.y + xi * u.x;
+            }
         }
-        out[i] = mk2(ar, ai);
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            if (g >= ng) break;
+            Cm[((size_t)b * nrhs + r0 + g) * ppl + i] = mk2(ar[g], ai[g]); // [box][rhs][p^2]
+        }
     }
 }
 
@@ -248,29 +267,39 @@ __global__ void m2l_reduce_kernel(int S, size_t n, const typename Cx<T>::t *__re
 }
 
 
-template <typename T>
+// L2P + near field + identity for element e (one warp) and a group of up to G right-hand sides
+// (blockIdx.y): the near row and the element's basis are loaded once for the group, the x
+// gathers and the local expansions per right-hand side.  Each column's sums run in the same
+// order whatever the group, so a column's result does not depend on nrhs.
+template <typename T, int G>
 __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_leaf, const typename Cx<T>::t *__restrict__ Dl,
                                 const typename Cx<T>::t *__restrict__ Rv, const int *__restrict__ near_beg,
                                 const int *__restrict__ near_col, const typename Cx<T>::t *__restrict__ nearv,
-                                const double2 *__restrict__ x, double2 a, double2 *__restrict__ y, int flip, int nb)
+                                const double2 *__restrict__ x, double2 a, double2 *__restrict__ y, int flip, int nb, int nrhs)
 {
     typedef typename Cx<T>::t C;
     int lane = threadIdx.x & 31;
     int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (e >= nf) return;
+    const int r0 = blockIdx.y * G, ng = min(G, nrhs - r0);
     int ppl = pl * pl;
-    x += (size_t)blockIdx.y * nf; // right-hand side blockIdx.y
-    y += (size_t)blockIdx.y * nf;
-    T ar = 0, ai = 0;
+    T ar[G], ai[G];
+#pragma unroll
+    for (int g = 0; g < G; g++) ar[g] = ai[g] = 0;
     for (int s = near_beg[e] + lane; s < near_beg[e + 1]; s += 32) {
-        C v = nearv[s];
-        double2 xd = x[near_col[s]];
-        T xr = (T)xd.x, xi = (T)xd.y;
-        ar += v.x * xr - v.y * xi;
-        ai += v.x * xi + v.y * xr;
+        const C v = nearv[s];
+        const int col = near_col[s];
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            if (g >= ng) break;
+            const double2 xd = x[(size_t)(r0 + g) * nf + col];
+            const T xr = (T)xd.x, xi = (T)xd.y;
+            ar[g] += v.x * xr - v.y * xi;
+            ai[g] += v.x * xi + v.y * xr;
+        }
     }
-    const C *D = Dl + ((size_t)elem_leaf[e] * gridDim.y + blockIdx.y) * ppl; // [box][rhs][p^2]
     const C *R = Rv + (size_t)e * ppl;
+    const size_t db = (size_t)elem_leaf[e] * nrhs; // [box][rhs][p^2]
     for (int i = lane; i < ppl; i += 32) {
         int q = i;
         if (flip) {
@@ -278,17 +307,28 @@ __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_lea
             decode_nm(i, n, m);
             q = n * n + n - m;
         }
-        C d = D[i], r = R[q];
-        ar += d.x * r.x - d.y * r.y;
-        ai += d.x * r.y + d.y * r.x;
+        const C r = R[q];
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            if (g >= ng) break;
+            const C d = Dl[(db + r0 + g) * ppl + i];
+            ar[g] += d.x * r.x - d.y * r.y;
+            ai[g] += d.x * r.y + d.y * r.x;
+        }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        ar += __shfl_xor_sync(0xffffffffu, ar, o);
-        ai += __shfl_xor_sync(0xffffffffu, ai, o);
-    }
-    if (lane == 0) {
-        double2 xe = x[e];
-        y[e] = make_double2(a.x * xe.x - a.y * xe.y + (double)ar, a.x * xe.y + a.y * xe.x + (double)ai);
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+        if (g >= ng) break;
+        T sr = ar[g], si = ai[g];
+        for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        if (lane == 0) {
+            const size_t k = (size_t)(r0 + g) * nf + e;
+            const double2 xe = x[k];
+            y[k] = make_double2(a.x * xe.x - a.y * xe.y + (double)sr, a.x * xe.y + a.y * xe.x + (double)si);
+        }
     }
 }
 
@@ -676,8 +716,12 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
     timer_begin(P, "p2m");
     // the transposed operator swaps the roles of the element moments and the centroid basis
     // (index-flipped), keeps every translation, and uses the transposed near-field matrix
-    p2m_kernel<T><<<dim3(LL.nb, nrhs), 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, transpose ? Rv : U, x, P->opt.k,
-                                                     Cm(lmax), transpose, P->nf, LL.nb);
+    if (nrhs == 1)
+        p2m_kernel<T, 1><<<dim3(LL.nb, 1), 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, transpose ? Rv : U, x, P->opt.k,
+                                                      Cm(lmax), transpose, P->nf, LL.nb, 1);
+    else
+        p2m_kernel<T, 8><<<dim3(LL.nb, (nrhs + 7) / 8), 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, transpose ? Rv : U, x,
+                                                                   P->opt.k, Cm(lmax), transpose, P->nf, LL.nb, nrhs);
     timer_end(P);
     if (!owner) {
         int e = translate32(P, nrhs);
@@ -716,9 +760,17 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
     timer_begin(P, "l2p_near");
     double2 a = make_double2(P->opt.a_re, P->opt.a_im);
     const C *nearT = f64 ? (const C *)P->nearT64 : (const C *)P->nearT32;
-    l2p_near_kernel<T><<<dim3((P->nf * 32 + 255) / 256, nrhs), 256, 0, st>>>(
-        P->nf, LL.p, P->elem_leaf, Dl(lmax), transpose ? U : Rv, transpose ? P->nearT_beg : P->near_beg,
-        transpose ? P->nearT_col : P->near_col, transpose ? nearT : nearv, x, a, y, transpose, LL.nb);
+    {
+        const int *nb_ = transpose ? P->nearT_beg : P->near_beg, *nc_ = transpose ? P->nearT_col : P->near_col;
+        const C *nv_ = transpose ? nearT : nearv, *rv_ = transpose ? U : Rv;
+        const unsigned gx = (unsigned)((P->nf * 32 + 255) / 256);
+        if (nrhs == 1)
+            l2p_near_kernel<T, 1><<<dim3(gx, 1), 256, 0, st>>>(P->nf, LL.p, P->elem_leaf, Dl(lmax), rv_, nb_, nc_, nv_, x, a,
+                                                            y, transpose, LL.nb, 1);
+        else
+            l2p_near_kernel<T, 8><<<dim3(gx, (nrhs + 7) / 8), 256, 0, st>>>(P->nf, LL.p, P->elem_leaf, Dl(lmax), rv_, nb_,
+                                                                         nc_, nv_, x, a, y, transpose, LL.nb, nrhs);
+    }
     timer_end(P);
     if (P->profiling) {
         cudaEventRecord(P->total.end, st);
