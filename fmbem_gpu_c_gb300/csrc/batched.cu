@@ -99,7 +99,7 @@ static __device__ __forceinline__ void rcr_tile(const RcrPass &ps, const int4 it
     float2 *sC = W + (size_t)pp * TC;
     float *sH = reinterpret_cast<float *>(sC + coax_size(p));
     const int cnt = it.z;
-    const float *Hg = ps.H + (size_t)it.x * ps.hstride;
+    const float *Hg = ps.H + (size_t)(ps.hrep ? ps.hrep[it.x] : it.x) * ps.hstride;
     const float2 *ph = ps.PH + (size_t)it.x * ps.phstride + ps.phoff;
     const float2 *Cg = ps.Cc + (size_t)it.w * coax_size(p);
     const float *H = SHC ? sH : Hg;

@@ -21,6 +21,7 @@
 namespace fmm {
 
 __constant__ int c_dir_dist[NDIR];
+__constant__ int c_dir_hrep[NDIR]; // direction -> the direction whose (identical) rotation table it reads
 
 template <typename T> struct Cx;
 template <> struct Cx<double> { typedef double2 t; };
@@ -243,7 +244,7 @@ __global__ void m2l_kernel(int p, int pmax, int pp, const int *__restrict__ sr_b
     }
     for (int s = sa; s < sb; s++) {
         int src = sr_src[s], dir = sr_dir[s];
-        rcr_block<T>(p, pmax, Hsr + (size_t)dir * rs, PHsr + (size_t)dir * w, Csr + (size_t)c_dir_dist[dir] * cs,
+        rcr_block<T>(p, pmax, Hsr + (size_t)c_dir_hrep[dir] * rs, PHsr + (size_t)dir * w, Csr + (size_t)c_dir_dist[dir] * cs,
                      Cm + (size_t)src * P2, p, sX, sW1, sW2, sY, p);
     }
     C *out = S > 1 ? part + ((size_t)c * gridDim.x + b) * P2 : Dl + (size_t)b * P2;
@@ -535,6 +536,7 @@ static RcrPass make_pass(int p, int pin, int pout, int atomic, const float *H, i
     ps.dst = dst;
     ps.items = nullptr;
     ps.g_src = ps.g_dst = nullptr;
+    ps.hrep = nullptr;
     return ps;
 }
 
@@ -546,6 +548,7 @@ RcrList *pass32_desc(Plan *P, int l, int which, int nrhs, RcrPass &ps)
     LevelDev &L = P->lev[l];
     if (which == PASS_M2L) {
         ps = make_pass(L.p, L.p, L.p, 1, P->Hsr32, rs, P->PHsr32, w, pmax - 1, L.Csr32, L.Cm32, L.Dl32, nrhs, L.nb, L.nb);
+        ps.hrep = P->hrep_dev;
         return &L.m2l;
     }
     if (l <= P->lmin) return nullptr;
@@ -833,9 +836,10 @@ int gen_dense_rcr(Plan *P, int l, int which, const int *keys, int nkeys, double2
     return FMM_OK;
 }
 
-int set_dir_dist(const int *dd)
+int set_dir_dist(const int *dd, const int *hrep)
 {
     FMM_CUDA_TRY(cudaMemcpyToSymbol(c_dir_dist, dd, sizeof(int) * NDIR));
+    FMM_CUDA_TRY(cudaMemcpyToSymbol(c_dir_hrep, hrep, sizeof(int) * NDIR));
     return FMM_OK;
 }
 

@@ -15,7 +15,7 @@
 #include <thread>
 
 namespace fmm {
-int set_dir_dist(const int *dd);
+int set_dir_dist(const int *dd, const int *hrep);
 }
 
 using namespace fmm;
@@ -97,7 +97,7 @@ static void free_plan(Plan *P)
             F(R->td.B); F(R->td.items); F(R->td.src); F(R->td.dst); F(R->td.dir);
         }
     }
-    F(P->tc_err); F(P->tc_ones); F(P->m2l_part64); F(P->Hall_ff); F(P->PHall_ff);
+    F(P->tc_err); F(P->tc_ones); F(P->hrep_dev); F(P->m2l_part64); F(P->Hall_ff); F(P->PHall_ff);
     F(P->Hsr64); F(P->PHsr64); F(P->Hsr32); F(P->PHsr32);
     F(P->V_dev); F(P->F_dev); F(P->elem_leaf); F(P->leaf_beg); F(P->leaf_elem);
     F(P->U64); F(P->Rv64); F(P->U32); F(P->Rv32); F(P->near_beg); F(P->near_col); F(P->near64); F(P->near32);
@@ -207,7 +207,9 @@ static int plan_create_impl(std::vector<double> &&V, std::vector<int> &&F, const
     CTRY(cudaMemcpy(P->F_dev, P->F.data(), sizeof(int) * P->F.size(), cudaMemcpyHostToDevice));
     CTRY(cudaMemcpy(P->elem_leaf, P->tree.elem_leaf.data(), sizeof(int) * nf, cudaMemcpyHostToDevice));
     TRY(gen_rotation_tables(P));
-    TRY(set_dir_dist(P->dir_dist));
+    TRY(set_dir_dist(P->dir_dist, P->dir_hrep));
+    CTRY(dev_alloc(P, (void **)&P->hrep_dev, sizeof(int) * NDIR));
+    CTRY(cudaMemcpy(P->hrep_dev, P->dir_hrep, sizeof(int) * NDIR, cudaMemcpyHostToDevice));
     TRY(build_lists(P));
     TRY(gen_coax_tables(P));
     for (int l = P->lmin; l <= P->lmax; l++) {

@@ -76,6 +76,7 @@ struct RcrPass {
     int p, pin, pout, atomic;        // RCR order, source order, destination order
     int nrhs, nsrc, ndst;            // right-hand sides; boxes per right-hand side in src and dst
     int hstride, phstride, phoff;    // per-direction strides of H and the phases; phase index m + phoff
+    const int *hrep;                 // M2L: direction -> the direction whose H table it reads (null: its own)
     const float *H;
     const float2 *PH;
     const float2 *Cc;                // coaxial blocks, item.w selects one (stride coax_size(p))
@@ -126,6 +127,9 @@ struct Plan {
     // direction tables
     int dir_slot[343];            // (dx+3)*49+(dy+3)*7+(dz+3) -> 0..315 or -1
     int dir_dist[NDIR];           // direction -> distance slot
+    int dir_hrep[NDIR];           // direction -> the first direction of equal polar angle, whose
+                                  // rotation table (bit-identical: the same acos(dz / |d|)) it reads
+    int *hrep_dev = nullptr;      // dir_hrep on the device
     double *Hsr64 = nullptr, *Hss64 = nullptr, *Hrr64 = nullptr; // real rotation coefficients at pmax
     float *Hsr32 = nullptr, *Hss32 = nullptr, *Hrr32 = nullptr;
     double2 *PHsr64 = nullptr, *PHss64 = nullptr, *PHrr64 = nullptr; // e^{i m phi}, m = -(pmax-1)..pmax-1

@@ -192,6 +192,7 @@ int gen_rotation_tables(Plan *P)
     int p = P->pmax, rs = rot_size(p), w = 2 * p - 1;
     std::vector<double> beta_sr(NDIR), phi_sr(NDIR), beta_ss(8), phi_ss(8), beta_rr(8), phi_rr(8);
     int idx = 0;
+    std::vector<int> polar_key(NDIR);  // (dz, dx^2 + dy^2) of each direction
     for (int s = 0; s < 343; s++) {
         int dx = s / 49 - 3, dy = (s / 7) % 7 - 3, dz = s % 7 - 3;
         if (std::abs(dx) <= 1 && std::abs(dy) <= 1 && std::abs(dz) <= 1) { P->dir_slot[s] = -1; continue; }
@@ -203,6 +204,12 @@ int gen_rotation_tables(Plan *P)
         int slot = -1;
         for (int q = 0; q < NDIST; q++) if (s2list[q] == s2) slot = q;
         P->dir_dist[idx] = slot;
+        // directions of equal dz and dx^2 + dy^2 have the same polar angle, so bit-identical
+        // rotation tables: all of them read the first one's, which keeps the tables in cache
+        P->dir_hrep[idx] = idx;
+        for (int q = 0; q < idx; q++)
+            if (polar_key[q] == (dz + 8) * 100 + dx * dx + dy * dy) { P->dir_hrep[idx] = q; break; }
+        polar_key[idx] = (dz + 8) * 100 + dx * dx + dy * dy;
         P->dir_slot[s] = idx++;
     }
     for (int o = 0; o < 8; o++) {
