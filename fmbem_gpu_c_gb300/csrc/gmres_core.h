@@ -161,8 +161,8 @@ int gmres_core(Ops &o, const double2 *B, double2 *X, int R, const std::vector<do
 }
 
 // The precision of the refinement's residuals: the FP64 matvec with its M2L in float-float
-// (FMM_FLOAT2: about 48 bits, several times faster than FP64 on GB300; plain FP64 where a plan's
-// tables leave the FP32 exponent range), or plain FP64 with FMMBEM_FF_RESIDUAL=0.
+// (FMM_FLOAT2: about 48 bits, about twice as fast as FP64 on GB300; plain FP64 where a plan has
+// no mixed tables), or plain FP64 with FMMBEM_FF_RESIDUAL=0.
 inline int residual_precision()
 {
     const char *e = getenv("FMMBEM_FF_RESIDUAL");

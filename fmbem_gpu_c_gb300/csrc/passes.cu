@@ -422,16 +422,60 @@ __global__ void ff_to_cplx_kernel(const float4 *__restrict__ in, double2 *__rest
         out[i] = make_double2(ff_to(ff(v.x, v.y)), ff_to(ff(v.z, v.w)));
     }
 }
+// the same for expansions [box][p^2] kept scaled by degree: entry i times ds[degree of i % ppl]
+__global__ void ff_from_cplx_deg_kernel(const double2 *__restrict__ in, float4 *__restrict__ out, size_t n, int ppl,
+                                        const double *__restrict__ ds)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        int deg, m;
+        decode_nm((int)(i % ppl), deg, m);
+        const double f = ds[deg];
+        const ff a = ff_from(in[i].x * f), b = ff_from(in[i].y * f);
+        out[i] = make_float4(a.hi, a.lo, b.hi, b.lo);
+    }
+}
+__global__ void ff_to_cplx_deg_kernel(const float4 *__restrict__ in, double2 *__restrict__ out, size_t n, int ppl,
+                                      const double *__restrict__ ds)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        int deg, m;
+        decode_nm((int)(i % ppl), deg, m);
+        const double f = ds[deg];
+        const float4 v = in[i];
+        out[i] = make_double2(ff_to(ff(v.x, v.y)) * f, ff_to(ff(v.z, v.w)) * f);
+    }
+}
 static unsigned ew_grid(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
+// nmat coaxial tables of order p (the layout of coax_off: block m, entry (n', n) at
+// (n - m)(p - m) + n' - m) with rows times row[n'] and columns times col[n], in float-float
+static std::vector<float4> ff_scaled_coax(const std::vector<double2> &in, int p, int nmat, const std::vector<double> &row,
+                                          const std::vector<double> &col)
+{
+    std::vector<float4> out(in.size());
+    const int cs = coax_size(p);
+    for (int q = 0; q < nmat; q++)
+        for (int m = 0; m < p; m++) {
+            const int sz = p - m, off = q * cs + coax_off(p, m);
+            for (int i = 0; i < sz * sz; i++) {
+                const int a = i % sz, b = i / sz;
+                const double f = row[m + a] * col[m + b], x = in[off + i].x * f, y = in[off + i].y * f;
+                const float xh = (float)x, yh = (float)y;
+                out[off + i] = make_float4(xh, (float)(x - (double)xh), yh, (float)(y - (double)yh));
+            }
+        }
+    return out;
+}
+
 // The float-float copies of the translation tables (rotations, phases, coaxial blocks) and
-// the expansions, made on first use.  Only where the FP32 exponent range
-// holds the plain tables (the mixed tables are built and not scaled by degree); elsewhere
-// FMM_FLOAT2 runs FMM_FP64.
+// the expansions, made on first use.  Where the FP32 mixed tables are built, the FP32 exponent
+// range holds them: plain, or scaled by degree as the FP32 ones (multipoles d_n M_n, locals
+// L_n / d_n, the coaxial tables scaled to match, the leaf expansions scaled on the way in and
+// out); elsewhere FMM_FLOAT2 runs FMM_FP64.
 static int ensure_ff(Plan *P)
 {
     if (P->ff_ready) return FMM_OK;
-    if (!P->opt.build_mixed || P->scaled || !P->U32) {
+    if (!P->opt.build_mixed || !P->U32) {
         P->ff_ready = -1;
         return FMM_OK;
     }
@@ -445,14 +489,43 @@ static int ensure_ff(Plan *P)
         LevelDev &L = P->lev[l];
         const size_t ncs = (size_t)NDIST * coax_size(L.p), ne = (size_t)L.nb * L.p * L.p;
         FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Csr_ff, sizeof(float4) * ncs));
-        ff_from_cplx_kernel<<<ew_grid(ncs), 256, 0, P->stream>>>(L.Csr64, L.Csr_ff, ncs);
-        if (l > P->lmin) {
-            const size_t nrr = (size_t)coax_size(P->lev[l - 1].p);
-            FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Crr_ff, sizeof(float4) * nrr));
-            ff_from_cplx_kernel<<<ew_grid(nrr), 256, 0, P->stream>>>(L.Crr64, L.Crr_ff, nrr);
+        if (l > P->lmin) FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Crr_ff, sizeof(float4) * coax_size(P->lev[l - 1].p)));
+        if (!P->scaled) {
+            ff_from_cplx_kernel<<<ew_grid(ncs), 256, 0, P->stream>>>(L.Csr64, L.Csr_ff, ncs);
+            if (l > P->lmin)
+                ff_from_cplx_kernel<<<ew_grid(coax_size(P->lev[l - 1].p)), 256, 0, P->stream>>>(
+                    L.Crr64, L.Crr_ff, coax_size(P->lev[l - 1].p));
+        } else {
+            // the scalings of the FP32 tables (gen_coax_tables): M2L 1/d^l both sides; M2M rows
+            // d^{l-1}, columns 1/d^l below the child order (0 above); L2L rows 1/d^l below the
+            // child order (0 above), columns d^{l-1}
+            const int pall = (int)P->dsc[l].size();
+            std::vector<double> inv(pall), up(pall, 0.0), down(pall, 0.0);
+            for (int n = 0; n < pall; n++) inv[n] = 1.0 / P->dsc[l][n];
+            for (int n = 0; n < L.p && n < pall; n++) up[n] = down[n] = inv[n];
+            std::vector<double2> h(ncs);
+            FMM_CUDA_TRY(cudaMemcpy(h.data(), L.Csr64, sizeof(double2) * ncs, cudaMemcpyDeviceToHost));
+            std::vector<float4> f = ff_scaled_coax(h, L.p, NDIST, inv, inv);
+            FMM_CUDA_TRY(cudaMemcpy(L.Csr_ff, f.data(), sizeof(float4) * ncs, cudaMemcpyHostToDevice));
+            if (l > P->lmin) {
+                const int pp = P->lev[l - 1].p;
+                const size_t nrr = coax_size(pp);
+                h.resize(nrr);
+                FMM_CUDA_TRY(cudaMemcpy(h.data(), L.Crr64, sizeof(double2) * nrr, cudaMemcpyDeviceToHost));
+                f = ff_scaled_coax(h, pp, 1, P->dsc[l - 1], up);
+                FMM_CUDA_TRY(cudaMemcpy(L.Crr_ff, f.data(), sizeof(float4) * nrr, cudaMemcpyHostToDevice));
+                f = ff_scaled_coax(h, pp, 1, down, P->dsc[l - 1]);
+                FMM_CUDA_TRY(dev_alloc(P, (void **)&L.CrrL_ff, sizeof(float4) * nrr));
+                FMM_CUDA_TRY(cudaMemcpy(L.CrrL_ff, f.data(), sizeof(float4) * nrr, cudaMemcpyHostToDevice));
+            }
         }
         FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Cm_ff, sizeof(float4) * ne));
         FMM_CUDA_TRY(dev_alloc(P, (void **)&L.Dl_ff, sizeof(float4) * ne));
+    }
+    if (P->scaled) {
+        const std::vector<double> &d = P->dsc[P->lmax];
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&P->dsc_leaf_dev, sizeof(double) * d.size()));
+        FMM_CUDA_TRY(cudaMemcpy(P->dsc_leaf_dev, d.data(), sizeof(double) * d.size(), cudaMemcpyHostToDevice));
     }
     FMM_CUDA_TRY(cudaGetLastError());
     P->ff_ready = 1;
@@ -494,7 +567,7 @@ static int launch_m2l_level_ff(Plan *P, int l, const char *tname)
     const ff *Hsr = Hall, *Hrr = Hall + (size_t)(NDIR + 8) * rs;
     const ff2 *PHsr = PHall, *PHrr = PHall + (size_t)(NDIR + 8) * w;
     const ff2 *Csr = reinterpret_cast<const ff2 *>(L.Csr_ff);
-    const ff2 *Crr = l > lmin ? reinterpret_cast<const ff2 *>(L.Crr_ff) : nullptr;
+    const ff2 *Crr = l > lmin ? reinterpret_cast<const ff2 *>(L.CrrL_ff ? L.CrrL_ff : L.Crr_ff) : nullptr;
     const ff2 *Cm = reinterpret_cast<const ff2 *>(L.Cm_ff);
     ff2 *Dl = reinterpret_cast<ff2 *>(L.Dl_ff);
     const ff2 *Dpar = l > lmin ? reinterpret_cast<const ff2 *>(P->lev[l - 1].Dl_ff) : nullptr;
@@ -743,7 +816,10 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
         // back to FP64 for L2P
         {
             const size_t n = (size_t)LL.nb * LL.p * LL.p;
-            ff_from_cplx_kernel<<<ew_grid(n), 256, 0, st>>>(LL.Cm64, LL.Cm_ff, n);
+            if (P->dsc_leaf_dev)
+                ff_from_cplx_deg_kernel<<<ew_grid(n), 256, 0, st>>>(LL.Cm64, LL.Cm_ff, n, LL.p * LL.p, P->dsc_leaf_dev);
+            else
+                ff_from_cplx_kernel<<<ew_grid(n), 256, 0, st>>>(LL.Cm64, LL.Cm_ff, n);
         }
         for (int l = lmax; l > lmin; l--) {
             int st = launch_m2m_level_ff(P, l, m2m_names[l]);
@@ -754,7 +830,10 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
             if (st) return st;
         }
         const size_t n = (size_t)LL.nb * LL.p * LL.p;
-        ff_to_cplx_kernel<<<ew_grid(n), 256, 0, st>>>(LL.Dl_ff, LL.Dl64, n);
+        if (P->dsc_leaf_dev)
+            ff_to_cplx_deg_kernel<<<ew_grid(n), 256, 0, st>>>(LL.Dl_ff, LL.Dl64, n, LL.p * LL.p, P->dsc_leaf_dev);
+        else
+            ff_to_cplx_kernel<<<ew_grid(n), 256, 0, st>>>(LL.Dl_ff, LL.Dl64, n);
     }
     for (int l = lmin; l <= lmax && owner && !ffm2l; l++) {
         int st = launch_m2l_level<T>(P, l, m2l_names[l]);

@@ -88,7 +88,7 @@ static void free_plan(Plan *P)
     for (int l = 0; l <= FMM_MAX_LEVEL + 1; l++) {
         LevelDev &L = P->lev[l];
         F(L.parent); F(L.octant); F(L.child_beg); F(L.child_list); F(L.sr_beg); F(L.sr_src); F(L.sr_dir);
-        F(L.Cm64); F(L.Dl64); F(L.Csr_ff); F(L.Crr_ff); F(L.Cm_ff); F(L.Dl_ff); F(L.Cm32); F(L.Dl32); F(L.Csr64); F(L.Csr32); F(L.Crr64); F(L.Crr32); F(L.Crr32L);
+        F(L.Cm64); F(L.Dl64); F(L.Csr_ff); F(L.Crr_ff); F(L.CrrL_ff); F(L.Cm_ff); F(L.Dl_ff); F(L.Cm32); F(L.Dl32); F(L.Csr64); F(L.Csr32); F(L.Crr64); F(L.Crr32); F(L.Crr32L);
         for (RcrList *R : {&L.m2l, &L.m2m, &L.l2l}) {
             F(R->items); F(R->src); F(R->dst);
             Tc3 &t = R->t3;
@@ -97,7 +97,7 @@ static void free_plan(Plan *P)
             F(R->td.B); F(R->td.items); F(R->td.src); F(R->td.dst); F(R->td.dir);
         }
     }
-    F(P->tc_err); F(P->tc_ones); F(P->hrep_dev); F(P->m2l_part64); F(P->Hall_ff); F(P->PHall_ff);
+    F(P->tc_err); F(P->tc_ones); F(P->hrep_dev); F(P->m2l_part64); F(P->Hall_ff); F(P->PHall_ff); F(P->dsc_leaf_dev);
     F(P->Hsr64); F(P->PHsr64); F(P->Hsr32); F(P->PHsr32);
     F(P->V_dev); F(P->F_dev); F(P->elem_leaf); F(P->leaf_beg); F(P->leaf_elem);
     F(P->U64); F(P->Rv64); F(P->U32); F(P->Rv32); F(P->near_beg); F(P->near_col); F(P->near64); F(P->near32);

@@ -100,6 +100,7 @@ struct LevelDev {
     // float-float M2L of the FP64 path (FMM_FLOAT2): coaxial tables and expansions, each
     // complex entry as (re hi, re lo, im hi, im lo)
     float4 *Csr_ff = nullptr, *Crr_ff = nullptr, *Cm_ff = nullptr, *Dl_ff = nullptr;
+    float4 *CrrL_ff = nullptr;    // the L2L's float-float table where the expansions are scaled
     float2 *Cm32 = nullptr, *Dl32 = nullptr;
     double2 *Csr64 = nullptr;     // NDIST coaxial (S|R) blocks at order p
     float2 *Csr32 = nullptr;
@@ -167,6 +168,7 @@ struct Plan {
     float2 *Hall_ff = nullptr;    // float-float rotation tables (as the FP64 ones, (hi, lo) each)
     float4 *PHall_ff = nullptr;   // float-float phases
     int ff_ready = 0;             // 1 once the float-float tables exist, -1 where they cannot
+    double *dsc_leaf_dev = nullptr; // degree scales d_n of the leaf level (plans with scaled expansions)
     double2 *m2l_part64 = nullptr; // FP64 M2L partial sums of split levels [run][box][p^2]
     size_t device_bytes = 0;
     char mixed_note[160] = "plan was created without build_mixed";

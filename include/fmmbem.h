@@ -47,8 +47,8 @@ typedef enum {
 } fmm_status;
 
 /* FMM_FLOAT2: the FP64 matvec with its M2L translations (the bulk of its work) in float-float
- * arithmetic on the FP32 pipes (about 48 bits; GB300's FP64 rate is a 64th of its FP32 rate);
- * plans whose tables leave the FP32 exponent range run FMM_FP64 instead.  The mixed solvers'
+ * arithmetic on the FP32 pipes (about 48 bits; GB300's FP64 rate is a 64th of its FP32 rate),
+ * degree-scaled where the plan's mixed tables are; plans without mixed tables run FMM_FP64.  The mixed solvers'
  * residuals use it; fmm_gmres / fmm_solve_batched / fmm_scene_solve with FMM_FLOAT2 run plain
  * GMRES on it. */
 typedef enum { FMM_FP64 = 0, FMM_MIXED = 1, FMM_FLOAT2 = 2 } fmm_precision;

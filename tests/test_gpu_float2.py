@@ -1,7 +1,7 @@
 """FMM_FLOAT2: the FP64 matvec with its M2L (and the L2L fused into it) in float-float
 arithmetic on the FP32 pipes, which the mixed solvers use for their residuals.  Against the
 plain FP64 matvec and the FP64 oracle, the transposed operator, Burton-Miller, a low-frequency
-plan (whose tables leave the FP32 range: FMM_FP64 runs instead) and the refined solve."""
+plan (degree-scaled tables and expansions) and the refined solve."""
 import os
 
 import numpy as np
@@ -52,14 +52,19 @@ def test_float2_with_burton_miller(fm):
     plan.close()
 
 
-def test_float2_falls_back_to_fp64_at_low_frequency(fm):
-    """p = 16 at 1 kHz: the coaxial (S|R) entries leave the FP32 range (the mixed path keeps
-    its expansions scaled by degree), so FMM_FLOAT2 is the plain FP64 matvec, bit for bit."""
+def test_float2_at_low_frequency_with_scaled_expansions(fm, oracle):
+    """p = 16 at 1 kHz: the coaxial (S|R) entries leave the FP32 range, so the float-float
+    translations run on degree-scaled tables and expansions, as the mixed path does."""
     V, F = fm.icosphere(3, 0.1)
     plan = fm.Plan(V, F, k=K1, depth=3, p_levels={2: 16, 3: 16}, rule=1, a=0.5, b=0.0, c=-1.0)
     assert plan.info.expansions_scaled == 1
-    x = np.random.default_rng(24).standard_normal(plan.nf) + 0j
-    assert np.array_equal(plan.matvec(x, fm.FMM_FLOAT2), plan.matvec(x, fm.FMM_FP64))
+    x = np.random.default_rng(24).standard_normal(plan.nf) + 1j * np.random.default_rng(25).standard_normal(plan.nf)
+    yff = plan.matvec(x, fm.FMM_FLOAT2)
+    assert np.isfinite(yff).all()
+    assert rel(yff, plan.matvec(x, fm.FMM_FP64)) < 1e-11
+    assert rel(plan.matvec_adjoint(x, fm.FMM_FLOAT2), plan.matvec_adjoint(x, fm.FMM_FP64)) < 1e-11
+    T = oracle.tree_for_fmm(V, F, depth=3)
+    assert rel(yff, oracle.FMM(V, F, K1, T, [16, 16], a=0.5, b=0.0, c=-1.0, rule=1).apply(x)) < 1e-10
     plan.close()
 
 
