@@ -120,10 +120,14 @@ __device__ void rcr_block(int p, int pmax, const T *__restrict__ H, const typena
 // coefficient i; the box's elements and their i k x_e are staged in shared memory once, so that
 // the loads of U depend on shared memory only and can all be in flight together, and each U
 // entry serves the whole group.  Each column's sum runs in the same order whatever the group.
+// With x32 given, the CTA also writes its elements' x in FP32 there (every element lies in one
+// leaf), for the gathers of the L2P + near-field pass: GB300 converts FP64 to FP32 at its FP64
+// rate, and the near field would otherwise convert each x once per near pair.
 template <typename T, int G>
 __global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *__restrict__ leaf_elem,
                            const typename Cx<T>::t *__restrict__ U, const double2 *__restrict__ x, double k,
-                           typename Cx<T>::t *__restrict__ Cm, int flip, int nf, int nb, int nrhs)
+                           typename Cx<T>::t *__restrict__ Cm, int flip, int nf, int nb, int nrhs,
+                           float2 *__restrict__ x32)
 {
     typedef typename Cx<T>::t C;
     constexpr int MAXE = 64;
@@ -131,14 +135,16 @@ __global__ void p2m_kernel(int pl, const int *__restrict__ leaf_beg, const int *
     __shared__ C s_x[MAXE][G];
     const int b = blockIdx.x, ppl = pl * pl, r0 = blockIdx.y * G, ng = min(G, nrhs - r0);
     const int s0 = leaf_beg[b], ne = leaf_beg[b + 1] - s0;
-    for (int j = threadIdx.x; j < ne && j < MAXE; j += blockDim.x) {
+    for (int j = threadIdx.x; j < ne; j += blockDim.x) {
         const int e = leaf_elem[s0 + j];
-        s_e[j] = e;
+        if (j < MAXE) s_e[j] = e;
 #pragma unroll
         for (int g = 0; g < G; g++) {
             if (g >= ng) break;
-            const double2 xe = x[(size_t)(r0 + g) * nf + e];
-            s_x[j][g] = mk2((T)(-k * xe.y), (T)(k * xe.x));  // i k x_e
+            const size_t k_e = (size_t)(r0 + g) * nf + e;
+            const double2 xe = x[k_e];
+            if (j < MAXE) s_x[j][g] = mk2((T)(-k * xe.y), (T)(k * xe.x));  // i k x_e
+            if (x32) x32[k_e] = make_float2((float)xe.x, (float)xe.y);
         }
     }
     __syncthreads();
@@ -271,12 +277,14 @@ __global__ void m2l_reduce_kernel(int S, size_t n, const typename Cx<T>::t *__re
 // L2P + near field + identity for element e (one warp) and a group of up to G right-hand sides
 // (blockIdx.y): the near row and the element's basis are loaded once for the group, the x
 // gathers and the local expansions per right-hand side.  Each column's sums run in the same
-// order whatever the group, so a column's result does not depend on nrhs.
+// order whatever the group, so a column's result does not depend on nrhs.  T = float gathers
+// the near field's x from x32, the FP32 copy P2M wrote (the same values as converting x here).
 template <typename T, int G>
 __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_leaf, const typename Cx<T>::t *__restrict__ Dl,
                                 const typename Cx<T>::t *__restrict__ Rv, const int *__restrict__ near_beg,
                                 const int *__restrict__ near_col, const typename Cx<T>::t *__restrict__ nearv,
-                                const double2 *__restrict__ x, double2 a, double2 *__restrict__ y, int flip, int nb, int nrhs)
+                                const double2 *__restrict__ x, const float2 *__restrict__ x32, double2 a,
+                                double2 *__restrict__ y, int flip, int nb, int nrhs)
 {
     typedef typename Cx<T>::t C;
     int lane = threadIdx.x & 31;
@@ -293,8 +301,16 @@ __global__ void l2p_near_kernel(int nf, int pl, const int *__restrict__ elem_lea
 #pragma unroll
         for (int g = 0; g < G; g++) {
             if (g >= ng) break;
-            const double2 xd = x[(size_t)(r0 + g) * nf + col];
-            const T xr = (T)xd.x, xi = (T)xd.y;
+            T xr, xi;
+            if constexpr (sizeof(T) == 4) {
+                const float2 xf = x32[(size_t)(r0 + g) * nf + col];
+                xr = xf.x;
+                xi = xf.y;
+            } else {
+                const double2 xd = x[(size_t)(r0 + g) * nf + col];
+                xr = xd.x;
+                xi = xd.y;
+            }
             ar[g] += v.x * xr - v.y * xi;
             ai[g] += v.x * xi + v.y * xr;
         }
@@ -784,6 +800,11 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
     const C *Rv = f64 ? (const C *)P->Rv64 : (const C *)P->Rv32;
     const C *nearv = f64 ? (const C *)P->near64 : (const C *)P->near32;
     LevelDev &LL = P->lev[lmax];
+    float2 *x32 = f64 ? nullptr : P->x32;
+    if (!f64 && (!x32 || P->x32_cap < nrhs)) {
+        fmm_set_error("mixed matvec: FP32 input buffer missing");
+        return FMM_ERR_CUDA;
+    }
 
     static const char *m2m_names[] = {"m2m_l0", "m2m_l1", "m2m_l2", "m2m_l3", "m2m_l4", "m2m_l5", "m2m_l6",
                                       "m2m_l7", "m2m_l8", "m2m_l9", "m2m_l10", "m2m_l11", "m2m_l12", "m2m_l13"};
@@ -794,10 +815,10 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
     // (index-flipped), keeps every translation, and uses the transposed near-field matrix
     if (nrhs == 1)
         p2m_kernel<T, 1><<<dim3(LL.nb, 1), 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, transpose ? Rv : U, x, P->opt.k,
-                                                      Cm(lmax), transpose, P->nf, LL.nb, 1);
+                                                      Cm(lmax), transpose, P->nf, LL.nb, 1, x32);
     else
         p2m_kernel<T, 8><<<dim3(LL.nb, (nrhs + 7) / 8), 128, 0, st>>>(LL.p, P->leaf_beg, P->leaf_elem, transpose ? Rv : U, x,
-                                                                   P->opt.k, Cm(lmax), transpose, P->nf, LL.nb, nrhs);
+                                                                   P->opt.k, Cm(lmax), transpose, P->nf, LL.nb, nrhs, x32);
     timer_end(P);
     if (!owner) {
         int e = translate32(P, nrhs);
@@ -847,11 +868,11 @@ static int run_matvec_t(Plan *P, const double2 *x, double2 *y, int transpose, in
         const C *nv_ = transpose ? nearT : nearv, *rv_ = transpose ? U : Rv;
         const unsigned gx = (unsigned)((P->nf * 32 + 255) / 256);
         if (nrhs == 1)
-            l2p_near_kernel<T, 1><<<dim3(gx, 1), 256, 0, st>>>(P->nf, LL.p, P->elem_leaf, Dl(lmax), rv_, nb_, nc_, nv_, x, a,
-                                                            y, transpose, LL.nb, 1);
+            l2p_near_kernel<T, 1><<<dim3(gx, 1), 256, 0, st>>>(P->nf, LL.p, P->elem_leaf, Dl(lmax), rv_, nb_, nc_, nv_, x, x32,
+                                                            a, y, transpose, LL.nb, 1);
         else
             l2p_near_kernel<T, 8><<<dim3(gx, (nrhs + 7) / 8), 256, 0, st>>>(P->nf, LL.p, P->elem_leaf, Dl(lmax), rv_, nb_,
-                                                                         nc_, nv_, x, a, y, transpose, LL.nb, nrhs);
+                                                                         nc_, nv_, x, x32, a, y, transpose, LL.nb, nrhs);
     }
     timer_end(P);
     if (P->profiling) {
@@ -925,6 +946,14 @@ int set_dir_dist(const int *dd, const int *hrep)
 // The FP32 expansions hold rhs_cap32 right-hand sides, level by level ([box][rhs][p^2]).
 static int ensure_rhs32(Plan *P, int nrhs)
 {
+    if (nrhs > P->x32_cap) {
+        cudaFree(P->x32);
+        P->x32 = nullptr;
+        P->device_bytes -= sizeof(float2) * (size_t)P->nf * P->x32_cap;
+        P->x32_cap = 0;
+        FMM_CUDA_TRY(dev_alloc(P, (void **)&P->x32, sizeof(float2) * (size_t)P->nf * nrhs));
+        P->x32_cap = nrhs;
+    }
     if (nrhs <= P->rhs_cap32) return FMM_OK;
     drop_graph(P); // the captured passes address the old expansions
     for (int l = P->lmin; l <= P->lmax; l++) {

@@ -102,7 +102,7 @@ static void free_plan(Plan *P)
     F(P->V_dev); F(P->F_dev); F(P->elem_leaf); F(P->leaf_beg); F(P->leaf_elem);
     F(P->U64); F(P->Rv64); F(P->U32); F(P->Rv32); F(P->near_beg); F(P->near_col); F(P->near64); F(P->near32);
     F(P->nearT_beg); F(P->nearT_col); F(P->nearT64); F(P->nearT32);
-    F(P->xbuf); F(P->ybuf);
+    F(P->xbuf); F(P->ybuf); F(P->x32);
     F(P->gm_V); F(P->gm_w); F(P->gm_r); F(P->gm_x); F(P->gm_b); F(P->gm_d); F(P->gm_dev_h); F(P->gm_part); F(P->gm_alpha);
     if (P->timers_created)
         for (int i = 0; i < MAX_TIMERS; i++) { cudaEventDestroy(P->timers[i].beg); cudaEventDestroy(P->timers[i].end); }

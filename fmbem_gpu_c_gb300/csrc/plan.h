@@ -154,6 +154,8 @@ struct Plan {
     double2 *xbuf = nullptr, *ybuf = nullptr;
     int nrhs_cap = 0;             // columns of xbuf / ybuf
     int rhs_cap32 = 1;            // right-hand sides the FP32 expansions (Cm32, Dl32) hold
+    float2 *x32 = nullptr;        // the mixed matvec's input in FP32 ([rhs][element]), written by P2M
+    int x32_cap = 0;              // columns of x32
     int buf_gen = 0;              // times Cm32 / Dl32 were reallocated (scenes hold their addresses)
     int scene_refs = 0;           // scenes built on this plan (it is not destroyed before them)
     cudaStream_t stream = nullptr;

@@ -90,6 +90,7 @@ struct Scene {
     int4 *chunks = nullptr;           // (plan, begin, end) over the scene vector for the BLAS
     int n_chunks = 0;
     double2 *xin = nullptr, *yout = nullptr;
+    float2 *xin32 = nullptr;          // xin in FP32, written by the P2M pass for the near-field gathers
     cudaGraphExec_t graph = nullptr;
     int calls = 0;
     // solver workspace
@@ -177,10 +178,15 @@ __global__ void __launch_bounds__(1024) scene_compact_kernel(const CompactJob *_
 }
 
 // C_b[n,m] = ik sum_e x_e U_e[n,m] for leaf box b of plan it.x (the plan's p2m_kernel for one
-// column in FP32)
+// column in FP32): the box's elements and their i k x_e staged in shared memory once per item,
+// and x_e in FP32 written to x32 for the near-field gathers of scene_l2p_kernel (every element
+// lies in one leaf box)
 __global__ void scene_p2m_kernel(const BodyDev *__restrict__ bodies, const int2 *__restrict__ items,
-                                 const int *__restrict__ nitems, const double2 *__restrict__ x)
+                                 const int *__restrict__ nitems, const double2 *__restrict__ x, float2 *__restrict__ x32)
 {
+    constexpr int MAXE = 64;
+    __shared__ int s_e[MAXE];
+    __shared__ float2 s_x[MAXE];
     const int n = *nitems;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const int2 it = items[w];
@@ -188,14 +194,32 @@ __global__ void scene_p2m_kernel(const BodyDev *__restrict__ bodies, const int2 
         const int b = it.y, ppl = bd.pl * bd.pl;
         float2 *out = bd.Cm + (size_t)b * ppl;
         const double2 *xb = x + bd.off;
-        const int s0 = bd.leaf_beg[b], s1 = bd.leaf_beg[b + 1];
+        const int s0 = bd.leaf_beg[b], ne = bd.leaf_beg[b + 1] - s0;
+        __syncthreads(); // the previous item's readers of s_e / s_x are done
+        for (int j = threadIdx.x; j < ne; j += blockDim.x) {
+            const int e = bd.leaf_elem[s0 + j];
+            const double2 xe = xb[e];
+            if (j < MAXE) {
+                s_e[j] = e;
+                s_x[j] = make_float2((float)(-bd.k * xe.y), (float)(bd.k * xe.x));
+            }
+            x32[bd.off + e] = make_float2((float)xe.x, (float)xe.y);
+        }
+        __syncthreads();
         for (int i = threadIdx.x; i < ppl; i += blockDim.x) {
             float ar = 0.f, ai = 0.f;
-            for (int s = s0; s < s1; s++) {
-                int e = bd.leaf_elem[s];
-                double2 xe = xb[e];
-                float xr = (float)(-bd.k * xe.y), xi = (float)(bd.k * xe.x);
-                float2 u = bd.U[(size_t)e * ppl + i];
+#pragma unroll 4
+            for (int j = 0; j < ne && j < MAXE; j++) {
+                const float2 xe = s_x[j];
+                const float2 u = bd.U[(size_t)s_e[j] * ppl + i];
+                ar += xe.x * u.x - xe.y * u.y;
+                ai += xe.x * u.y + xe.y * u.x;
+            }
+            for (int j = MAXE; j < ne; j++) {
+                const int e = bd.leaf_elem[s0 + j];
+                const double2 xe = xb[e];
+                const float xr = (float)(-bd.k * xe.y), xi = (float)(bd.k * xe.x);
+                const float2 u = bd.U[(size_t)e * ppl + i];
                 ar += xr * u.x - xi * u.y;
                 ai += xr * u.y + xi * u.x;
             }
@@ -205,15 +229,16 @@ __global__ void scene_p2m_kernel(const BodyDev *__restrict__ bodies, const int2 
 }
 
 static __device__ __forceinline__ void l2p_element(const BodyDev &bd, int e, const double2 *__restrict__ x,
-                                                   double2 *__restrict__ y)
+                                                   const float2 *__restrict__ x32, double2 *__restrict__ y)
 {
     const int lane = threadIdx.x & 31;
     const double2 *xb = x + bd.off;
+    const float2 *xb32 = x32 + bd.off;
     float ar = 0.f, ai = 0.f;
     for (int s = bd.near_beg[e] + lane; s < bd.near_beg[e + 1]; s += 32) {
-        float2 v = bd.nearv[s];
-        double2 xd = xb[bd.near_col[s]];
-        float xr = (float)xd.x, xi = (float)xd.y;
+        const float2 v = bd.nearv[s];
+        const float2 xf = xb32[bd.near_col[s]];
+        const float xr = xf.x, xi = xf.y;
         ar += v.x * xr - v.y * xi;
         ai += v.x * xi + v.y * xr;
     }
@@ -238,14 +263,15 @@ static __device__ __forceinline__ void l2p_element(const BodyDev &bd, int e, con
 // elements of one plan per item (the plan's l2p_near_kernel for one column), over the items of
 // the switched-on plans (y of the others is zeroed before)
 __global__ void scene_l2p_kernel(const BodyDev *__restrict__ bodies, const int2 *__restrict__ items,
-                                 const int *__restrict__ nitems, const double2 *__restrict__ x, double2 *__restrict__ y)
+                                 const int *__restrict__ nitems, const double2 *__restrict__ x,
+                                 const float2 *__restrict__ x32, double2 *__restrict__ y)
 {
     const int n = *nitems;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const int2 it = items[w];
         const BodyDev &bd = bodies[it.x];
         const int e = it.y + (threadIdx.x >> 5);
-        if (e < bd.nf) l2p_element(bd, e, x, y);
+        if (e < bd.nf) l2p_element(bd, e, x, x32, y);
     }
 }
 
@@ -487,6 +513,7 @@ static int build_scene(Scene *S)
         if ((st = upload(S, &S->jobs, jobs))) return st;
     }
     FMM_CUDA_TRY(salloc(S, &S->xin, sizeof(double2) * S->N));
+    FMM_CUDA_TRY(salloc(S, &S->xin32, sizeof(float2) * S->N));
     FMM_CUDA_TRY(salloc(S, &S->yout, sizeof(double2) * S->N));
     S->events.resize(2 * nphase * SCENE_SIDE + 2 * n + 2);
     for (cudaEvent_t &e : S->events) FMM_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -508,7 +535,8 @@ static int scene_translate(Scene *S)
     FMM_CUDA_TRY(cudaMemsetAsync(S->yout, 0, sizeof(double2) * S->N, st));
     const int ng = S->n_jobs - 2;
     if (S->n_p2m)
-        scene_p2m_kernel<<<std::min(S->n_p2m, 152 * 16), 128, 0, st>>>(S->bodies, S->p2m_items, S->counts + ng, S->xin);
+        scene_p2m_kernel<<<std::min(S->n_p2m, 152 * 16), 128, 0, st>>>(S->bodies, S->p2m_items, S->counts + ng, S->xin,
+                                                                      S->xin32);
     FMM_CUDA_TRY(cudaGetLastError());
     int ev = 0;
     for (auto &groups : S->phases) {
@@ -539,7 +567,7 @@ static int scene_translate(Scene *S)
     }
     if (S->n_l2p)
         scene_l2p_kernel<<<std::min(S->n_l2p, 152 * 8), 256, 0, st>>>(S->bodies, S->l2p_items, S->counts + ng + 1, S->xin,
-                                                                      S->yout);
+                                                                      S->xin32, S->yout);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
