@@ -78,6 +78,25 @@ __device__ __forceinline__ ff &operator+=(ff &a, ff b)
     return a;
 }
 
+// c + a b for the accumulations of the translations: TwoProd of the high parts with the two
+// cross products, then one TwoSum of the high parts with the low parts and the product's error
+// added without their own TwoSum (Dekker's "sloppy" addition, 15 FP32 instructions against 27
+// for the product and the accurate sum above).  Its error is bounded relative to |c| + |a b|,
+// not to |c + a b|: a sum of n such terms is accurate to about n 2^-47 of the sum of the terms'
+// magnitudes, the same form of bound as FP64 summation (n 2^-53).
+__device__ __forceinline__ ff ff_fma(ff a, ff b, ff c)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    float s, t;
+    ff_two_sum(c.hi, p, s, t);
+    t = __fadd_rn(t, __fadd_rn(c.lo, e));
+    ff_fast_two_sum(s, t, s, t);
+    return ff(s, t);
+}
+
 __device__ __forceinline__ ff2 mk2(ff a, ff b) { return ff2{a, b}; }
 
 // nearest float-float to a double, and back

@@ -17,6 +17,7 @@
 #include "ff.cuh"
 #include <algorithm>
 #include <vector>
+#include <type_traits>
 
 namespace fmm {
 
@@ -41,6 +42,17 @@ __device__ __forceinline__ float2 to_c(double2 v, float) { return make_float2((f
 __device__ __forceinline__ double2 to_c(double2 v, double) { return v; }
 __device__ __forceinline__ double2 to_d(float2 v) { return make_double2(v.x, v.y); }
 __device__ __forceinline__ double2 to_d(double2 v) { return v; }
+
+// acc += a b: as written for FP32 and FP64 (contracted to an FMA), the fused float-float
+// multiply-add for ff
+template <typename T>
+__device__ __forceinline__ void mac(T &acc, T a, T b)
+{
+    if constexpr (std::is_same<T, ff>::value)
+        acc = ff_fma(a, b, acc);
+    else
+        acc += a * b;
+}
 
 // One RCR translation by a whole CTA.  x has pin^2 entries (zero padded to p); the result
 // for n < pout is accumulated into sY.  H and ph are the direction's real rotation table
@@ -69,8 +81,8 @@ __device__ void rcr_block(int p, int pmax, const T *__restrict__ H, const typena
         for (int m = 0; m < w; m++) {
             T h = col[m * w];
             C v = sX[base + m];
-            ar += h * v.x;
-            ai += h * v.y;
+            mac(ar, h, v.x);
+            mac(ai, h, v.y);
         }
         sW1[i] = mk2(ar, ai);
     }
@@ -84,8 +96,15 @@ __device__ void rcr_block(int p, int pmax, const T *__restrict__ H, const typena
         for (int n = am; n < p; n++) {
             C c = col[(n - am) * sz];
             C v = sW1[n * n + n + m];
-            ar += c.x * v.x - c.y * v.y;
-            ai += c.x * v.y + c.y * v.x;
+            if constexpr (std::is_same<T, ff>::value) {
+                ar = ff_fma(c.x, v.x, ar);
+                ar = ff_fma(-c.y, v.y, ar);
+                ai = ff_fma(c.x, v.y, ai);
+                ai = ff_fma(c.y, v.x, ai);
+            } else {
+                ar += c.x * v.x - c.y * v.y;
+                ai += c.x * v.y + c.y * v.x;
+            }
         }
         sW2[i] = mk2(ar, ai);
     }
@@ -100,8 +119,8 @@ __device__ void rcr_block(int p, int pmax, const T *__restrict__ H, const typena
         for (int m = 0; m < w; m++) {
             T h = col[m * w];
             C v = sW2[base + m];
-            ar += h * v.x;
-            ai += h * v.y;
+            mac(ar, h, v.x);
+            mac(ai, h, v.y);
         }
         C e = ph[mp + off];
         // conj(e) * (ar + i ai)
