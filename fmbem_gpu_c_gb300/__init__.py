@@ -47,7 +47,7 @@ class Info(ctypes.Structure):
                 ("num_near", ctypes.c_longlong), ("device_bytes", ctypes.c_size_t), ("setup_seconds", ctypes.c_double),
                 ("m2l_columns", ctypes.c_int * (MAX_LEVEL + 1)), ("m2l_tensor", ctypes.c_int * (MAX_LEVEL + 1)),
                 ("expansions_scaled", ctypes.c_int), ("pass_tc3", ctypes.c_int * (MAX_LEVEL + 1)),
-                ("pass_dense", ctypes.c_int * (MAX_LEVEL + 1))]
+                ("pass_dense", ctypes.c_int * (MAX_LEVEL + 1)), ("pass_balanced", ctypes.c_int * (MAX_LEVEL + 1))]
 
 
 _lib = None

@@ -90,7 +90,17 @@ static __device__ __forceinline__ void cmac(float2 &acc, float2 c, float ar, flo
 // One tile: item it = (direction, first column, count, coaxial block) of pass ps, with the
 // CTA's dynamic shared memory smem4 and its column indices s_src / s_dst.  SHC also stages
 // the direction's rotation block and coaxial block in shared memory, after the two tiles.
-template <int TC, int CG, int R1, int R2, bool SHC>
+//
+// A stage lasts as long as its busiest thread.  The units of a stage are ordered by cost
+// (longest first); without BAL thread t takes units t, t + B, t + 2B, ... (B threads), which
+// leaves most threads idle while the few longest units finish when the units barely outnumber
+// the threads.  BAL takes them in boustrophedon order (t, 2B - 1 - t, 2B + t, ...), so a thread
+// that drew a long unit in one round draws a short one in the next, ranks the column groups
+// inside each cost class, and gives +m and -m of the coaxial stage units of their own; with
+// one-row units (R1 = R2 = 1) the busiest thread is within about 10 % of the average at
+// p = 20-40, against about 55 % above it.  Every output is still summed in the same order, so
+// the results do not depend on BAL, R1 or R2.
+template <int TC, int CG, int R1, int R2, bool SHC, bool BAL = false>
 static __device__ __forceinline__ void rcr_tile(const RcrPass &ps, const int4 it, float4 *smem4, int *s_src, int *s_dst)
 {
     const int p = ps.p, pp = p * p;
@@ -136,11 +146,14 @@ static __device__ __forceinline__ void rcr_tile(const RcrPass &ps, const int4 it
 
     // stage 1: W_n = H_n X_n, n < p; a unit is R1 rows x CG columns, longest blocks first
     constexpr int G = TC / CG, HC = CG / 2;
+    const int B = blockDim.x, tid = threadIdx.x;
     int U = 0;
     for (int n = 0; n < p; n++) U += (2 * n + R1) / R1;
-    for (int u = threadIdx.x; u < U * G; u += blockDim.x) {
-        const int g = u / U;
-        int n = p - 1, q = u - g * U;
+    for (int k = 0;; k++) {
+        const int u = k * B + ((BAL && (k & 1)) ? B - 1 - tid : tid);
+        if (u >= U * G) break;
+        const int g = BAL ? u % G : u / U;
+        int n = p - 1, q = BAL ? u / G : u - g * U;
         while (q >= (2 * n + R1) / R1) {
             q -= (2 * n + R1) / R1;
             n--;
@@ -161,58 +174,112 @@ static __device__ __forceinline__ void rcr_tile(const RcrPass &ps, const int4 it
 
     // stage 2: X_{+-m} = C_|m| W_{+-m} for the rows n' < nq (the ones stage 3 reads)
     const int nq = min(ps.pout, p);
-    U = 0;
-    for (int am = 0; am < nq; am++) U += (nq - am + R2 - 1) / R2;
-    for (int u = threadIdx.x; u < U * G; u += blockDim.x) {
-        const int g = u / U;
-        int am = 0, q = u - g * U;
-        while (q >= (nq - am + R2 - 1) / R2) {
-            q -= (nq - am + R2 - 1) / R2;
-            am++;
-        }
-        const int sz = p - am, nrow = nq - am, j0 = q * R2;
-        const float2 *Cb = Cc + coax_off(p, am);
-        float2 accP[R2][CG], accM[R2][CG];
-#pragma unroll
-        for (int k = 0; k < R2; k++)
-#pragma unroll
-            for (int t = 0; t < CG; t++) accP[k][t] = accM[k][t] = make_float2(0.f, 0.f);
-        float2 cn[R2];
-#pragma unroll
-        for (int k = 0; k < R2; k++) cn[k] = (j0 + k < nrow) ? Cb[j0 + k] : make_float2(0.f, 0.f);
-        for (int j = 0; j < sz; j++) {
-            float2 c[R2];
-#pragma unroll
-            for (int k = 0; k < R2; k++) {
-                c[k] = cn[k];
-                cn[k] = (j + 1 < sz && j0 + k < nrow) ? Cb[(j + 1) * sz + j0 + k] : make_float2(0.f, 0.f);
+    if constexpr (!BAL) {
+        U = 0;
+        for (int am = 0; am < nq; am++) U += (nq - am + R2 - 1) / R2;
+        for (int u = threadIdx.x; u < U * G; u += blockDim.x) {
+            const int g = u / U;
+            int am = 0, q = u - g * U;
+            while (q >= (nq - am + R2 - 1) / R2) {
+                q -= (nq - am + R2 - 1) / R2;
+                am++;
             }
-            const int n = am + j, rp = n * n + n + am, rm = n * n + n - am;
+            const int sz = p - am, nrow = nq - am, j0 = q * R2;
+            const float2 *Cb = Cc + coax_off(p, am);
+            float2 accP[R2][CG], accM[R2][CG];
 #pragma unroll
-            for (int cc = 0; cc < HC; cc++) {
-                float4 a = *chunk<TC>(W, rp, g * HC + cc), b = *chunk<TC>(W, rm, g * HC + cc);
+            for (int k = 0; k < R2; k++)
+#pragma unroll
+                for (int t = 0; t < CG; t++) accP[k][t] = accM[k][t] = make_float2(0.f, 0.f);
+            float2 cn[R2];
+#pragma unroll
+            for (int k = 0; k < R2; k++) cn[k] = (j0 + k < nrow) ? Cb[j0 + k] : make_float2(0.f, 0.f);
+            for (int j = 0; j < sz; j++) {
+                float2 c[R2];
 #pragma unroll
                 for (int k = 0; k < R2; k++) {
-                    cmac(accP[k][2 * cc], c[k], a.x, a.y);
-                    cmac(accP[k][2 * cc + 1], c[k], a.z, a.w);
-                    cmac(accM[k][2 * cc], c[k], b.x, b.y);
-                    cmac(accM[k][2 * cc + 1], c[k], b.z, b.w);
+                    c[k] = cn[k];
+                    cn[k] = (j + 1 < sz && j0 + k < nrow) ? Cb[(j + 1) * sz + j0 + k] : make_float2(0.f, 0.f);
                 }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < R2; k++)
-            if (j0 + k < nrow) {
-                const int np = am + j0 + k;
+                const int n = am + j, rp = n * n + n + am, rm = n * n + n - am;
 #pragma unroll
                 for (int cc = 0; cc < HC; cc++) {
-                    *chunk<TC>(X, np * np + np + am, g * HC + cc) =
-                        make_float4(accP[k][2 * cc].x, accP[k][2 * cc].y, accP[k][2 * cc + 1].x, accP[k][2 * cc + 1].y);
-                    if (am > 0)
-                        *chunk<TC>(X, np * np + np - am, g * HC + cc) = make_float4(
-                            accM[k][2 * cc].x, accM[k][2 * cc].y, accM[k][2 * cc + 1].x, accM[k][2 * cc + 1].y);
+                    float4 a = *chunk<TC>(W, rp, g * HC + cc), b = *chunk<TC>(W, rm, g * HC + cc);
+#pragma unroll
+                    for (int k = 0; k < R2; k++) {
+                        cmac(accP[k][2 * cc], c[k], a.x, a.y);
+                        cmac(accP[k][2 * cc + 1], c[k], a.z, a.w);
+                        cmac(accM[k][2 * cc], c[k], b.x, b.y);
+                        cmac(accM[k][2 * cc + 1], c[k], b.z, b.w);
+                    }
                 }
             }
+#pragma unroll
+            for (int k = 0; k < R2; k++)
+                if (j0 + k < nrow) {
+                    const int np = am + j0 + k;
+#pragma unroll
+                    for (int cc = 0; cc < HC; cc++) {
+                        *chunk<TC>(X, np * np + np + am, g * HC + cc) =
+                            make_float4(accP[k][2 * cc].x, accP[k][2 * cc].y, accP[k][2 * cc + 1].x, accP[k][2 * cc + 1].y);
+                        if (am > 0)
+                            *chunk<TC>(X, np * np + np - am, g * HC + cc) = make_float4(
+                                accM[k][2 * cc].x, accM[k][2 * cc].y, accM[k][2 * cc + 1].x, accM[k][2 * cc + 1].y);
+                    }
+                }
+        }
+    } else {
+        // units (|m|, row block, sign, column group), |m| ascending = cost descending
+        U = 0;
+        for (int am = 0; am < nq; am++) U += (am > 0 ? 2 : 1) * ((nq - am + R2 - 1) / R2);
+        for (int k = 0;; k++) {
+            const int u = k * B + ((k & 1) ? B - 1 - tid : tid);
+            if (u >= U * G) break;
+            const int g = u % G;
+            int am = 0, q = u / G;
+            while (q >= (am > 0 ? 2 : 1) * ((nq - am + R2 - 1) / R2)) {
+                q -= (am > 0 ? 2 : 1) * ((nq - am + R2 - 1) / R2);
+                am++;
+            }
+            const int sg = am > 0 ? (q & 1) : 0, m = sg ? -am : am;
+            const int sz = p - am, nrow = nq - am, j0 = (am > 0 ? q >> 1 : q) * R2;
+            const float2 *Cb = Cc + coax_off(p, am);
+            float2 acc[R2][CG];
+#pragma unroll
+            for (int r = 0; r < R2; r++)
+#pragma unroll
+                for (int t = 0; t < CG; t++) acc[r][t] = make_float2(0.f, 0.f);
+            float2 cn[R2];
+#pragma unroll
+            for (int r = 0; r < R2; r++) cn[r] = (j0 + r < nrow) ? Cb[j0 + r] : make_float2(0.f, 0.f);
+            for (int j = 0; j < sz; j++) {
+                float2 c[R2];
+#pragma unroll
+                for (int r = 0; r < R2; r++) {
+                    c[r] = cn[r];
+                    cn[r] = (j + 1 < sz && j0 + r < nrow) ? Cb[(j + 1) * sz + j0 + r] : make_float2(0.f, 0.f);
+                }
+                const int n = am + j, row = n * n + n + m;
+#pragma unroll
+                for (int cc = 0; cc < HC; cc++) {
+                    const float4 a = *chunk<TC>(W, row, g * HC + cc);
+#pragma unroll
+                    for (int r = 0; r < R2; r++) {
+                        cmac(acc[r][2 * cc], c[r], a.x, a.y);
+                        cmac(acc[r][2 * cc + 1], c[r], a.z, a.w);
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < R2; r++)
+                if (j0 + r < nrow) {
+                    const int np = am + j0 + r;
+#pragma unroll
+                    for (int cc = 0; cc < HC; cc++)
+                        *chunk<TC>(X, np * np + np + m, g * HC + cc) =
+                            make_float4(acc[r][2 * cc].x, acc[r][2 * cc].y, acc[r][2 * cc + 1].x, acc[r][2 * cc + 1].y);
+                }
+        }
     }
     __syncthreads();
 
@@ -220,9 +287,11 @@ static __device__ __forceinline__ void rcr_tile(const RcrPass &ps, const int4 it
     const int po2 = ps.pout * ps.pout;
     U = 0;
     for (int n = 0; n < nq; n++) U += (2 * n + R1) / R1;
-    for (int u = threadIdx.x; u < U * G; u += blockDim.x) {
-        const int g = u / U;
-        int n = nq - 1, q = u - g * U;
+    for (int k = 0;; k++) {
+        const int u = k * B + ((BAL && (k & 1)) ? B - 1 - tid : tid);
+        if (u >= U * G) break;
+        const int g = BAL ? u % G : u / U;
+        int n = nq - 1, q = BAL ? u / G : u - g * U;
         while (q >= (2 * n + R1) / R1) {
             q -= (2 * n + R1) / R1;
             n--;
@@ -253,12 +322,12 @@ static __device__ __forceinline__ void rcr_tile(const RcrPass &ps, const int4 it
     }
 }
 
-template <int TC, int CG, int R1, int R2, bool SHC>
+template <int TC, int CG, int R1, int R2, bool SHC, bool BAL = false>
 __global__ void __launch_bounds__(256, 2) rcr_tile_kernel(RcrPass ps)
 {
     extern __shared__ float4 smem4[];
     __shared__ int s_src[TC], s_dst[TC];
-    rcr_tile<TC, CG, R1, R2, SHC>(ps, ps.items[blockIdx.x], smem4, s_src, s_dst);
+    rcr_tile<TC, CG, R1, R2, SHC, BAL>(ps, ps.items[blockIdx.x], smem4, s_src, s_dst);
 }
 
 // Persistent form for many passes at once (the translation passes of many plans, one phase
@@ -291,13 +360,13 @@ size_t rcr_tile_smem(int p, int tc, int shc)
     return s;
 }
 
-template <int TC, int CG, int R1, int R2, bool SHC>
+template <int TC, int CG, int R1, int R2, bool SHC, bool BAL = false>
 static int launch_tile(const RcrPass &ps, int n_items, size_t sm, cudaStream_t st)
 {
     static size_t attr = 0;
-    int e = raise_smem_limit((const void *)rcr_tile_kernel<TC, CG, R1, R2, SHC>, sm, &attr);
+    int e = raise_smem_limit((const void *)rcr_tile_kernel<TC, CG, R1, R2, SHC, BAL>, sm, &attr);
     if (e) return e;
-    rcr_tile_kernel<TC, CG, R1, R2, SHC><<<n_items, 256, sm, st>>>(ps);
+    rcr_tile_kernel<TC, CG, R1, R2, SHC, BAL><<<n_items, 256, sm, st>>>(ps);
     FMM_CUDA_TRY(cudaGetLastError());
     return FMM_OK;
 }
@@ -435,6 +504,24 @@ int launch_rcr_pass(RcrList &Lst, RcrPass ps, cudaStream_t st)
     ps.g_dst = Lst.dst;
     const int p = ps.p;
     size_t sm = rcr_tile_smem(p, Lst.tc, Lst.shc);
+    if (Lst.bal) {
+        if (Lst.shc) {
+            switch (Lst.tc) {
+            case 64: return launch_tile<64, 16, 1, 1, true, true>(ps, Lst.n_items, sm, st);
+            case 32: return launch_tile<32, 8, 1, 1, true, true>(ps, Lst.n_items, sm, st);
+            default: break;
+            }
+        } else {
+            switch (Lst.tc) {
+            case 64: return launch_tile<64, 16, 1, 1, false, true>(ps, Lst.n_items, sm, st);
+            case 32: return launch_tile<32, 8, 1, 1, false, true>(ps, Lst.n_items, sm, st);
+            case 16: return launch_tile<16, 8, 1, 1, false, true>(ps, Lst.n_items, sm, st);
+            case 8: return launch_tile<8, 8, 2, 1, false, true>(ps, Lst.n_items, sm, st);
+            case 4: return launch_tile<4, 4, 2, 1, false, true>(ps, Lst.n_items, sm, st);
+            default: break;
+            }
+        }
+    }
     if (Lst.shc) {
         switch (Lst.tc) {
         case 64: return launch_tile<64, 16, 2, 1, true>(ps, Lst.n_items, sm, st);
@@ -572,11 +659,12 @@ int build_rcr_lists(Plan *P)
 } // namespace fmm
 
 namespace fmm {
-// Tile width per pass, chosen at plan creation by timing the candidates on this plan's own
-// lists and tables (one right-hand side): the default from pick_tile and a narrower tile --
-// 4 columns where the default is 8 (large p, few items per direction: more CTAs, two per
-// SM), half the width where it is 32 or 64.  The winner is kept; matvec results do not
-// depend on the choice beyond FP32 rounding.
+// Tile width and schedule per pass, chosen at plan creation by timing the candidates on this
+// plan's own lists and tables (one right-hand side): the default from pick_tile and a narrower
+// tile -- 4 columns where the default is 8 (large p, few items per direction: more CTAs, two
+// per SM), half the width where it is 32 or 64 -- each with the default and the balanced unit
+// schedule (BAL).  The winner is kept; matvec results do not depend on the choice beyond the
+// order of the FP32 atomic additions.
 int tune_rcr_tiles(Plan *P)
 {
     cudaEvent_t a, b;
@@ -590,15 +678,18 @@ int tune_rcr_tiles(Plan *P)
             RcrList &Lst = which == PASS_M2M ? L.m2m : which == PASS_M2L ? L.m2l : L.l2l;
             if (Lst.key_beg.empty() || Lst.key_beg.back() == 0) continue;
             int p = which == PASS_M2L ? L.p : P->lev[l - 1].p;
-            std::vector<std::pair<int, int>> cand = {{Lst.tc, Lst.shc}};
-            if (Lst.tc == 8) cand.push_back({4, 0});
-            if (Lst.tc >= 32) cand.push_back({Lst.tc / 2, rcr_tile_smem(p, Lst.tc / 2, 1) <= TWO_CTA_SMEM ? 1 : 0});
-            if (cand.size() < 2) continue;
+            std::vector<int3> cand = {{Lst.tc, Lst.shc, 0}};
+            if (Lst.tc == 8) cand.push_back({4, 0, 0});
+            if (Lst.tc >= 32) cand.push_back({Lst.tc / 2, rcr_tile_smem(p, Lst.tc / 2, 1) <= TWO_CTA_SMEM ? 1 : 0, 0});
+            // balanced variants exist for every width without staged blocks, and for 32 and 64 with
+            for (size_t i = 0, n0 = cand.size(); i < n0; i++)
+                if (cand[i].y == 0 || cand[i].x >= 32) cand.push_back({cand[i].x, cand[i].y, 1});
             float best = 1e30f;
-            std::pair<int, int> pick = cand[0];
+            int3 pick = cand[0];
             for (auto &c : cand) {
-                Lst.tc = c.first;
-                Lst.shc = c.second;
+                Lst.tc = c.x;
+                Lst.shc = c.y;
+                Lst.bal = c.z;
                 Lst.items_nrhs = 0;
                 float tot = 0.f;
                 for (int rep = 0; rep < 4 && rc == FMM_OK; rep++) {
@@ -616,8 +707,9 @@ int tune_rcr_tiles(Plan *P)
                     pick = c;
                 }
             }
-            Lst.tc = pick.first;
-            Lst.shc = pick.second;
+            Lst.tc = pick.x;
+            Lst.shc = pick.y;
+            Lst.bal = pick.z;
             Lst.items_nrhs = 0;
         }
     }

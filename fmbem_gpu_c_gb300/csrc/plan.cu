@@ -325,8 +325,12 @@ extern "C" int fmm_plan_info(const fmm_plan *plan, fmm_info *info)
         info->m2l_tensor[l] = P->opt.build_mixed && dense(L.m2l) ? 1 : 0;
         info->pass_dense[l] =
             P->opt.build_mixed ? (dense(L.m2m) ? 1 : 0) | (dense(L.m2l) ? 2 : 0) | (dense(L.l2l) ? 4 : 0) : 0;
-        if (P->opt.build_mixed)
+        if (P->opt.build_mixed) {
             info->pass_tc3[l] = (P->lev[l].m2m.t3.on ? 1 : 0) | (P->lev[l].m2l.t3.on ? 2 : 0) | (P->lev[l].l2l.t3.on ? 4 : 0);
+            // SIMT tiles with the balanced schedule: neither tensor-core form, and bal set
+            auto bal = [&](const RcrList &R) { return !R.t3.on && !dense(R) && R.bal; };
+            info->pass_balanced[l] = (bal(L.m2m) ? 1 : 0) | (bal(L.m2l) ? 2 : 0) | (bal(L.l2l) ? 4 : 0);
+        }
     }
     info->expansions_scaled = P->opt.build_mixed && P->scaled ? 1 : 0;
     info->num_near = P->num_near;

@@ -67,6 +67,7 @@ struct RcrList {
     int ndst_rank = 0;            // boxes of the destination level
     int n_items = 0, items_nrhs = 0;
     int tc = 8, shc = 0;          // columns per item; rotation/coaxial blocks staged in shared memory
+    int bal = 0;                  // balanced unit schedule (one-row units, boustrophedon order; plan passes only)
     Tc3 t3;                       // three-stage tensor-core form (used where t3.on)
     TcDense td;                   // dense tensor-core form (used where td.on)
 };

@@ -108,6 +108,9 @@ typedef struct {
                                             never, 1: wherever the orders allow); M2M and L2L only with
                                             FMMBEM_TENSOR_M2M=1 (about ten times the rounding error of
                                             the SIMT form) */
+    int pass_balanced[FMM_MAX_LEVEL + 1]; /* mixed path: SIMT-tile passes of level l that run the balanced
+                                            unit schedule (one-row units in boustrophedon order), same bits
+                                            as pass_tc3; chosen at plan creation by timing */
 } fmm_info;
 
 typedef struct fmm_plan fmm_plan;
