@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(256, 2) rcr_tile_kernel(RcrPass ps)
 // of a lockstep matvec): a grid of resident CTAs takes work items (pass, tile) from a device
 // queue, in the order given (longest first), until it is empty.  The queue head is an
 // atomic counter, zeroed before the launch; no CTA waits on another.
-template <int TC, int CG, int R1, int R2, bool SHC>
+template <int TC, int CG, int R1, int R2, bool SHC, bool BAL = false>
 __global__ void __launch_bounds__(256, 2) rcr_queue_kernel(const RcrPass *__restrict__ passes, const int *__restrict__ work_pass,
                                                            const int4 *__restrict__ work_item, const int *__restrict__ nwork,
                                                            int *head)
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(256, 2) rcr_queue_kernel(const RcrPass *__rest
         __syncthreads();
         const int w = s_w;
         if (w >= n) break;
-        rcr_tile<TC, CG, R1, R2, SHC>(passes[work_pass[w]], work_item[w], smem4, s_src, s_dst);
+        rcr_tile<TC, CG, R1, R2, SHC, BAL>(passes[work_pass[w]], work_item[w], smem4, s_src, s_dst);
         __syncthreads();
     }
 }
@@ -371,74 +371,97 @@ static int launch_tile(const RcrPass &ps, int n_items, size_t sm, cudaStream_t s
     return FMM_OK;
 }
 
-template <int TC, int CG, int R1, int R2, bool SHC>
-static const void *queue_fn()
-{
-    return (const void *)rcr_queue_kernel<TC, CG, R1, R2, SHC>;
-}
+// The tile shapes, as template arguments: Tile<TC, CG, R1, R2, SHC, BAL>
+template <int TC_, int CG_, int R1_, int R2_, bool SHC_, bool BAL_>
+struct Tile {
+    static constexpr int TC = TC_, CG = CG_, R1 = R1_, R2 = R2_;
+    static constexpr bool SHC = SHC_, BAL = BAL_;
+};
 
-template <int TC, int CG, int R1, int R2, bool SHC>
-static int queue_prep(size_t sm, int nwork, int *grid)
+// Calls f(Tile<...>{}) for the shape that serves (columns tc, staged blocks shc, schedule bal):
+// bal 0 the default schedule, 1 the balanced one with narrow column groups where they pay, 2 the
+// balanced one with the default groups; a (tc, shc, bal) without a balanced shape runs bal 0.
+template <class F>
+static int with_tile(int tc, int shc, int bal, F &&f)
 {
-    static size_t attr = 0;
-    const void *fn = queue_fn<TC, CG, R1, R2, SHC>();
-    int e = raise_smem_limit(fn, sm, &attr);
-    if (e) return e;
-    int dev = 0, nsm = 0, per_sm = 0;
-    FMM_CUDA_TRY(cudaGetDevice(&dev));
-    FMM_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    FMM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, sm));
-    *grid = std::max(1, std::min(nwork, nsm * std::max(per_sm, 1)));
-    return FMM_OK;
+    if (bal == 2) {
+        if (shc) {
+            if (tc == 32) return f(Tile<32, 16, 1, 1, true, true>{});
+        } else {
+            switch (tc) {
+            case 32: return f(Tile<32, 16, 1, 1, false, true>{});
+            case 16: return f(Tile<16, 16, 1, 1, false, true>{});
+            case 8: return f(Tile<8, 8, 1, 1, false, true>{});
+            case 4: return f(Tile<4, 4, 1, 1, false, true>{});
+            default: break;
+            }
+        }
+    }
+    if (bal == 1) {
+        if (shc) {
+            switch (tc) {
+            case 64: return f(Tile<64, 16, 1, 1, true, true>{});
+            case 32: return f(Tile<32, 8, 1, 1, true, true>{});
+            default: break;
+            }
+        } else {
+            switch (tc) {
+            case 64: return f(Tile<64, 16, 1, 1, false, true>{});
+            case 32: return f(Tile<32, 8, 1, 1, false, true>{});
+            case 16: return f(Tile<16, 8, 1, 1, false, true>{});
+            case 8: return f(Tile<8, 8, 2, 1, false, true>{});
+            case 4: return f(Tile<4, 4, 2, 1, false, true>{});
+            default: break;
+            }
+        }
+    }
+    if (shc) {
+        switch (tc) {
+        case 64: return f(Tile<64, 16, 2, 1, true, false>{});
+        case 32: return f(Tile<32, 16, 2, 1, true, false>{});
+        case 16: return f(Tile<16, 16, 2, 1, true, false>{});
+        default: return f(Tile<8, 8, 4, 2, true, false>{});
+        }
+    }
+    switch (tc) {
+    case 64: return f(Tile<64, 16, 2, 1, false, false>{});
+    case 32: return f(Tile<32, 16, 2, 1, false, false>{});
+    case 16: return f(Tile<16, 16, 2, 1, false, false>{});
+    case 4: return f(Tile<4, 4, 8, 4, false, false>{});
+    default: return f(Tile<8, 8, 4, 2, false, false>{});
+    }
 }
 
 // Raise the queue kernel's shared-memory limit and size its grid: every CTA resident at once
 // (SMs x CTAs per SM at this shared memory), no more than the items.
-int rcr_queue_prepare(int tc, int shc, size_t sm, int nwork, int *grid)
+int rcr_queue_prepare(int tc, int shc, int bal, size_t sm, int nwork, int *grid)
 {
-    if (shc) {
-        switch (tc) {
-        case 64: return queue_prep<64, 16, 2, 1, true>(sm, nwork, grid);
-        case 32: return queue_prep<32, 16, 2, 1, true>(sm, nwork, grid);
-        case 16: return queue_prep<16, 16, 2, 1, true>(sm, nwork, grid);
-        default: return queue_prep<8, 8, 4, 2, true>(sm, nwork, grid);
-        }
-    }
-    switch (tc) {
-    case 64: return queue_prep<64, 16, 2, 1, false>(sm, nwork, grid);
-    case 32: return queue_prep<32, 16, 2, 1, false>(sm, nwork, grid);
-    case 16: return queue_prep<16, 16, 2, 1, false>(sm, nwork, grid);
-    case 4: return queue_prep<4, 4, 8, 4, false>(sm, nwork, grid);
-    default: return queue_prep<8, 8, 4, 2, false>(sm, nwork, grid);
-    }
+    return with_tile(tc, shc, bal, [&](auto t) -> int {
+        using T = decltype(t);
+        static size_t attr = 0;
+        const void *fn = (const void *)rcr_queue_kernel<T::TC, T::CG, T::R1, T::R2, T::SHC, T::BAL>;
+        int e = raise_smem_limit(fn, sm, &attr);
+        if (e) return e;
+        int dev = 0, nsm = 0, per_sm = 0;
+        FMM_CUDA_TRY(cudaGetDevice(&dev));
+        FMM_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        FMM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, sm));
+        *grid = std::max(1, std::min(nwork, nsm * std::max(per_sm, 1)));
+        return FMM_OK;
+    });
 }
 
-#define QUEUE_LAUNCH(TC, CG, R1, R2, SHC) \
-    rcr_queue_kernel<TC, CG, R1, R2, SHC><<<grid, 256, sm, st>>>(passes, work_pass, work_item, nwork, head)
-
-int launch_rcr_queue(int tc, int shc, const RcrPass *passes, const int *work_pass, const int4 *work_item,
+int launch_rcr_queue(int tc, int shc, int bal, const RcrPass *passes, const int *work_pass, const int4 *work_item,
                      const int *nwork, int *head, size_t sm, int grid, cudaStream_t st)
 {
-    if (shc) {
-        switch (tc) {
-        case 64: QUEUE_LAUNCH(64, 16, 2, 1, true); break;
-        case 32: QUEUE_LAUNCH(32, 16, 2, 1, true); break;
-        case 16: QUEUE_LAUNCH(16, 16, 2, 1, true); break;
-        default: QUEUE_LAUNCH(8, 8, 4, 2, true); break;
-        }
-    } else {
-        switch (tc) {
-        case 64: QUEUE_LAUNCH(64, 16, 2, 1, false); break;
-        case 32: QUEUE_LAUNCH(32, 16, 2, 1, false); break;
-        case 16: QUEUE_LAUNCH(16, 16, 2, 1, false); break;
-        case 4: QUEUE_LAUNCH(4, 4, 8, 4, false); break;
-        default: QUEUE_LAUNCH(8, 8, 4, 2, false); break;
-        }
-    }
-    FMM_CUDA_TRY(cudaGetLastError());
-    return FMM_OK;
+    return with_tile(tc, shc, bal, [&](auto t) -> int {
+        using T = decltype(t);
+        rcr_queue_kernel<T::TC, T::CG, T::R1, T::R2, T::SHC, T::BAL><<<grid, 256, sm, st>>>(passes, work_pass, work_item,
+                                                                                         nwork, head);
+        FMM_CUDA_TRY(cudaGetLastError());
+        return FMM_OK;
+    });
 }
-#undef QUEUE_LAUNCH
 
 void rcr_list_items(const RcrList &Lst, std::vector<int4> &items) { build_items(Lst, 1, Lst.tc, 0, true, items); }
 
@@ -504,39 +527,10 @@ int launch_rcr_pass(RcrList &Lst, RcrPass ps, cudaStream_t st)
     ps.g_dst = Lst.dst;
     const int p = ps.p;
     size_t sm = rcr_tile_smem(p, Lst.tc, Lst.shc);
-    if (Lst.bal) {
-        if (Lst.shc) {
-            switch (Lst.tc) {
-            case 64: return launch_tile<64, 16, 1, 1, true, true>(ps, Lst.n_items, sm, st);
-            case 32: return launch_tile<32, 8, 1, 1, true, true>(ps, Lst.n_items, sm, st);
-            default: break;
-            }
-        } else {
-            switch (Lst.tc) {
-            case 64: return launch_tile<64, 16, 1, 1, false, true>(ps, Lst.n_items, sm, st);
-            case 32: return launch_tile<32, 8, 1, 1, false, true>(ps, Lst.n_items, sm, st);
-            case 16: return launch_tile<16, 8, 1, 1, false, true>(ps, Lst.n_items, sm, st);
-            case 8: return launch_tile<8, 8, 2, 1, false, true>(ps, Lst.n_items, sm, st);
-            case 4: return launch_tile<4, 4, 2, 1, false, true>(ps, Lst.n_items, sm, st);
-            default: break;
-            }
-        }
-    }
-    if (Lst.shc) {
-        switch (Lst.tc) {
-        case 64: return launch_tile<64, 16, 2, 1, true>(ps, Lst.n_items, sm, st);
-        case 32: return launch_tile<32, 16, 2, 1, true>(ps, Lst.n_items, sm, st);
-        case 16: return launch_tile<16, 16, 2, 1, true>(ps, Lst.n_items, sm, st);
-        default: return launch_tile<8, 8, 4, 2, true>(ps, Lst.n_items, sm, st);
-        }
-    }
-    switch (Lst.tc) {
-    case 64: return launch_tile<64, 16, 2, 1, false>(ps, Lst.n_items, sm, st);
-    case 32: return launch_tile<32, 16, 2, 1, false>(ps, Lst.n_items, sm, st);
-    case 16: return launch_tile<16, 16, 2, 1, false>(ps, Lst.n_items, sm, st);
-    case 4: return launch_tile<4, 4, 8, 4, false>(ps, Lst.n_items, sm, st);
-    default: return launch_tile<8, 8, 4, 2, false>(ps, Lst.n_items, sm, st);
-    }
+    return with_tile(Lst.tc, Lst.shc, Lst.bal, [&](auto t) -> int {
+        using T = decltype(t);
+        return launch_tile<T::TC, T::CG, T::R1, T::R2, T::SHC, T::BAL>(ps, Lst.n_items, sm, st);
+    });
 }
 
 // Shared memory that keeps two CTAs on an SM: 228 KB per SM, 1 KB reserved and the static
@@ -681,9 +675,12 @@ int tune_rcr_tiles(Plan *P)
             std::vector<int3> cand = {{Lst.tc, Lst.shc, 0}};
             if (Lst.tc == 8) cand.push_back({4, 0, 0});
             if (Lst.tc >= 32) cand.push_back({Lst.tc / 2, rcr_tile_smem(p, Lst.tc / 2, 1) <= TWO_CTA_SMEM ? 1 : 0, 0});
-            // balanced variants exist for every width without staged blocks, and for 32 and 64 with
-            for (size_t i = 0, n0 = cand.size(); i < n0; i++)
+            // balanced variants (1: narrow column groups where they pay, 2: the default groups, one-row
+            // units) exist for every width without staged blocks, and for 32 (and 64: 1 only) with
+            for (size_t i = 0, n0 = cand.size(); i < n0; i++) {
                 if (cand[i].y == 0 || cand[i].x >= 32) cand.push_back({cand[i].x, cand[i].y, 1});
+                if (cand[i].x <= 32 && (cand[i].y == 0 || cand[i].x == 32)) cand.push_back({cand[i].x, cand[i].y, 2});
+            }
             float best = 1e30f;
             int3 pick = cand[0];
             for (auto &c : cand) {

@@ -67,7 +67,7 @@ struct RcrList {
     int ndst_rank = 0;            // boxes of the destination level
     int n_items = 0, items_nrhs = 0;
     int tc = 8, shc = 0;          // columns per item; rotation/coaxial blocks staged in shared memory
-    int bal = 0;                  // balanced unit schedule (one-row units, boustrophedon order; plan passes only)
+    int bal = 0;                  // balanced unit schedule (1, 2: two tile shapes; one-row units, boustrophedon order)
     Tc3 t3;                       // three-stage tensor-core form (used where t3.on)
     TcDense td;                   // dense tensor-core form (used where td.on)
 };
@@ -259,11 +259,11 @@ void rcr_list_items(const RcrList &Lst, std::vector<int4> &out);
 // items for nrhs columns in tiles of `width`, ordered by destination Morton ranges where the
 // pass's expansions (ws_bytes) exceed L2
 void build_items(const RcrList &Lst, int nrhs, int width, size_t ws_bytes, bool coax_w, std::vector<int4> &items);
-// persistent work-queue launch over many passes of one tile shape (tc, shc); smem for the
-// largest order among them; grid from rcr_queue_prepare (resident CTAs)
-int rcr_queue_prepare(int tc, int shc, size_t smem, int nwork, int *grid);
+// persistent work-queue launch over many passes of one tile shape (tc, shc, schedule bal as in
+// RcrList); smem for the largest order among them; grid from rcr_queue_prepare (resident CTAs)
+int rcr_queue_prepare(int tc, int shc, int bal, size_t smem, int nwork, int *grid);
 // (*nwork: the number of items, read on the device)
-int launch_rcr_queue(int tc, int shc, const RcrPass *passes, const int *work_pass, const int4 *work_item,
+int launch_rcr_queue(int tc, int shc, int bal, const RcrPass *passes, const int *work_pass, const int4 *work_item,
                      const int *nwork, int *head, size_t smem, int grid, cudaStream_t st);
 
 } // namespace fmm

@@ -42,7 +42,7 @@ struct BodyDev {
 };
 
 struct QueueGroup {               // one persistent launch: the passes of one tile shape in a phase
-    int tc = 8, shc = 0, nwork = 0, head = 0, grid = 1;
+    int tc = 8, shc = 0, bal = 0, nwork = 0, head = 0, grid = 1;
     size_t smem = 0;
     int *work_pass = nullptr;         // the items of the switched-on plans (compacted per matvec)
     int4 *work_item = nullptr;
@@ -404,16 +404,17 @@ static int build_scene(Scene *S)
     // then L2L of levels 3..Lmax
     std::vector<RcrPass> passes;
     struct Work { int pass; int4 item; double cost; };
-    struct Key { int phase, tc, shc, cls; };
+    struct Key { int phase, tc, shc, bal, cls; };
     std::vector<Key> keys;
     std::vector<std::vector<Work>> work;
     std::vector<size_t> smem;
     // passes of one tile shape are grouped further by the CTAs per SM their shared memory
     // allows, so that a few high-order passes do not set the occupancy of all the others
-    auto group_of = [&](int phase, int tc, int shc, int cls) {
+    auto group_of = [&](int phase, int tc, int shc, int bal, int cls) {
         for (size_t g = 0; g < keys.size(); g++)
-            if (keys[g].phase == phase && keys[g].tc == tc && keys[g].shc == shc && keys[g].cls == cls) return (int)g;
-        keys.push_back({phase, tc, shc, cls});
+            if (keys[g].phase == phase && keys[g].tc == tc && keys[g].shc == shc && keys[g].bal == bal && keys[g].cls == cls)
+                return (int)g;
+        keys.push_back({phase, tc, shc, bal, cls});
         work.emplace_back();
         smem.push_back(0);
         return (int)keys.size() - 1;
@@ -432,7 +433,7 @@ static int build_scene(Scene *S)
                 int phase = which == PASS_M2M ? Lmax - l : which == PASS_M2L ? ph_m2l : ph_m2l + (l - 2);
                 size_t sm = rcr_tile_smem(ps.p, Lst->tc, Lst->shc);
                 int cls = sm <= 76 * 1024 ? 3 : sm <= 113 * 1024 ? 2 : 1;
-                int g = group_of(phase, Lst->tc, Lst->shc, cls);
+                int g = group_of(phase, Lst->tc, Lst->shc, Lst->bal, cls);
                 smem[g] = std::max(smem[g], sm);
                 int pi = (int)passes.size();
                 passes.push_back(ps);
@@ -482,11 +483,12 @@ static int build_scene(Scene *S)
         QueueGroup G;
         G.tc = keys[g].tc;
         G.shc = keys[g].shc;
+        G.bal = keys[g].bal;
         G.nwork = (int)W.size();
         G.head = (int)g;
         G.smem = smem[g];
         int st;
-        if ((st = rcr_queue_prepare(G.tc, G.shc, G.smem, G.nwork, &G.grid))) return st;
+        if ((st = rcr_queue_prepare(G.tc, G.shc, G.bal, G.smem, G.nwork, &G.grid))) return st;
         std::vector<int> own(W.size());
         for (size_t q = 0; q < W.size(); q++) own[q] = powner[wp[q]];
         int *wp_all = nullptr, *own_d = nullptr;
@@ -543,7 +545,7 @@ static int scene_translate(Scene *S)
         if (groups.empty()) continue;
         if (groups.size() == 1) {
             const QueueGroup &G = groups[0];
-            int e = launch_rcr_queue(G.tc, G.shc, S->passes, G.work_pass, G.work_item, S->counts + G.head,
+            int e = launch_rcr_queue(G.tc, G.shc, G.bal, S->passes, G.work_pass, G.work_item, S->counts + G.head,
                                      S->heads + G.head, G.smem, G.grid, st);
             if (e) return e;
             continue;
@@ -555,7 +557,7 @@ static int scene_translate(Scene *S)
         for (int q = 0; q < ns; q++) FMM_CUDA_TRY(cudaStreamWaitEvent(S->side[q], fork, 0));
         for (size_t g = 0; g < groups.size(); g++) {
             const QueueGroup &G = groups[g];
-            int e = launch_rcr_queue(G.tc, G.shc, S->passes, G.work_pass, G.work_item, S->counts + G.head,
+            int e = launch_rcr_queue(G.tc, G.shc, G.bal, S->passes, G.work_pass, G.work_item, S->counts + G.head,
                                      S->heads + G.head, G.smem, G.grid, S->side[g % SCENE_SIDE]);
             if (e) return e;
         }
