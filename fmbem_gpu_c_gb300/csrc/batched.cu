@@ -656,8 +656,8 @@ namespace fmm {
 // Tile width and schedule per pass, chosen at plan creation by timing the candidates on this
 // plan's own lists and tables (one right-hand side): the default from pick_tile and a narrower
 // tile -- 4 columns where the default is 8 (large p, few items per direction: more CTAs, two
-// per SM), half the width where it is 32 or 64 -- each with the default and the balanced unit
-// schedule (BAL).  The winner is kept; matvec results do not depend on the choice beyond the
+// per SM), half the width where it is 16, 32 or 64 -- each with the default and the balanced
+// unit schedule (BAL).  The winner is kept; matvec results do not depend on the choice beyond the
 // order of the FP32 atomic additions.
 int tune_rcr_tiles(Plan *P)
 {
@@ -674,6 +674,7 @@ int tune_rcr_tiles(Plan *P)
             int p = which == PASS_M2L ? L.p : P->lev[l - 1].p;
             std::vector<int3> cand = {{Lst.tc, Lst.shc, 0}};
             if (Lst.tc == 8) cand.push_back({4, 0, 0});
+            if (Lst.tc == 16) cand.push_back({8, 0, 0});
             if (Lst.tc >= 32) cand.push_back({Lst.tc / 2, rcr_tile_smem(p, Lst.tc / 2, 1) <= TWO_CTA_SMEM ? 1 : 0, 0});
             // balanced variants (1: narrow column groups where they pay, 2: the default groups, one-row
             // units) exist for every width without staged blocks, and for 32 (and 64: 1 only) with
