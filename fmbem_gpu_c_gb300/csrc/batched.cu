@@ -21,6 +21,7 @@
 // (L2L).
 #include "plan.h"
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 namespace fmm {
@@ -661,6 +662,17 @@ namespace fmm {
 // order of the FP32 atomic additions.
 int tune_rcr_tiles(Plan *P)
 {
+    // FMMBEM_TILE_BAL=0/1/2 forces one schedule on every pass (default tile width; a shape
+    // without that schedule runs the default one), for tests
+    if (const char *env = getenv("FMMBEM_TILE_BAL")) {
+        const int bal = std::max(0, std::min(2, atoi(env)));
+        for (int l = P->lmin; l <= P->lmax; l++)
+            for (RcrList *R : {&P->lev[l].m2m, &P->lev[l].m2l, &P->lev[l].l2l}) {
+                R->bal = bal;
+                R->items_nrhs = 0;
+            }
+        return FMM_OK;
+    }
     cudaEvent_t a, b;
     FMM_CUDA_TRY(cudaEventCreate(&a));
     FMM_CUDA_TRY(cudaEventCreate(&b));

@@ -991,7 +991,7 @@ orc_fmm *orc_fmm_create(int nv, const double *V, int nf, const int *F, double k,
     for (int e = 0; e < nf; e++) f->leaf_beg[elem_leaf[e] + 1]++;
     for (int i = 0; i < LL->nb; i++) f->leaf_beg[i + 1] += f->leaf_beg[i];
     {
-        int *fill = (int *)calloc(LL->nb, sizeof(int));
+        int *fill = (int *)calloc((size_t)LL->nb + 1, sizeof(int));
         for (int e = 0; e < nf; e++) f->leaf_elem[f->leaf_beg[elem_leaf[e]] + fill[elem_leaf[e]]++] = e;
         free(fill);
     }
