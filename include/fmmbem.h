@@ -225,7 +225,8 @@ int fmm_scene_set_active(fmm_scene *scene, const int *on);
 int fmm_scene_solve(fmm_scene *scene, const cuDoubleComplex *b, cuDoubleComplex *x, double tol, int maxit,
                     int restart, int precision, int *iters, double *relres);
 /* The last fmm_scene_solve: wall seconds, and the device time (ms) and count of its mixed and
- * FP64 scene matvecs (CUDA events around each); the rest is the Krylov vector work and the
+ * FP64-quality scene matvecs (the refinement's residuals: FMM_FLOAT2 by default, FMM_FP64 with
+ * FMMBEM_FF_RESIDUAL=0; CUDA events around each); the rest is the Krylov vector work and the
  * host.  Any pointer may be NULL. */
 int fmm_scene_timings(const fmm_scene *scene, double *solve_s, double *mixed_ms, int *mixed_calls, double *fp64_ms,
                       int *fp64_calls);
