@@ -98,9 +98,10 @@ static __device__ __forceinline__ void cmac(float2 &acc, float2 c, float ar, flo
 // the threads.  BAL takes them in boustrophedon order (t, 2B - 1 - t, 2B + t, ...), so a thread
 // that drew a long unit in one round draws a short one in the next, ranks the column groups
 // inside each cost class, and gives +m and -m of the coaxial stage units of their own; with
-// one-row units (R1 = R2 = 1) the busiest thread is within about 10 % of the average at
-// p = 20-40, against about 55 % above it.  Every output is still summed in the same order, so
-// the results do not depend on BAL, R1 or R2.
+// one- or two-row units the busiest thread does about 1.05-1.15 times the average work at
+// p = 20-40 (counting each unit's FMAs and loads), against about 1.8 times with the default
+// schedule.  Every output is still summed in the same order, so the results do not depend on
+// BAL, R1 or R2.
 template <int TC, int CG, int R1, int R2, bool SHC, bool BAL = false>
 static __device__ __forceinline__ void rcr_tile(const RcrPass &ps, const int4 it, float4 *smem4, int *s_src, int *s_dst)
 {
